@@ -1,0 +1,340 @@
+"""Benchmark: body-steps/s of the full rigid-body step on GB300.
+
+Workload (default): 1024 independent joint + contact scenes (body counts
+log-uniform in [16, 2048], rope / ball-socket / spring chains and loose boxes
+on the ground), dt 1/60, 10 AVBD iterations, packed into one device world
+and stepped by dio_step (broad -> narrow -> rows + warm start -> solve).
+
+One JSON line on rank 0:
+  value      body-steps/s with the world resident in HBM (CUDA events on the
+             library's stream, K steps, max over ranks)
+  e2e        the same metric through the public API with host buffers: every
+             step re-uploads poses + state (dio_world_set_state) and reads
+             poses + state back (dio_world_download)
+  plain      the one-scene-per-launch path (one context per scene) on a
+             sample of scenes, for the batched-vs-plain ratio
+  roofline   the primal kernel: algorithmic bytes per launch / event time
+  cpu_baseline  the CPU oracle (OpenMP over bodies / rows) on a sample
+--impl reference times the CPU restatement of the reference path (the
+reference is Rust + Vulkan and cannot run on the GPU machine).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "body-steps/s at 10 iters, batched vs plain on 1 GB300; max pos err vs FP64 (m)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--scenes", type=int, default=1024)
+    ap.add_argument("--plain-scenes", type=int, default=128)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-f64", action="store_true")
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.samples = []
+        self.idx = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for s in self.samples:
+            for k, nm in enumerate(names):
+                if len(s) > 5 + k and s[5 + k].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+def measured_hbm_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def world_capacity(sc):
+    from diomedes_gb300 import compute
+
+    n = sc.n
+    return compute.capacity(n, max_pairs=max(1024, 12 * n), max_contacts=max(4096, 40 * n),
+                            max_joints=max(1, len(sc.constraints)), max_scenes=sc.n_scenes,
+                            max_hull_vertices=max(1, 0 if sc.hull_vertices is None else len(sc.hull_vertices)))
+
+
+def primal_bytes(n_dyn, m, j_inc):
+    """Compulsory bytes of one primal launch (SoA FP32 model): per dynamic body
+    132 B (snapshot, initial, inertial, inverse mass/moment, CSR offset, new
+    pose), per contact row 108 B + two 4-byte CSR entries, per joint
+    incidence 44 B + 4 B."""
+    return 132 * n_dyn + (108 + 8) * m + 48 * j_inc
+
+
+def run_cpu(sc, steps, warmup, threads, budget_s=20.0):
+    """CPU oracle (f32) on a scene: body-steps/s."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as O
+
+    w = O.World(sc, threads=threads)
+    w.step(sc.options, warmup)
+    t0 = time.perf_counter()
+    done = 0
+    while done < steps:
+        w.step(sc.options, 1)
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return sc.n * done / dt, done, dt
+
+
+def sample_scenes(scenes_mod, sc, count):
+    """The first `count` scenes of a packed batch as their own world."""
+    off = sc.scene_offsets
+    count = min(count, len(off) - 1)
+    hi = int(off[count])
+    cons = sc.constraints[(sc.constraints["a"] < hi)]
+    return scenes_mod.Scene(f"{sc.name}[:{count}]", sc.bodies[:hi].copy(), sc.state[:hi].copy(), constraints=cons,
+                            scene_offsets=off[: count + 1].copy(), containers=sc.containers[:count],
+                            options=sc.options, steps=sc.steps)
+
+
+def reference_arm(args, rank):
+    from diomedes_gb300 import scenes
+
+    if rank != 0:
+        return
+    sc = scenes.batched(n_scenes=args.scenes)
+    sample = sample_scenes(scenes, sc, 64)
+    threads = os.cpu_count() or 1
+    v, done, dt = run_cpu(sample, max(1, args.steps), max(1, min(args.warmup, 3)), threads, budget_s=60.0)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "body-steps/s", "n_gpus": args.gpus,
+        "steps": done, "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(1, done), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"batched {args.scenes} scenes (joints + contacts), 10 iterations",
+                   "sample": f"first 64 scenes, {sample.n} bodies"},
+        "cpu_baseline": {"value": v, "unit": "body-steps/s", "cores": threads, "kind": "port",
+                         "sample": f"first 64 of {args.scenes} scenes ({sample.n} bodies), {done} steps"},
+        "e2e": {"value": v, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_info()
+    if args.impl == "reference":
+        return reference_arm(args, rank)
+
+    import torch
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+
+    from diomedes_gb300 import compute, scenes
+
+    sc = scenes.batched(n_scenes=args.scenes, seed=4 + 1000 * rank)
+    stream = torch.cuda.current_stream()
+    w = compute.World(world_capacity(sc), profile=1)
+    w.set_stream(stream.cuda_stream)
+    w.upload(sc.bodies, sc.state, **sc.upload_kwargs())
+    o = sc.options
+    w.step(o, args.warmup)
+    torch.cuda.synchronize()
+    w.reset_timers()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(local) as clk:
+        e0.record(stream)
+        w.step(o, args.steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ms = e0.elapsed_time(e1)
+    st = w.stats()
+    t = torch.tensor([ms], device="cuda")
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    n_dyn = int((sc.state["inv_mass"] != 0).sum())
+    total_bodies = sc.n * world
+    value = total_bodies * args.steps / (ms_max / 1e3)
+
+    # roofline of the primal kernel (event-timed on the launching stream)
+    peak, peak_kind = measured_hbm_peak()
+    prim_ms = st["primal_ms"] / max(1, st["primal_launches"])
+    j_inc = 2 * len(sc.constraints)
+    pb = primal_bytes(n_dyn, st["contacts"], j_inc)
+    achieved = pb / (prim_ms / 1e3) / 1e9 if prim_ms > 0 else None
+
+    # end to end through the public API with host buffers
+    e2e = None
+    if not args.no_e2e:
+        hb = np.zeros(sc.n, sc.bodies.dtype)
+        hs = np.zeros(sc.n, sc.state.dtype)
+        w.download_into(hb, hs)
+        k2 = max(3, args.steps // 2)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(k2):
+            w.set_state(hb, hs)
+            w.step(o, 1)
+            w.download_into(hb, hs)
+        t1 = time.perf_counter()
+        e2e = {"value": total_bodies * k2 / (t1 - t0), "unit": "body-steps/s",
+               "h2d_bytes_per_step": int(hb.nbytes + hs.nbytes), "d2h_bytes_per_step": int(hb.nbytes + hs.nbytes),
+               "steps": k2}
+
+    # plain path: one context per scene, stepped one scene at a time
+    plain = None
+    if not args.no_plain and rank == 0:
+        idx = np.linspace(0, sc.n_scenes - 1, min(args.plain_scenes, sc.n_scenes)).astype(int)
+        worlds, nb = [], 0
+        for s in idx:
+            lo, hi = int(sc.scene_offsets[s]), int(sc.scene_offsets[s + 1])
+            cmask = (sc.constraints["a"] >= lo) & (sc.constraints["a"] < hi)
+            cons = sc.constraints[cmask].copy()
+            cons["a"] -= lo
+            cons["b"] -= lo
+            one = scenes.Scene("one", sc.bodies[lo:hi], sc.state[lo:hi], constraints=cons,
+                               containers=[sc.containers[s]], options=o)
+            pw = compute.World(world_capacity(one))
+            pw.set_stream(stream.cuda_stream)
+            pw.upload(one.bodies, one.state, **one.upload_kwargs())
+            worlds.append(pw)
+            nb += one.n
+        for pw in worlds:
+            pw.step(o, 2)
+        torch.cuda.synchronize()
+        kp = 3
+        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
+        for _ in range(kp):
+            for pw in worlds:
+                pw.step(o, 1)
+        p1.record(stream)
+        torch.cuda.synchronize()
+        pv = nb * kp / (p0.elapsed_time(p1) / 1e3)
+        plain = {"value": pv, "unit": "body-steps/s", "sample": f"{len(idx)} of {sc.n_scenes} scenes ({nb} bodies)",
+                 "batched_over_plain": value / world / pv}
+        for pw in worlds:
+            pw.close()
+
+    # max position error vs the all-FP64 world after the same steps
+    f64 = None
+    if not args.no_f64 and rank == 0:
+        b32, _ = w.download()
+        steps_done = args.warmup + args.steps
+        wf = compute.World(world_capacity(sc), precision=2)
+        wf.upload(sc.bodies, sc.state, **sc.upload_kwargs())
+        wf.step(o, steps_done)
+        p64, _ = wf.download_f64()
+        err = np.abs(b32["position"][:, :3].astype(np.float64) - p64).max(axis=1)
+        f64 = {"max_pos_err_m": float(err.max()), "median_pos_err_m": float(np.median(err)), "steps": steps_done}
+        wf.close()
+
+    cpu = None
+    if not args.no_cpu and rank == 0:
+        sample = sample_scenes(scenes, sc, 32)
+        threads = os.cpu_count() or 1
+        v, done, dt = run_cpu(sample, 5, 1, threads, budget_s=20.0)
+        cpu = {"value": v, "unit": "body-steps/s", "cores": threads, "kind": "port",
+               "sample": f"first 32 of {sc.n_scenes} scenes ({sample.n} bodies), {done} steps after 1 warm-up"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"batched {sc.n_scenes} scenes (rope / ball-socket / spring chains + loose "
+                                   f"boxes), {sc.n} bodies per GPU, dt 1/60, 10 iterations",
+                       "bodies_per_gpu": sc.n, "contacts_last_step": st["contacts"],
+                       "pairs_last_step": st["pairs"], "joints": len(sc.constraints),
+                       "l2": "working set > L2 (129 MB): poses, rows and CSR re-read every iteration",
+                       "parallelism": f"scene-sharded x{world}"},
+            "e2e": e2e, "plain": plain, "fp64_error": f64,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak if achieved else None, "traffic": None,
+                         "kernel": "k_primal", "bytes_per_launch": pb, "avg_launch_ms": prim_ms,
+                         "peak_kind": peak_kind},
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "gpu_launches": st["kernel_launches"],
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

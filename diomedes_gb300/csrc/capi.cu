@@ -1,0 +1,281 @@
+// capi.cu -- the extern "C" boundary declared in include/dio_cuda.h.
+//
+// A DioCtx owns a CUDA stream and up to two engines: an FP32 engine behind
+// the reference-mirror calls (created on first use, as the reference's
+// Renderer creates NarrowPhaseCompute / AvbdCompute lazily,
+// engine/src/render/renderer.rs:80-81,140-141) and a world engine of the
+// configured precision behind dio_world_* / dio_step.
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <mutex>
+#include <string>
+
+#include "../../include/dio_cuda.h"
+#include "engine_base.h"
+
+struct DioCtx {
+    DioCapacity cap{};
+    DioConfig cfg{};
+    cudaStream_t stream = nullptr;  // the stream calls are ordered on
+    cudaStream_t own = nullptr;     // the stream this context created
+    std::unique_ptr<dio::EngineBase> api;
+    std::unique_ptr<dio::EngineBase> world;
+    uint32_t world_precision = 0xFFFFFFFFu;
+    std::string last_error;
+};
+
+namespace {
+
+DioConfig default_config() {
+    DioConfig c{};
+    c.solver_mode = DIO_SOLVER_JACOBI;
+    c.precision = DIO_PREC_F32;
+    c.contacts_per_pair = DIO_CONTACTS_PER_PAIR;
+    c.use_graph = 0;
+    c.primal_group = 1;
+    c.block_size = 128;
+    c.batched_solver = 0;
+    return c;
+}
+
+int fail(DioCtx* ctx, int rc, const std::string& msg) {
+    if (ctx) ctx->last_error = msg;
+    return rc;
+}
+
+int api_engine(DioCtx* ctx, dio::EngineBase** out) {
+    if (!ctx->api) {
+        DioConfig c = ctx->cfg;
+        c.precision = DIO_PREC_F32;
+        dio::EngineBase* e = dio::make_engine_f32(ctx->cap, ctx->stream, c);
+        if (!e) return fail(ctx, DIO_ERR_CUDA, "failed to allocate the FP32 engine");
+        ctx->api.reset(e);
+    }
+    *out = ctx->api.get();
+    return DIO_OK;
+}
+
+int world_engine(DioCtx* ctx, bool create, dio::EngineBase** out) {
+    if (!ctx->world || (create && ctx->world_precision != ctx->cfg.precision)) {
+        if (!create) return fail(ctx, DIO_ERR_STATE, "no world uploaded");
+        ctx->world.reset();
+        dio::EngineBase* e = nullptr;
+        switch (ctx->cfg.precision) {
+            case DIO_PREC_F32:
+                e = dio::make_engine_f32(ctx->cap, ctx->stream, ctx->cfg);
+                break;
+            case DIO_PREC_SPLIT:
+                e = dio::make_engine_split(ctx->cap, ctx->stream, ctx->cfg);
+                break;
+            case DIO_PREC_F64:
+                e = dio::make_engine_f64(ctx->cap, ctx->stream, ctx->cfg);
+                break;
+            default:
+                return fail(ctx, DIO_ERR_INVALID, "unknown precision");
+        }
+        if (!e) return fail(ctx, DIO_ERR_CUDA, "failed to allocate the world engine");
+        ctx->world.reset(e);
+        ctx->world_precision = ctx->cfg.precision;
+    }
+    *out = ctx->world.get();
+    return DIO_OK;
+}
+
+template <class F>
+int with_api(DioCtx* ctx, F&& f) {
+    if (!ctx) return DIO_ERR_INVALID;
+    dio::EngineBase* e = nullptr;
+    int rc = api_engine(ctx, &e);
+    if (rc) return rc;
+    e->err.clear();
+    rc = f(e);
+    if (rc) ctx->last_error = e->err;
+    return rc;
+}
+
+template <class F>
+int with_world(DioCtx* ctx, bool create, F&& f) {
+    if (!ctx) return DIO_ERR_INVALID;
+    dio::EngineBase* e = nullptr;
+    int rc = world_engine(ctx, create, &e);
+    if (rc) return rc;
+    e->err.clear();
+    rc = f(e);
+    if (rc) ctx->last_error = e->err;
+    return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dio_ctx_create(const DioCapacity* capacity, DioCtx** out) {
+    if (!capacity || !out) return DIO_ERR_INVALID;
+    *out = nullptr;
+    if (capacity->max_bodies >= 0x7FFFFFFFu) return DIO_ERR_INVALID;
+    int dev_count = 0;
+    if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0) return DIO_ERR_CUDA;
+    auto* ctx = new DioCtx();
+    ctx->cap = *capacity;
+    if (ctx->cap.max_scenes == 0) ctx->cap.max_scenes = 1;
+    ctx->cfg = default_config();
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete ctx;
+        return DIO_ERR_CUDA;
+    }
+    ctx->own = ctx->stream;
+    *out = ctx;
+    return DIO_OK;
+}
+
+int dio_ctx_destroy(DioCtx* ctx) {
+    if (!ctx) return DIO_ERR_INVALID;
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    ctx->api.reset();
+    ctx->world.reset();
+    if (ctx->own) cudaStreamDestroy(ctx->own);
+    delete ctx;
+    return DIO_OK;
+}
+
+const char* dio_status_string(int status) {
+    switch (status) {
+        case DIO_OK:
+            return "ok";
+        case DIO_ERR_INVALID:
+            return "invalid argument";
+        case DIO_ERR_CAPACITY:
+            return "capacity exceeded";
+        case DIO_ERR_TIMEOUT:
+            return "device wait timed out";
+        case DIO_ERR_CUDA:
+            return "CUDA error";
+        case DIO_ERR_NONFINITE:
+            return "non-finite state";
+        case DIO_ERR_STATE:
+            return "invalid call order";
+        default:
+            return "unknown status";
+    }
+}
+
+const char* dio_ctx_last_error(const DioCtx* ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+int dio_ctx_configure(DioCtx* ctx, const DioConfig* config) {
+    if (!ctx || !config) return DIO_ERR_INVALID;
+    if (config->solver_mode > DIO_SOLVER_COLORED) return fail(ctx, DIO_ERR_INVALID, "unknown solver mode");
+    if (config->precision > DIO_PREC_F64) return fail(ctx, DIO_ERR_INVALID, "unknown precision");
+    if (config->contacts_per_pair != 4 && config->contacts_per_pair != 8)
+        return fail(ctx, DIO_ERR_INVALID, "contacts_per_pair must be 4 or 8");
+    bool realloc = config->contacts_per_pair > ctx->cfg.contacts_per_pair;
+    ctx->cfg = *config;
+    if (realloc) {
+        ctx->api.reset();
+        ctx->world.reset();
+        ctx->world_precision = 0xFFFFFFFFu;
+    }
+    if (ctx->api) ctx->api->set_config(*config);
+    if (ctx->world && ctx->world_precision == config->precision) ctx->world->set_config(*config);
+    return DIO_OK;
+}
+
+int dio_ctx_get_config(const DioCtx* ctx, DioConfig* out) {
+    if (!ctx || !out) return DIO_ERR_INVALID;
+    *out = ctx->cfg;
+    return DIO_OK;
+}
+
+int dio_ctx_set_stream(DioCtx* ctx, void* cuda_stream) {
+    if (!ctx) return DIO_ERR_INVALID;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(cuda_stream);
+    if (!s) s = ctx->own;
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    ctx->stream = s;  // engines created later use it too
+    if (ctx->api) ctx->api->set_stream(s);
+    if (ctx->world) ctx->world->set_stream(s);
+    return DIO_OK;
+}
+
+int dio_ctx_synchronize(DioCtx* ctx) {
+    if (!ctx) return DIO_ERR_INVALID;
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    return e == cudaSuccess ? DIO_OK : fail(ctx, DIO_ERR_CUDA, cudaGetErrorString(e));
+}
+
+int dio_broad_submit(DioCtx* ctx, const DioGpuBody* bodies, uint32_t n) {
+    return with_api(ctx, [&](dio::EngineBase* e) { return e->broad_submit(bodies, n); });
+}
+int dio_broad_pair_count(DioCtx* ctx, uint32_t* count) {
+    return with_api(ctx, [&](dio::EngineBase* e) { return e->pair_count(count); });
+}
+int dio_read_pairs(DioCtx* ctx, DioPair* out, uint32_t cap, uint32_t* n) {
+    return with_api(ctx, [&](dio::EngineBase* e) { return e->read_pairs(out, cap, n); });
+}
+int dio_narrow_submit_pairs(DioCtx* ctx, const DioGpuBody* bodies, uint32_t n, const DioPair* pairs,
+                            uint32_t n_pairs) {
+    return with_api(ctx, [&](dio::EngineBase* e) { return e->narrow_submit_pairs(bodies, n, pairs, n_pairs); });
+}
+int dio_narrow_submit(DioCtx* ctx, uint32_t pair_count) {
+    return with_api(ctx, [&](dio::EngineBase* e) { return e->narrow_submit(pair_count); });
+}
+int dio_narrow_read(DioCtx* ctx, DioContactOut* out, uint32_t cap, uint32_t* n) {
+    return with_api(ctx, [&](dio::EngineBase* e) { return e->narrow_read(out, cap, n); });
+}
+int dio_set_hull_vertices(DioCtx* ctx, const float* xyzw, uint32_t count) {
+    return with_api(ctx, [&](dio::EngineBase* e) { return e->set_hull(xyzw, count); });
+}
+
+int dio_prepare_contacts(DioCtx* ctx, const DioGpuBody* bodies, const DioBodyState* state, uint32_t n,
+                         const DioContactOut* slots, uint32_t n_slots, const DioContact* prev, uint32_t n_prev,
+                         const DioContainer* container, const DioAvbdOptions* options, DioContact* out, uint32_t cap,
+                         uint32_t* m, uint32_t* offsets, uint32_t* indices, uint32_t index_cap) {
+    if (!m || !offsets || (cap && !out)) return fail(ctx, DIO_ERR_INVALID, "null output");
+    return with_api(ctx, [&](dio::EngineBase* e) {
+        return e->prepare_contacts(bodies, state, n, slots, n_slots, prev, n_prev, container, options, out, cap, m,
+                                   offsets, indices, index_cap);
+    });
+}
+
+int dio_avbd_submit(DioCtx* ctx, const DioBodyState* state, const float* positions, const float* orientations,
+                    uint32_t n, const DioContact* contacts, uint32_t m, const DioConstraint* constraints,
+                    uint32_t n_constraints, const uint32_t* offsets, const uint32_t* indices,
+                    const DioRunOptions* options) {
+    return with_api(ctx, [&](dio::EngineBase* e) {
+        return e->avbd_submit(state, positions, orientations, n, contacts, m, constraints, n_constraints, offsets,
+                              indices, options);
+    });
+}
+int dio_avbd_read(DioCtx* ctx, const DioAvbdResult* out) {
+    return with_api(ctx, [&](dio::EngineBase* e) { return e->avbd_read(out); });
+}
+
+int dio_world_upload(DioCtx* ctx, const DioWorldDesc* desc) {
+    return with_world(ctx, true, [&](dio::EngineBase* e) { return e->world_upload(desc); });
+}
+int dio_step(DioCtx* ctx, const DioAvbdOptions* options, uint32_t steps) {
+    return with_world(ctx, false, [&](dio::EngineBase* e) { return e->step(options, steps); });
+}
+int dio_world_set_state(DioCtx* ctx, const DioGpuBody* bodies, const DioBodyState* state) {
+    return with_world(ctx, false, [&](dio::EngineBase* e) { return e->set_state(bodies, state); });
+}
+int dio_world_download(DioCtx* ctx, DioGpuBody* bodies, DioBodyState* state) {
+    return with_world(ctx, false, [&](dio::EngineBase* e) { return e->download(bodies, state); });
+}
+int dio_world_download_f64(DioCtx* ctx, double* positions, double* orientations) {
+    return with_world(ctx, false, [&](dio::EngineBase* e) { return e->download_f64(positions, orientations); });
+}
+int dio_world_contacts(DioCtx* ctx, DioContact* out, uint32_t cap, uint32_t* m) {
+    return with_world(ctx, false, [&](dio::EngineBase* e) { return e->contacts(out, cap, m); });
+}
+int dio_world_colors(DioCtx* ctx, uint32_t* out, uint32_t cap, uint32_t* n) {
+    return with_world(ctx, false, [&](dio::EngineBase* e) { return e->colors(out, cap, n); });
+}
+int dio_world_stats(DioCtx* ctx, DioStepStats* out) {
+    return with_world(ctx, false, [&](dio::EngineBase* e) { return e->stats(out); });
+}
+int dio_world_reset_timers(DioCtx* ctx) {
+    return with_world(ctx, false, [&](dio::EngineBase* e) { return e->reset_timers(); });
+}
+
+}  // extern "C"

@@ -1,0 +1,181 @@
+// engine.cuh -- device buffer layout and per-phase launch entry points.
+//
+// HBM layout (structure of arrays, one slot per body / pair / row, sized by
+// the context capacities):
+//   bodies   pos[2], rot[2]       ping-pong pose buffers (Jacobi parity)
+//            init_pos, init_rot   pose at step start       (avbd_init)
+//            inert_pos, inert_rot inertial target           (avbd_init)
+//            vel, ang, prev_vel   velocities
+//            inv                  inverse moment xyz, inverse mass in w
+//            shape                DioShape (80 B, the reference GpuShape)
+//            scene                scene index of the body
+//   pairs    DioPair list sorted by (a, b), count in counters
+//   slots    narrow-phase output, `per_pair` slots per pair
+//   rows     RowStatic (80 B at FP32) + RowDual (penalty, lambda) + (a, b)
+//   CSR      row_off[n+1], row_idx[2m] (row), row_oth[2m] (other body | B flag)
+//   joints   DioConstraint records + per-body joint CSR
+// Pose arrays use P (float or double), everything else R.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/dio_cuda.h"
+#include "dio_math.cuh"
+
+namespace dio {
+
+constexpr uint32_t kContainer = 0xFFFFFFFFu;
+constexpr uint32_t kIsB = 0x80000000u;  // row_oth flag: this body is `b`
+
+// error_flags bits (device counters)
+enum : uint32_t {
+    kErrPairOverflow = 1u << 0,
+    kErrRowOverflow = 1u << 1,
+    kErrEpaFaces = 1u << 2,
+    kErrEpaHorizon = 1u << 3,
+    kErrTimeout = 1u << 4,
+    kErrNonFinite = 1u << 5,
+    kErrIndexOverflow = 1u << 6,
+    kErrColorOverflow = 1u << 7,
+    kErrBadIndex = 1u << 8,
+};
+
+struct Counters {
+    uint32_t pairs;           // candidate pairs found (may exceed capacity)
+    uint32_t rows;            // total contact rows
+    uint32_t pair_rows;       // rows from narrow-phase slots
+    uint32_t container_rows;  // rows against containers
+    uint32_t gjk_work;        // pairs routed to GJK
+    uint32_t epa_work;        // pairs routed to EPA
+    uint32_t error_flags;
+    uint32_t colors;
+    uint32_t color_remaining;
+    uint32_t scene_cursor;
+    uint32_t pad[6];
+};
+
+// Static part of one contact row (80 B at R = float):
+//   n.xyz normal, n.w friction; t1.xyz, t1.w = c0.z; t2.xyz;
+//   ra.xyz r_a (body frame), ra.w = c0.x; rb.xyz r_b, rb.w = c0.y
+template <class R>
+struct RowStatic {
+    A4<R> n, t1, t2, ra, rb;
+};
+template <class P, class R>
+struct RowDual {
+    A4<R> penalty;  // xyz
+    A4<P> lambda;   // xyz
+};
+
+// Narrow-phase slot; at R = float its bytes are exactly DioContactOut.
+template <class R>
+struct Slot {
+    uint32_t valid, a, b, pad;
+    A4<R> normal;
+    R depth, pad2[3];
+    A4<R> pa, pb;
+};
+
+// One scene of a packed world.
+struct SceneDesc {
+    uint32_t body_lo, body_hi;
+    uint32_t has_container, pad;
+    float center[3], half_extent;
+    float rotation[4];
+};
+
+template <class P, class R>
+struct DevWorld {
+    uint32_t n;  // bodies
+    // poses
+    A4<P>* pos[2];
+    A4<P>* rot[2];
+    A4<P>* init_pos;
+    A4<P>* init_rot;
+    A4<P>* inert_pos;
+    A4<P>* inert_rot;
+    A4<P>* vel;
+    A4<P>* ang;
+    A4<P>* prev_vel;
+    A4<R>* inv;  // inv_moment xyz, inv_mass w
+    R* friction;
+    DioShape* shape;
+    uint32_t* scene;
+    A4<P>* origin;  // per-scene detection origin (split precision rebase)
+    const A4<R>* hull;  // hull vertex pool
+    // broad phase
+    A4<R>* aabb_min;
+    A4<R>* aabb_max;
+    DioPair* pairs;
+    uint32_t max_pairs;
+    // narrow phase
+    Slot<R>* slots;
+    uint32_t per_pair;
+    uint32_t* gjk_list;
+    A4<R>* simplex;   // 8 x A4 per EPA entry (4 points, 4 witnesses)
+    uint32_t* epa_list;
+    // rows
+    RowStatic<R>* rs;
+    RowDual<P, R>* rd;
+    uint2* ab;
+    uint32_t max_rows;
+    uint32_t* row_off;
+    uint32_t* row_idx;
+    uint32_t* row_oth;
+    uint32_t max_incid;
+    // joints
+    const DioConstraint* joints;
+    uint32_t n_joints;
+    const uint32_t* joint_off;
+    const uint32_t* joint_idx;
+    // colouring
+    uint32_t* color;
+    uint32_t* color_order;  // bodies sorted by colour
+    uint32_t* color_off;    // colour -> first index in color_order
+    // scenes
+    const SceneDesc* scenes;
+    uint32_t n_scenes;
+    Counters* ctr;
+};
+
+// Solver parameters shared by init / primal / dual / recover
+// (AvbdPush, engine/src/render/gpu_physics.rs:61-71).
+template <class R>
+struct SolveParams {
+    R dt;
+    R gx, gy, gz;
+    R alpha;
+    R beta_lin;
+    R penalty_max;
+    uint32_t iterations;
+};
+
+template <class R>
+struct PrepParams {
+    R dt;
+    R margin;
+    R penalty_min;
+    R penalty_max;
+    R alpha_gamma;  // alpha * gamma, rounded in R
+    R gamma;
+    R friction;
+};
+
+inline int grid_for(uint64_t n, int block, int max_blocks = 1 << 20) {
+    uint64_t g = (n + block - 1) / block;
+    if (g < 1) g = 1;
+    if (g > (uint64_t)max_blocks) g = max_blocks;
+    return (int)g;
+}
+
+// ---- launch entry points (explicitly instantiated per precision) ----
+template <class P, class R>
+void launch_aabb(const DevWorld<P, R>& w, uint32_t lo, uint32_t hi, cudaStream_t s);
+template <class P, class R>
+void launch_broad_dense(const DevWorld<P, R>& w, uint32_t lo, uint32_t hi, uint32_t* counts, uint32_t* offsets,
+                        void* scan_tmp, size_t scan_tmp_bytes, cudaStream_t s);
+template <class P, class R>
+void launch_narrow(const DevWorld<P, R>& w, uint32_t pair_lo, uint32_t pair_hi, cudaStream_t s);
+
+}  // namespace dio

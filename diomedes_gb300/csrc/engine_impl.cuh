@@ -1,0 +1,1182 @@
+// engine_impl.cuh -- one engine instance: device buffers and the step
+// pipeline, templated on pose precision P and arithmetic precision R.
+// Included by exactly one translation unit per precision.
+#pragma once
+
+#include <cub/cub.cuh>
+
+#include <algorithm>
+#include <cstddef>
+#include <cstring>
+#include <vector>
+
+#include "engine_base.h"
+#include "k_avbd.cuh"
+#include "k_broad.cuh"
+#include "k_narrow_kernels.cuh"
+#include "k_rows.cuh"
+
+namespace dio {
+
+#define DIO_CK(expr)                                                            \
+    do {                                                                        \
+        cudaError_t e_ = (expr);                                                \
+        if (e_ != cudaSuccess) {                                                \
+            err = std::string(#expr) + ": " + cudaGetErrorString(e_);           \
+            return DIO_ERR_CUDA;                                                \
+        }                                                                       \
+    } while (0)
+
+#define DIO_TRY(expr)            \
+    do {                         \
+        int rc_ = (expr);        \
+        if (rc_ != DIO_OK) return rc_; \
+    } while (0)
+
+// small kernels used by the pipeline ------------------------------------
+static __global__ void k_set_u32(uint32_t* dst, uint32_t v) { *dst = v; }
+static __global__ void k_copy_u32(uint32_t* dst, const uint32_t* src) { *dst = *src; }
+static __global__ void k_sum_rows(Counters* c, const uint32_t* pair_rows, const uint32_t* cont_rows, uint32_t max_rows) {
+    c->pair_rows = *pair_rows;
+    c->container_rows = *cont_rows;
+    uint64_t t = (uint64_t)*pair_rows + *cont_rows;
+    c->rows = t > max_rows ? max_rows : (uint32_t)t;
+    if (t > max_rows) c->error_flags |= kErrRowOverflow;
+}
+static __global__ void k_pairs_total(Counters* c, const uint32_t* total, uint32_t max_pairs) {
+    c->pairs = *total;
+    if (*total > max_pairs) c->error_flags |= kErrPairOverflow;
+}
+
+template <class P, class R>
+__global__ void k_unpack_bodies(DevWorld<P, R> w, const DioGpuBody* bodies, uint32_t n) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const DioGpuBody b = bodies[i];
+        w.pos[0][i] = A4<P>{P(b.position[0]), P(b.position[1]), P(b.position[2]), P(0)};
+        w.rot[0][i] = A4<P>{P(b.orientation[0]), P(b.orientation[1]), P(b.orientation[2]), P(b.orientation[3])};
+        w.shape[i] = b.shape;
+        w.scene[i] = 0;
+    }
+}
+
+template <class P, class R>
+__global__ void k_set_pose(DevWorld<P, R> w, const DioGpuBody* bodies, uint32_t n) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 p = *reinterpret_cast<const float4*>(bodies[i].position);
+        const float4 q = *reinterpret_cast<const float4*>(bodies[i].orientation);
+        w.pos[0][i] = A4<P>{P(p.x), P(p.y), P(p.z), P(0)};
+        w.rot[0][i] = A4<P>{P(q.x), P(q.y), P(q.z), P(q.w)};
+    }
+}
+
+template <class P, class R>
+__global__ void k_unpack_pose3(DevWorld<P, R> w, const float* pos3, const float* quat4, uint32_t n) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        w.pos[0][i] = A4<P>{P(pos3[3 * i]), P(pos3[3 * i + 1]), P(pos3[3 * i + 2]), P(0)};
+        w.rot[0][i] = A4<P>{P(quat4[4 * i]), P(quat4[4 * i + 1]), P(quat4[4 * i + 2]), P(quat4[4 * i + 3])};
+        w.scene[i] = 0;
+    }
+}
+
+template <class P, class R>
+__global__ void k_unpack_pose_f64(DevWorld<P, R> w, const double* pos3, const double* quat4, uint32_t n) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (pos3) w.pos[0][i] = A4<P>{P(pos3[3 * i]), P(pos3[3 * i + 1]), P(pos3[3 * i + 2]), P(0)};
+        if (quat4)
+            w.rot[0][i] = A4<P>{P(quat4[4 * i]), P(quat4[4 * i + 1]), P(quat4[4 * i + 2]), P(quat4[4 * i + 3])};
+    }
+}
+
+template <class P, class R>
+__global__ void k_unpack_state(DevWorld<P, R> w, const DioBodyState* st, uint32_t n) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const DioBodyState s = st[i];
+        w.vel[i] = A4<P>{P(s.vel[0]), P(s.vel[1]), P(s.vel[2]), P(0)};
+        w.ang[i] = A4<P>{P(s.ang[0]), P(s.ang[1]), P(s.ang[2]), P(0)};
+        w.prev_vel[i] = A4<P>{P(s.prev_vel[0]), P(s.prev_vel[1]), P(s.prev_vel[2]), P(0)};
+        w.inv[i] = A4<R>{R(s.inv_moment[0]), R(s.inv_moment[1]), R(s.inv_moment[2]), R(s.inv_mass)};
+        w.friction[i] = R(s.friction);
+    }
+}
+
+template <class P, class R>
+__global__ void k_unpack_contacts(RowStatic<R>* rs, RowDual<P, R>* rd, uint2* ab, const DioContact* c, uint32_t m,
+                                  uint32_t n, uint32_t* err) {
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) {
+        const DioContact x = c[r];
+        RowStatic<R> s;
+        s.n = A4<R>{R(x.normal[0]), R(x.normal[1]), R(x.normal[2]), R(x.friction)};
+        s.t1 = A4<R>{R(x.tangent1[0]), R(x.tangent1[1]), R(x.tangent1[2]), R(x.c0[2])};
+        s.t2 = A4<R>{R(x.tangent2[0]), R(x.tangent2[1]), R(x.tangent2[2]), R(0)};
+        s.ra = A4<R>{R(x.r_a[0]), R(x.r_a[1]), R(x.r_a[2]), R(x.c0[0])};
+        s.rb = A4<R>{R(x.r_b[0]), R(x.r_b[1]), R(x.r_b[2]), R(x.c0[1])};
+        rs[r] = s;
+        RowDual<P, R> d;
+        d.penalty = A4<R>{R(x.penalty[0]), R(x.penalty[1]), R(x.penalty[2]), R(0)};
+        d.lambda = A4<P>{P(x.lambda[0]), P(x.lambda[1]), P(x.lambda[2]), P(0)};
+        rd[r] = d;
+        ab[r] = make_uint2(x.a, x.b);
+        if (x.a >= n || (x.b != kContainer && x.b >= n)) atomicOr(err, kErrBadIndex);
+    }
+}
+
+template <class P, class R>
+__global__ void k_pack_contacts(const RowStatic<R>* rs, const RowDual<P, R>* rd, const uint2* ab, DioContact* out,
+                                const uint32_t* m_dev) {
+    uint32_t m = *m_dev;
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) {
+        const RowStatic<R> s = rs[r];
+        const RowDual<P, R> d = rd[r];
+        DioContact x;
+        x.a = ab[r].x;
+        x.b = ab[r].y;
+        x.friction = float(s.n.w);
+        x.pad = 0.f;
+        auto put = [](float* f, A4<R> v) {
+            f[0] = float(v.x);
+            f[1] = float(v.y);
+            f[2] = float(v.z);
+            f[3] = 0.f;
+        };
+        put(x.normal, s.n);
+        put(x.tangent1, s.t1);
+        put(x.tangent2, s.t2);
+        put(x.r_a, s.ra);
+        put(x.r_b, s.rb);
+        x.c0[0] = float(s.ra.w);
+        x.c0[1] = float(s.rb.w);
+        x.c0[2] = float(s.t1.w);
+        x.c0[3] = 0.f;
+        put(x.penalty, d.penalty);
+        x.lambda[0] = float(d.lambda.x);
+        x.lambda[1] = float(d.lambda.y);
+        x.lambda[2] = float(d.lambda.z);
+        x.lambda[3] = 0.f;
+        out[r] = x;
+    }
+}
+
+// Given the reference CSR (offsets, indices), derive the other-body array.
+static __global__ void k_csr_other(const uint32_t* off, const uint32_t* idx, const uint2* ab, uint32_t* oth, uint32_t n,
+                            uint32_t m, uint32_t* err) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        for (uint32_t j = off[i]; j < off[i + 1]; ++j) {
+            uint32_t r = idx[j];
+            if (r >= m) {
+                atomicOr(err, kErrBadIndex);
+                oth[j] = kContainer;
+                continue;
+            }
+            uint2 v = ab[r];
+            if (v.y == kContainer)
+                oth[j] = kContainer;
+            else if (v.x == i)
+                oth[j] = v.y;
+            else
+                oth[j] = v.x | kIsB;
+        }
+    }
+}
+
+template <class P, class R>
+__global__ void k_pack_result(DevWorld<P, R> w, uint32_t n, int buf, float* pos3, float* quat4, float* vel,
+                              float* ang, float* prev) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        A4<P> p = w.pos[buf][i], q = w.rot[buf][i], v = w.vel[i], a = w.ang[i], pv = w.prev_vel[i];
+        pos3[3 * i] = float(p.x);
+        pos3[3 * i + 1] = float(p.y);
+        pos3[3 * i + 2] = float(p.z);
+        quat4[4 * i] = float(q.x);
+        quat4[4 * i + 1] = float(q.y);
+        quat4[4 * i + 2] = float(q.z);
+        quat4[4 * i + 3] = float(q.w);
+        vel[3 * i] = float(v.x);
+        vel[3 * i + 1] = float(v.y);
+        vel[3 * i + 2] = float(v.z);
+        ang[3 * i] = float(a.x);
+        ang[3 * i + 1] = float(a.y);
+        ang[3 * i + 2] = float(a.z);
+        prev[3 * i] = float(pv.x);
+        prev[3 * i + 1] = float(pv.y);
+        prev[3 * i + 2] = float(pv.z);
+    }
+}
+
+template <class P, class R>
+__global__ void k_pack_dual(const RowDual<P, R>* rd, uint32_t m, float* lambda, float* penalty) {
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) {
+        RowDual<P, R> d = rd[r];
+        lambda[3 * r] = float(d.lambda.x);
+        lambda[3 * r + 1] = float(d.lambda.y);
+        lambda[3 * r + 2] = float(d.lambda.z);
+        penalty[3 * r] = float(d.penalty.x);
+        penalty[3 * r + 1] = float(d.penalty.y);
+        penalty[3 * r + 2] = float(d.penalty.z);
+    }
+}
+
+template <class P, class R>
+__global__ void k_pack_world(DevWorld<P, R> w, DioGpuBody* bodies, DioBodyState* st, double* p64, double* q64) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < w.n; i += gridDim.x * blockDim.x) {
+        A4<P> p = w.pos[0][i], q = w.rot[0][i];
+        if (bodies) {
+            DioGpuBody b;
+            b.position[0] = float(p.x);
+            b.position[1] = float(p.y);
+            b.position[2] = float(p.z);
+            b.position[3] = 0.f;
+            b.orientation[0] = float(q.x);
+            b.orientation[1] = float(q.y);
+            b.orientation[2] = float(q.z);
+            b.orientation[3] = float(q.w);
+            b.shape = w.shape[i];
+            bodies[i] = b;
+        }
+        if (st) {
+            DioBodyState s;
+            A4<P> v = w.vel[i], a = w.ang[i], pv = w.prev_vel[i];
+            A4<R> inv = w.inv[i];
+            s.vel[0] = float(v.x), s.vel[1] = float(v.y), s.vel[2] = float(v.z), s.vel[3] = 0.f;
+            s.ang[0] = float(a.x), s.ang[1] = float(a.y), s.ang[2] = float(a.z), s.ang[3] = 0.f;
+            s.prev_vel[0] = float(pv.x), s.prev_vel[1] = float(pv.y), s.prev_vel[2] = float(pv.z);
+            s.prev_vel[3] = 0.f;
+            s.inv_moment[0] = float(inv.x), s.inv_moment[1] = float(inv.y), s.inv_moment[2] = float(inv.z);
+            s.inv_moment[3] = 0.f;
+            s.inv_mass = float(inv.w);
+            s.friction = float(w.friction[i]);
+            s.pad[0] = s.pad[1] = 0.f;
+            st[i] = s;
+        }
+        if (p64) {
+            p64[3 * i] = double(p.x);
+            p64[3 * i + 1] = double(p.y);
+            p64[3 * i + 2] = double(p.z);
+        }
+        if (q64) {
+            q64[4 * i] = double(q.x);
+            q64[4 * i + 1] = double(q.y);
+            q64[4 * i + 2] = double(q.z);
+            q64[4 * i + 3] = double(q.w);
+        }
+    }
+}
+
+// joint incidences (body, joint id) for the per-body joint CSR
+static __global__ void k_joint_inc(const DioConstraint* j, uint32_t nj, uint32_t n, uint32_t* body, uint32_t* id,
+                            uint32_t* err) {
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nj; k += gridDim.x * blockDim.x) {
+        uint32_t a = j[k].a, b = j[k].b;
+        if (a >= n || b >= n) {
+            atomicOr(err, kErrBadIndex);
+            a = n;
+            b = n;
+        }
+        body[2 * k] = a;
+        id[2 * k] = k;
+        body[2 * k + 1] = (b == a) ? n : b;
+        id[2 * k + 1] = k;
+    }
+}
+
+static __global__ void k_count_lt(const uint32_t* body, uint32_t total, uint32_t n, uint32_t* counts) {
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < total; j += gridDim.x * blockDim.x)
+        if (body[j] < n) atomicAdd(&counts[body[j]], 1u);
+}
+
+static __global__ void k_scene_of(uint32_t* scene, const SceneDesc* sc, uint32_t ns) {
+    uint32_t s = blockIdx.x;
+    if (s >= ns) return;
+    for (uint32_t i = sc[s].body_lo + threadIdx.x; i < sc[s].body_hi; i += blockDim.x) scene[i] = s;
+}
+
+static inline uint32_t bits_for(uint32_t v) {
+    uint32_t b = 1;
+    while (b < 32 && (1ull << b) <= v) ++b;
+    return b;
+}
+
+template <class P, class R>
+class Engine final : public EngineBase {
+   public:
+    Engine(const DioCapacity& cap, cudaStream_t s, const DioConfig& cfg) : cap_(cap), stream_(s), cfg_(cfg) {}
+    ~Engine() override {
+        collect_spans();
+        for (auto e : ev_free_) cudaEventDestroy(e);
+        release();
+    }
+
+    int init() {
+        const uint32_t N = std::max(1u, cap_.max_bodies);
+        const uint32_t PP = std::max(1u, cap_.max_pairs);
+        const uint32_t M = std::max(1u, cap_.max_contacts);
+        const uint32_t J = std::max(1u, cap_.max_joints);
+        const uint32_t S = std::max(1u, cap_.max_scenes);
+        const uint32_t H = std::max(1u, cap_.max_hull_vertices);
+        per_cap_ = cfg_.contacts_per_pair == 8 ? 8 : 4;
+        for (int b = 0; b < 2; ++b) {
+            DIO_TRY(alloc(&w_.pos[b], N));
+            DIO_TRY(alloc(&w_.rot[b], N));
+        }
+        DIO_TRY(alloc(&w_.init_pos, N));
+        DIO_TRY(alloc(&w_.init_rot, N));
+        DIO_TRY(alloc(&w_.inert_pos, N));
+        DIO_TRY(alloc(&w_.inert_rot, N));
+        DIO_TRY(alloc(&w_.vel, N));
+        DIO_TRY(alloc(&w_.ang, N));
+        DIO_TRY(alloc(&w_.prev_vel, N));
+        DIO_TRY(alloc(&w_.inv, N));
+        DIO_TRY(alloc(&w_.friction, N));
+        DIO_TRY(alloc(&w_.shape, N));
+        DIO_TRY(alloc(&w_.scene, N));
+        DIO_TRY(alloc(&origin_, S));
+        DIO_TRY(alloc(&w_.aabb_min, N));
+        DIO_TRY(alloc(&w_.aabb_max, N));
+        DIO_TRY(alloc(&w_.color, N));
+        DIO_TRY(alloc(&w_.color_order, N));
+        DIO_TRY(alloc(&w_.color_off, 1025));
+        DIO_TRY(alloc(&w_.pairs, PP));
+        DIO_TRY(alloc(&w_.slots, (size_t)PP * per_cap_));
+        DIO_TRY(alloc(&w_.gjk_list, PP));
+        DIO_TRY(alloc(&w_.epa_list, PP));
+        DIO_TRY(alloc(&w_.simplex, (size_t)PP * 8));
+        for (int b = 0; b < 2; ++b) {
+            DIO_TRY(alloc(&rs_[b], M));
+            DIO_TRY(alloc(&rd_[b], M));
+            DIO_TRY(alloc(&ab_[b], M));
+            DIO_TRY(alloc(&keys_s_[b], M));
+            DIO_TRY(alloc(&ids_s_[b], M));
+        }
+        DIO_TRY(alloc(&keys_raw_, M));
+        DIO_TRY(alloc(&ids_raw_, M));
+        const size_t INC = std::max<size_t>(2ull * M, 2ull * J);
+        DIO_TRY(alloc(&inc_body_, INC));
+        DIO_TRY(alloc(&inc_row_, INC));
+        DIO_TRY(alloc(&inc_body_s_, INC));
+        DIO_TRY(alloc(&inc_row_s_, INC));
+        DIO_TRY(alloc(&w_.row_off, (size_t)N + 1));
+        DIO_TRY(alloc(&w_.row_idx, 2ull * M));
+        DIO_TRY(alloc(&w_.row_oth, 2ull * M));
+        DIO_TRY(alloc(&joints_, J));
+        DIO_TRY(alloc(&joint_off_, (size_t)N + 1));
+        DIO_TRY(alloc(&joint_idx_, 2ull * J));
+        const size_t CNT = std::max<size_t>(std::max<size_t>(N, (size_t)PP * per_cap_), 2ull * M) + 2;
+        DIO_TRY(alloc(&counts_, CNT));
+        DIO_TRY(alloc(&offsets_, CNT));
+        DIO_TRY(alloc(&counts2_, (size_t)N + 2));
+        DIO_TRY(alloc(&offsets2_, (size_t)N + 2));
+        DIO_TRY(alloc(&scenes_, S));
+        DIO_TRY(alloc(&hull_, H));
+        DIO_TRY(alloc(&ctr_, 1));
+        DIO_CK(cudaMallocHost(&hctr_, sizeof(Counters)));
+        // CUB temporary storage for the largest sort / scan
+        size_t t1 = 0, t2 = 0, t3 = 0;
+        cub::DeviceRadixSort::SortPairs(nullptr, t1, keys_raw_, keys_s_[0], ids_raw_, ids_s_[0], (int)M, 0, 64,
+                                        stream_);
+        cub::DeviceRadixSort::SortPairs(nullptr, t2, inc_body_, inc_body_s_, inc_row_, inc_row_s_, (int)INC, 0, 32,
+                                        stream_);
+        cub::DeviceScan::ExclusiveSum(nullptr, t3, counts_, offsets_, (int)CNT, stream_);
+        cub_bytes_ = std::max(t1, std::max(t2, t3)) + 256;
+        DIO_CK(cudaMalloc(&cub_tmp_, cub_bytes_));
+        // API staging (device + pinned host)
+        stage_bytes_ = (size_t)N * (sizeof(DioGpuBody) + sizeof(DioBodyState) + 64 + 16) + (size_t)M * sizeof(DioContact) +
+                       (size_t)J * sizeof(DioConstraint) + ((size_t)N + 1) * 4 + 2ull * M * 4 +
+                       (size_t)PP * per_cap_ * sizeof(DioContactOut) + (size_t)PP * sizeof(DioPair) +
+                       (size_t)M * 24 + 4096;
+        DIO_CK(cudaMalloc(&dstage_, stage_bytes_));
+        DIO_CK(cudaMallocHost(&hstage_, stage_bytes_));
+        DIO_CK(cudaMemsetAsync(ctr_, 0, sizeof(Counters), stream_));
+        DIO_CK(cudaMemsetAsync(joint_off_, 0, ((size_t)N + 1) * 4, stream_));
+        w_.origin = nullptr;
+        w_.hull = hull_;
+        w_.max_pairs = PP;
+        w_.per_pair = per_cap_;
+        w_.max_rows = M;
+        w_.max_incid = 2 * M;
+        w_.joints = joints_;
+        w_.joint_off = joint_off_;
+        w_.joint_idx = joint_idx_;
+        w_.n_joints = 0;
+        w_.scenes = scenes_;
+        w_.n_scenes = 0;
+        w_.ctr = ctr_;
+        w_.n = 0;
+        set_rows(0);
+        int dev = 0;
+        DIO_CK(cudaGetDevice(&dev));
+        DIO_CK(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev));
+        return DIO_OK;
+    }
+
+    void set_stream(cudaStream_t s) override { stream_ = s; }
+    void set_config(const DioConfig& c) override {
+        uint32_t per = cfg_.contacts_per_pair;
+        cfg_ = c;
+        if (c.contacts_per_pair != 4 && c.contacts_per_pair != 8) cfg_.contacts_per_pair = per;
+        if (cfg_.contacts_per_pair > per_cap_) cfg_.contacts_per_pair = per_cap_;
+    }
+
+    // ------------------------------------------------ reference-mirror API
+    int broad_submit(const DioGpuBody* bodies, uint32_t n) override {
+        if (n > cap_.max_bodies) return cap_err("too many bodies for the compute buffers");
+        api_bodies_ = n;
+        if (n == 0) {
+            DIO_CK(cudaMemsetAsync(ctr_, 0, sizeof(Counters), stream_));
+            return DIO_OK;
+        }
+        DIO_TRY(upload_bodies(bodies, n));
+        DIO_TRY(single_scene(n, nullptr));
+        DIO_CK(cudaMemsetAsync(ctr_, 0, sizeof(Counters), stream_));
+        return run_broad(0, n);
+    }
+    int pair_count(uint32_t* count) override {
+        if (!count) return inval("null count");
+        DIO_TRY(pull_counters());
+        *count = hctr_->pairs;
+        if (hctr_->pairs > cap_.max_pairs) return cap_err("broad phase found more pairs than max_pairs");
+        return DIO_OK;
+    }
+    int read_pairs(DioPair* out, uint32_t cap, uint32_t* n) override {
+        DIO_TRY(pull_counters());
+        uint32_t c = std::min(hctr_->pairs, cap_.max_pairs);
+        if (n) *n = c;
+        uint32_t k = std::min(c, cap);
+        if (k && out) {
+            DIO_CK(cudaMemcpyAsync(out, w_.pairs, (size_t)k * sizeof(DioPair), cudaMemcpyDeviceToHost, stream_));
+            DIO_CK(cudaStreamSynchronize(stream_));
+        }
+        return c > cap ? cap_err("output buffer smaller than the pair count") : DIO_OK;
+    }
+    int narrow_submit_pairs(const DioGpuBody* bodies, uint32_t n, const DioPair* pairs, uint32_t np) override {
+        if (n > cap_.max_bodies) return cap_err("too many bodies for the compute buffers");
+        if (np > cap_.max_pairs) return cap_err("too many pairs for the compute buffers");
+        last_np_ = np;
+        if (np == 0) return DIO_OK;
+        DIO_TRY(upload_bodies(bodies, n));
+        api_bodies_ = n;
+        DIO_TRY(single_scene(n, nullptr));
+        DIO_CK(cudaMemcpyAsync(w_.pairs, pairs, (size_t)np * sizeof(DioPair), cudaMemcpyHostToDevice, stream_));
+        DIO_CK(cudaMemsetAsync(ctr_, 0, sizeof(Counters), stream_));
+        return run_narrow(np, nullptr);
+    }
+    int narrow_submit(uint32_t np) override {
+        if (np > cap_.max_pairs) return cap_err("too many pairs for the compute buffers");
+        last_np_ = np;
+        if (np == 0) return DIO_OK;
+        DIO_CK(cudaMemsetAsync(&ctr_->gjk_work, 0, 2 * sizeof(uint32_t), stream_));
+        return run_narrow(np, nullptr);
+    }
+    int narrow_read(DioContactOut* out, uint32_t cap, uint32_t* n) override {
+        uint32_t slots = last_np_ * cfg_.contacts_per_pair;
+        if (n) *n = slots;
+        if (slots > cap) return cap_err("output buffer smaller than the slot count");
+        if (slots == 0) return DIO_OK;
+        if (sizeof(R) == 4 && cfg_.contacts_per_pair == w_.per_pair) {
+            DIO_CK(cudaMemcpyAsync(out, w_.slots, (size_t)slots * sizeof(DioContactOut), cudaMemcpyDeviceToHost,
+                                   stream_));
+        } else {
+            return inval("narrow_read needs an FP32 engine");
+        }
+        DIO_CK(cudaStreamSynchronize(stream_));
+        DIO_TRY(check_flags());
+        return DIO_OK;
+    }
+    int set_hull(const float* xyzw, uint32_t count) override {
+        if (count > cap_.max_hull_vertices) return cap_err("too many hull vertices");
+        if (count == 0) return DIO_OK;
+        std::vector<A4<R>> tmp(count);
+        for (uint32_t i = 0; i < count; ++i)
+            tmp[i] = A4<R>{R(xyzw[4 * i]), R(xyzw[4 * i + 1]), R(xyzw[4 * i + 2]), R(0)};
+        DIO_CK(cudaMemcpyAsync(hull_, tmp.data(), count * sizeof(A4<R>), cudaMemcpyHostToDevice, stream_));
+        DIO_CK(cudaStreamSynchronize(stream_));
+        return DIO_OK;
+    }
+
+    int prepare_contacts(const DioGpuBody* bodies, const DioBodyState* state, uint32_t n, const DioContactOut* slots,
+                         uint32_t n_slots, const DioContact* prev, uint32_t n_prev, const DioContainer* container,
+                         const DioAvbdOptions* options, DioContact* out, uint32_t cap, uint32_t* m, uint32_t* offsets,
+                         uint32_t* indices, uint32_t index_cap) override {
+        if (!options || (n && (!bodies || !state))) return inval("null argument");
+        if (n > cap_.max_bodies) return cap_err("too many bodies");
+        if ((uint64_t)n_slots > (uint64_t)cap_.max_pairs * per_cap_) return cap_err("too many slots");
+        if (n_prev > cap_.max_contacts) return cap_err("too many previous contacts");
+        if (sizeof(R) != 4) return inval("prepare_contacts needs an FP32 engine");
+        DIO_TRY(upload_bodies(bodies, n));
+        DIO_TRY(upload_state(state, n));
+        DIO_TRY(single_scene(n, container));
+        DIO_CK(cudaMemsetAsync(ctr_, 0, sizeof(Counters), stream_));
+        // previous rows into the "previous" buffer, then their sorted keys
+        int pb = 1 - cur_;
+        if (n_prev) {
+            DioContact* dprev = reinterpret_cast<DioContact*>(dstage_);
+            DIO_CK(cudaMemcpyAsync(dprev, prev, (size_t)n_prev * sizeof(DioContact), cudaMemcpyHostToDevice, stream_));
+            k_unpack_contacts<P, R><<<grid_for(n_prev, 256), 256, 0, stream_>>>(rs_[pb], rd_[pb], ab_[pb], dprev,
+                                                                                n_prev, 0xFFFFFFFFu, &ctr_->error_flags);
+            DIO_TRY(sort_keys(ab_[pb], n_prev, keys_s_[pb], ids_s_[pb]));
+        }
+        n_prev_rows_ = n_prev;
+        // slots -> device (FP32 slots are DioContactOut bytes)
+        if (n_slots)
+            DIO_CK(cudaMemcpyAsync(w_.slots, slots, (size_t)n_slots * sizeof(DioContactOut), cudaMemcpyHostToDevice,
+                                   stream_));
+        DIO_TRY(build_rows(opts_prep(*options), n_slots, 1, nullptr, n));
+        DIO_TRY(pull_counters());
+        uint32_t M = hctr_->rows;
+        *m = M;
+        DIO_TRY(finish_rows(opts_prep(*options), M, n));
+        uint32_t ninc = 0;
+        DIO_CK(cudaMemcpyAsync(&ninc, w_.row_off + n, 4, cudaMemcpyDeviceToHost, stream_));
+        DIO_CK(cudaStreamSynchronize(stream_));
+        DIO_TRY(check_flags());
+        if (M > cap || ninc > index_cap) return cap_err("output buffers smaller than the rows / CSR");
+        DioContact* dout = reinterpret_cast<DioContact*>(dstage_);
+        k_pack_contacts<P, R><<<grid_for(M, 256), 256, 0, stream_>>>(w_.rs, w_.rd, w_.ab, dout, &ctr_->rows);
+        if (M) DIO_CK(cudaMemcpyAsync(out, dout, (size_t)M * sizeof(DioContact), cudaMemcpyDeviceToHost, stream_));
+        DIO_CK(cudaMemcpyAsync(offsets, w_.row_off, ((size_t)n + 1) * 4, cudaMemcpyDeviceToHost, stream_));
+        if (ninc) DIO_CK(cudaMemcpyAsync(indices, w_.row_idx, (size_t)ninc * 4, cudaMemcpyDeviceToHost, stream_));
+        DIO_CK(cudaStreamSynchronize(stream_));
+        cur_ = 1 - cur_;
+        set_rows(cur_);
+        return DIO_OK;
+    }
+
+    int avbd_submit(const DioBodyState* state, const float* positions, const float* orientations, uint32_t n,
+                    const DioContact* contacts, uint32_t m, const DioConstraint* constraints, uint32_t nj,
+                    const uint32_t* offsets, const uint32_t* indices, const DioRunOptions* options) override {
+        if (!options) return inval("null options");
+        if (n > cap_.max_bodies) return cap_err("too many bodies for the AVBD buffers");
+        if (m > cap_.max_contacts) return cap_err("too many contacts for the AVBD buffers");
+        if (nj > cap_.max_joints) return cap_err("too many constraints for the AVBD buffers");
+        api_n_ = n;
+        api_m_ = m;
+        api_iters_ = options->iterations;
+        if (n == 0) return DIO_OK;
+        if (!state || !positions || !orientations || !offsets || (m && !contacts) || (nj && !constraints))
+            return inval("null argument");
+        uint32_t ninc = offsets[n];
+        if (ninc > 2ull * cap_.max_contacts) return cap_err("too many CSR indices");
+        if (ninc && !indices) return inval("null indices");
+        DIO_TRY(upload_state(state, n));
+        // poses
+        char* st = reinterpret_cast<char*>(dstage_);
+        float* dpos = reinterpret_cast<float*>(st);
+        float* dq = dpos + 3 * (size_t)n;
+        DIO_CK(cudaMemcpyAsync(dpos, positions, (size_t)n * 12, cudaMemcpyHostToDevice, stream_));
+        DIO_CK(cudaMemcpyAsync(dq, orientations, (size_t)n * 16, cudaMemcpyHostToDevice, stream_));
+        k_unpack_pose3<P, R><<<grid_for(n, 256), 256, 0, stream_>>>(w_, dpos, dq, n);
+        DIO_CK(cudaMemsetAsync(ctr_, 0, sizeof(Counters), stream_));
+        // rows
+        w_.n = n;
+        if (m) {
+            DioContact* dc = reinterpret_cast<DioContact*>(st + align256((size_t)n * 28));
+            DIO_CK(cudaMemcpyAsync(dc, contacts, (size_t)m * sizeof(DioContact), cudaMemcpyHostToDevice, stream_));
+            k_unpack_contacts<P, R><<<grid_for(m, 256), 256, 0, stream_>>>(w_.rs, w_.rd, w_.ab, dc, m, n,
+                                                                           &ctr_->error_flags);
+        }
+        DIO_CK(cudaMemcpyAsync(w_.row_off, offsets, ((size_t)n + 1) * 4, cudaMemcpyHostToDevice, stream_));
+        if (ninc) DIO_CK(cudaMemcpyAsync(w_.row_idx, indices, (size_t)ninc * 4, cudaMemcpyHostToDevice, stream_));
+        k_csr_other<<<grid_for(n, 128), 128, 0, stream_>>>(w_.row_off, w_.row_idx, w_.ab, w_.row_oth, n, m,
+                                                          &ctr_->error_flags);
+        DIO_TRY(upload_joints(constraints, nj, n));
+        k_set_u32<<<1, 1, 0, stream_>>>(&ctr_->rows, m);
+        SolveParams<R> o = solve_params(options->dt, options->gravity, options->alpha, options->beta_lin,
+                                        options->penalty_max, options->iterations);
+        DIO_TRY(solve(o, n, m));
+        return DIO_OK;
+    }
+
+    int avbd_read(const DioAvbdResult* out) override {
+        if (!out) return inval("null result");
+        uint32_t n = api_n_, m = api_m_;
+        if (n == 0) return DIO_OK;
+        uint32_t fp_read = (api_iters_ == 0 ? 0u : api_iters_ - 1u) % 2u;
+        int buf = 1 - (int)fp_read;
+        size_t nb = (size_t)n * 4 * (3 + 4 + 3 + 3 + 3);
+        size_t mb = (size_t)m * 4 * 6;
+        float* d = reinterpret_cast<float*>(dstage_);
+        float *dp = d, *dqq = dp + 3 * (size_t)n, *dv = dqq + 4 * (size_t)n, *da = dv + 3 * (size_t)n,
+              *dpv = da + 3 * (size_t)n, *dl = dpv + 3 * (size_t)n, *dk = dl + 3 * (size_t)m;
+        k_pack_result<P, R><<<grid_for(n, 256), 256, 0, stream_>>>(w_, n, buf, dp, dqq, dv, da, dpv);
+        if (m) k_pack_dual<P, R><<<grid_for(m, 256), 256, 0, stream_>>>(w_.rd, m, dl, dk);
+        DIO_CK(cudaMemcpyAsync(hstage_, d, nb + mb, cudaMemcpyDeviceToHost, stream_));
+        DIO_CK(cudaStreamSynchronize(stream_));
+        DIO_TRY(check_flags());
+        const float* h = reinterpret_cast<const float*>(hstage_);
+        const float *hp = h, *hq = hp + 3 * (size_t)n, *hv = hq + 4 * (size_t)n, *ha = hv + 3 * (size_t)n,
+                    *hpv = ha + 3 * (size_t)n, *hl = hpv + 3 * (size_t)n, *hk = hl + 3 * (size_t)m;
+        if (out->positions) std::memcpy(out->positions, hp, (size_t)n * 12);
+        if (out->orientations) std::memcpy(out->orientations, hq, (size_t)n * 16);
+        if (out->velocities) std::memcpy(out->velocities, hv, (size_t)n * 12);
+        if (out->angular_velocities) std::memcpy(out->angular_velocities, ha, (size_t)n * 12);
+        if (out->prev_velocities) std::memcpy(out->prev_velocities, hpv, (size_t)n * 12);
+        if (out->lambda && m) std::memcpy(out->lambda, hl, (size_t)m * 12);
+        if (out->penalty && m) std::memcpy(out->penalty, hk, (size_t)m * 12);
+        return DIO_OK;
+    }
+
+    // ------------------------------------------------------------- world
+    int world_upload(const DioWorldDesc* d) override {
+        if (!d) return inval("null world");
+        uint32_t n = d->n_bodies;
+        if (n > cap_.max_bodies) return cap_err("too many bodies");
+        if (d->n_constraints > cap_.max_joints) return cap_err("too many constraints");
+        uint32_t ns = d->n_scenes == 0 ? 1 : d->n_scenes;
+        if (ns > cap_.max_scenes) return cap_err("too many scenes");
+        if (d->n_hull_vertices > cap_.max_hull_vertices) return cap_err("too many hull vertices");
+        if (n && (!d->bodies || !d->state)) return inval("null bodies/state");
+        DIO_TRY(upload_bodies(d->bodies, n));
+        if (d->positions_f64 || d->orientations_f64) {
+            double* dp = reinterpret_cast<double*>(dstage_);
+            double* dq = dp + 3 * (size_t)n;
+            if (d->positions_f64)
+                DIO_CK(cudaMemcpyAsync(dp, d->positions_f64, (size_t)n * 24, cudaMemcpyHostToDevice, stream_));
+            if (d->orientations_f64)
+                DIO_CK(cudaMemcpyAsync(dq, d->orientations_f64, (size_t)n * 32, cudaMemcpyHostToDevice, stream_));
+            k_unpack_pose_f64<P, R><<<grid_for(n, 256), 256, 0, stream_>>>(
+                w_, d->positions_f64 ? dp : nullptr, d->orientations_f64 ? dq : nullptr, n);
+        }
+        DIO_TRY(upload_state(d->state, n));
+        // scenes
+        std::vector<SceneDesc> sc(ns);
+        std::vector<A4<P>> org(ns);
+        for (uint32_t s = 0; s < ns; ++s) {
+            SceneDesc& x = sc[s];
+            std::memset(&x, 0, sizeof x);
+            x.body_lo = (d->scene_offsets && d->n_scenes) ? d->scene_offsets[s] : 0;
+            x.body_hi = (d->scene_offsets && d->n_scenes) ? d->scene_offsets[s + 1] : n;
+            if (x.body_hi < x.body_lo || x.body_hi > n) return inval("bad scene offsets");
+            x.rotation[3] = 1.f;
+            org[s] = A4<P>{P(0), P(0), P(0), P(0)};
+            if (d->containers) {
+                const DioContainer& c = d->containers[s];
+                x.has_container = 1;
+                std::memcpy(x.center, c.center, 12);
+                x.half_extent = c.half_extent;
+                std::memcpy(x.rotation, c.rotation, 16);
+                if (cfg_.precision == DIO_PREC_SPLIT) org[s] = A4<P>{P(c.center[0]), P(c.center[1]), P(c.center[2]), P(0)};
+            }
+        }
+        scenes_host_ = sc;
+        DIO_CK(cudaMemcpyAsync(scenes_, sc.data(), ns * sizeof(SceneDesc), cudaMemcpyHostToDevice, stream_));
+        DIO_CK(cudaMemcpyAsync(origin_, org.data(), ns * sizeof(A4<P>), cudaMemcpyHostToDevice, stream_));
+        w_.origin = cfg_.precision == DIO_PREC_SPLIT ? origin_ : nullptr;
+        w_.n_scenes = ns;
+        k_scene_of<<<ns, 128, 0, stream_>>>(w_.scene, scenes_, ns);
+        if (d->n_hull_vertices) {
+            std::vector<A4<R>> hv(d->n_hull_vertices);
+            for (uint32_t i = 0; i < d->n_hull_vertices; ++i)
+                hv[i] = A4<R>{R(d->hull_vertices[4 * i]), R(d->hull_vertices[4 * i + 1]),
+                              R(d->hull_vertices[4 * i + 2]), R(0)};
+            DIO_CK(cudaMemcpyAsync(hull_, hv.data(), hv.size() * sizeof(A4<R>), cudaMemcpyHostToDevice, stream_));
+            DIO_CK(cudaStreamSynchronize(stream_));
+        }
+        w_.n = n;
+        DIO_CK(cudaMemsetAsync(ctr_, 0, sizeof(Counters), stream_));
+        DIO_TRY(upload_joints(d->constraints, d->n_constraints, n));
+        n_prev_rows_ = 0;
+        steps_ = 0;
+        world_ready_ = true;
+        DIO_CK(cudaStreamSynchronize(stream_));
+        return check_flags();
+    }
+
+    int step(const DioAvbdOptions* options, uint32_t steps) override {
+        if (!options) return inval("null options");
+        if (!world_ready_) return state_err("no world uploaded");
+        for (uint32_t k = 0; k < steps; ++k) DIO_TRY(step_once(*options));
+        return DIO_OK;
+    }
+
+    int set_state(const DioGpuBody* bodies, const DioBodyState* state) override {
+        if (!world_ready_) return state_err("no world uploaded");
+        uint32_t n = w_.n;
+        if (bodies) {
+            DioGpuBody* db = reinterpret_cast<DioGpuBody*>(dstage_);
+            DIO_CK(cudaMemcpyAsync(db, bodies, (size_t)n * sizeof(DioGpuBody), cudaMemcpyHostToDevice, stream_));
+            k_set_pose<P, R><<<grid_for(n, 256), 256, 0, stream_>>>(w_, db, n);
+            ++launches_;
+        }
+        if (state) {
+            DIO_TRY(upload_state(state, n));
+            ++launches_;
+        }
+        return DIO_OK;
+    }
+
+    int download(DioGpuBody* bodies, DioBodyState* state) override {
+        if (!world_ready_) return state_err("no world uploaded");
+        uint32_t n = w_.n;
+        if (!n) return DIO_OK;
+        DioGpuBody* db = reinterpret_cast<DioGpuBody*>(dstage_);
+        DioBodyState* ds = reinterpret_cast<DioBodyState*>(reinterpret_cast<char*>(dstage_) +
+                                                           align256((size_t)n * sizeof(DioGpuBody)));
+        k_pack_world<P, R><<<grid_for(n, 256), 256, 0, stream_>>>(w_, bodies ? db : nullptr, state ? ds : nullptr,
+                                                                  nullptr, nullptr);
+        if (bodies) DIO_CK(cudaMemcpyAsync(bodies, db, (size_t)n * sizeof(DioGpuBody), cudaMemcpyDeviceToHost, stream_));
+        if (state) DIO_CK(cudaMemcpyAsync(state, ds, (size_t)n * sizeof(DioBodyState), cudaMemcpyDeviceToHost, stream_));
+        DIO_CK(cudaStreamSynchronize(stream_));
+        return DIO_OK;
+    }
+
+    int download_f64(double* positions, double* orientations) override {
+        if (!world_ready_) return state_err("no world uploaded");
+        uint32_t n = w_.n;
+        if (!n) return DIO_OK;
+        double* dp = reinterpret_cast<double*>(dstage_);
+        double* dq = dp + 3 * (size_t)n;
+        k_pack_world<P, R><<<grid_for(n, 256), 256, 0, stream_>>>(w_, nullptr, nullptr, dp, dq);
+        if (positions) DIO_CK(cudaMemcpyAsync(positions, dp, (size_t)n * 24, cudaMemcpyDeviceToHost, stream_));
+        if (orientations) DIO_CK(cudaMemcpyAsync(orientations, dq, (size_t)n * 32, cudaMemcpyDeviceToHost, stream_));
+        DIO_CK(cudaStreamSynchronize(stream_));
+        return DIO_OK;
+    }
+
+    int contacts(DioContact* out, uint32_t cap, uint32_t* m) override {
+        // rows of the last step live in the "previous" buffer after the swap
+        int pb = 1 - cur_;
+        uint32_t M = n_prev_rows_;
+        if (m) *m = M;
+        if (M > cap) return cap_err("output buffer smaller than the row count");
+        if (!M) return DIO_OK;
+        DioContact* dout = reinterpret_cast<DioContact*>(dstage_);
+        uint32_t* dm = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(dstage_) + align256((size_t)M * sizeof(DioContact)));
+        k_set_u32<<<1, 1, 0, stream_>>>(dm, M);
+        k_pack_contacts<P, R><<<grid_for(M, 256), 256, 0, stream_>>>(rs_[pb], rd_[pb], ab_[pb], dout, dm);
+        DIO_CK(cudaMemcpyAsync(out, dout, (size_t)M * sizeof(DioContact), cudaMemcpyDeviceToHost, stream_));
+        DIO_CK(cudaStreamSynchronize(stream_));
+        return DIO_OK;
+    }
+
+    int colors(uint32_t* out, uint32_t cap, uint32_t* n) override {
+        uint32_t N = w_.n;
+        if (n) *n = N;
+        if (N > cap) return cap_err("output buffer smaller than the body count");
+        if (N) {
+            DIO_CK(cudaMemcpyAsync(out, w_.color, (size_t)N * 4, cudaMemcpyDeviceToHost, stream_));
+            DIO_CK(cudaStreamSynchronize(stream_));
+        }
+        return DIO_OK;
+    }
+
+    int stats(DioStepStats* out) override {
+        if (!out) return inval("null stats");
+        DIO_TRY(pull_counters());
+        out->pairs = hctr_->pairs;
+        out->contacts = hctr_->rows;
+        out->colors = hctr_->colors;
+        out->error_flags = hctr_->error_flags;
+        out->steps = steps_;
+        collect_spans();
+        out->kernel_launches = launches_;
+        out->primal_launches = primal_n_;
+        out->dual_launches = dual_n_;
+        out->primal_ms = primal_ms_;
+        out->dual_ms = dual_ms_;
+        return DIO_OK;
+    }
+
+   private:
+    // ------------------------------------------------------------ helpers
+    template <class T>
+    int alloc(T** p, size_t count) {
+        DIO_CK(cudaMalloc(reinterpret_cast<void**>(p), std::max<size_t>(1, count) * sizeof(T)));
+        allocs_.push_back(*p);
+        return DIO_OK;
+    }
+    void release() {
+        for (void* p : allocs_) cudaFree(p);
+        allocs_.clear();
+        if (cub_tmp_) cudaFree(cub_tmp_);
+        if (dstage_) cudaFree(dstage_);
+        if (hstage_) cudaFreeHost(hstage_);
+        if (hctr_) cudaFreeHost(hctr_);
+        cub_tmp_ = dstage_ = nullptr;
+        hstage_ = nullptr;
+        hctr_ = nullptr;
+    }
+    static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+    int inval(const char* m) {
+        err = m;
+        return DIO_ERR_INVALID;
+    }
+    int cap_err(const char* m) {
+        err = m;
+        return DIO_ERR_CAPACITY;
+    }
+    int state_err(const char* m) {
+        err = m;
+        return DIO_ERR_STATE;
+    }
+    void set_rows(int b) {
+        w_.rs = rs_[b];
+        w_.rd = rd_[b];
+        w_.ab = ab_[b];
+    }
+    int pull_counters() {
+        DIO_CK(cudaMemcpyAsync(hctr_, ctr_, sizeof(Counters), cudaMemcpyDeviceToHost, stream_));
+        DIO_CK(cudaStreamSynchronize(stream_));
+        return DIO_OK;
+    }
+    int check_flags() {
+        DIO_TRY(pull_counters());
+        uint32_t f = hctr_->error_flags;
+        if (!f) return DIO_OK;
+        DIO_CK(cudaMemsetAsync(&ctr_->error_flags, 0, 4, stream_));
+        if (f & kErrBadIndex) return inval("body / row index out of range");
+        if (f & (kErrPairOverflow | kErrRowOverflow | kErrIndexOverflow)) return cap_err("device capacity exceeded");
+        if (f & (kErrEpaFaces | kErrEpaHorizon)) return cap_err("EPA polytope exceeded its shared-memory capacity");
+        if (f & kErrTimeout) {
+            err = "device wait timed out";
+            return DIO_ERR_TIMEOUT;
+        }
+        if (f & kErrNonFinite) {
+            err = "non-finite solver state";
+            return DIO_ERR_NONFINITE;
+        }
+        return DIO_OK;
+    }
+    int upload_bodies(const DioGpuBody* bodies, uint32_t n) {
+        if (!n) return DIO_OK;
+        if (!bodies) return inval("null bodies");
+        DioGpuBody* db = reinterpret_cast<DioGpuBody*>(dstage_);
+        DIO_CK(cudaMemcpyAsync(db, bodies, (size_t)n * sizeof(DioGpuBody), cudaMemcpyHostToDevice, stream_));
+        k_unpack_bodies<P, R><<<grid_for(n, 256), 256, 0, stream_>>>(w_, db, n);
+        w_.n = n;
+        return DIO_OK;
+    }
+    int upload_state(const DioBodyState* state, uint32_t n) {
+        if (!n) return DIO_OK;
+        if (!state) return inval("null state");
+        DioBodyState* ds = reinterpret_cast<DioBodyState*>(reinterpret_cast<char*>(dstage_) +
+                                                           align256((size_t)n * sizeof(DioGpuBody)));
+        DIO_CK(cudaMemcpyAsync(ds, state, (size_t)n * sizeof(DioBodyState), cudaMemcpyHostToDevice, stream_));
+        k_unpack_state<P, R><<<grid_for(n, 256), 256, 0, stream_>>>(w_, ds, n);
+        return DIO_OK;
+    }
+    int single_scene(uint32_t n, const DioContainer* c) {
+        SceneDesc x;
+        std::memset(&x, 0, sizeof x);
+        x.body_lo = 0;
+        x.body_hi = n;
+        x.rotation[3] = 1.f;
+        if (c) {
+            x.has_container = 1;
+            std::memcpy(x.center, c->center, 12);
+            x.half_extent = c->half_extent;
+            std::memcpy(x.rotation, c->rotation, 16);
+        }
+        DIO_CK(cudaMemcpyAsync(scenes_, &x, sizeof x, cudaMemcpyHostToDevice, stream_));
+        DIO_CK(cudaMemsetAsync(w_.scene, 0, (size_t)std::max(n, 1u) * 4, stream_));
+        w_.n_scenes = 1;
+        w_.origin = nullptr;
+        w_.n = n;
+        // the API path is single-scene FP32; keep host scene table in sync
+        scenes_host_.assign(1, x);
+        DIO_CK(cudaStreamSynchronize(stream_));
+        return DIO_OK;
+    }
+    int upload_joints(const DioConstraint* cons, uint32_t nj, uint32_t n) {
+        w_.n_joints = nj;
+        if (!nj) {
+            DIO_CK(cudaMemsetAsync(joint_off_, 0, ((size_t)n + 1) * 4, stream_));
+            return DIO_OK;
+        }
+        DIO_CK(cudaMemcpyAsync(joints_, cons, (size_t)nj * sizeof(DioConstraint), cudaMemcpyHostToDevice, stream_));
+        uint32_t total = 2 * nj;
+        k_joint_inc<<<grid_for(nj, 256), 256, 0, stream_>>>(joints_, nj, n, inc_body_, inc_row_, &ctr_->error_flags);
+        size_t tb = cub_bytes_;
+        DIO_CK(cub::DeviceRadixSort::SortPairs(cub_tmp_, tb, inc_body_, inc_body_s_, inc_row_, inc_row_s_, (int)total,
+                                               0, (int)bits_for(n + 1), stream_));
+        DIO_CK(cudaMemsetAsync(counts2_, 0, ((size_t)n + 1) * 4, stream_));
+        k_count_lt<<<grid_for(total, 256), 256, 0, stream_>>>(inc_body_s_, total, n, counts2_);
+        tb = cub_bytes_;
+        DIO_CK(cub::DeviceScan::ExclusiveSum(cub_tmp_, tb, counts2_, joint_off_, (int)n + 1, stream_));
+        DIO_CK(cudaMemcpyAsync(joint_idx_, inc_row_s_, (size_t)total * 4, cudaMemcpyDeviceToDevice, stream_));
+        return DIO_OK;
+    }
+    int sort_keys(const uint2* ab, uint32_t m, unsigned long long* keys_out, uint32_t* ids_out) {
+        if (!m) return DIO_OK;
+        return sort_keys_n(ab, m, keys_out, ids_out);
+    }
+    int sort_keys_n(const uint2* ab, uint32_t m, unsigned long long* keys_out, uint32_t* ids_out);
+
+    static PrepParams<R> opts_prep(const DioAvbdOptions& o) {
+        PrepParams<R> p;
+        p.dt = R(o.dt);
+        p.margin = R(o.margin);
+        p.penalty_min = R(o.penalty_min);
+        p.penalty_max = R(o.penalty_max);
+        p.alpha_gamma = R(o.alpha) * R(o.gamma);
+        p.gamma = R(o.gamma);
+        p.friction = R(o.friction);
+        return p;
+    }
+    static SolveParams<R> solve_params(float dt, const float* g, float alpha, float beta, float kmax, uint32_t it) {
+        SolveParams<R> o;
+        o.dt = R(dt);
+        o.gx = R(g[0]);
+        o.gy = R(g[1]);
+        o.gz = R(g[2]);
+        o.alpha = R(alpha);
+        o.beta_lin = R(beta);
+        o.penalty_max = R(kmax);
+        o.iterations = it;
+        return o;
+    }
+
+    int run_broad(uint32_t lo, uint32_t hi) {
+        uint32_t n = hi - lo;
+        int g = grid_for(n, 128);
+        k_aabb<P, R><<<g, 128, 0, stream_>>>(w_, lo, hi);
+        constexpr int kB = 128;
+        int gd = grid_for(n, kB);
+        k_dense<P, R, kB><<<gd, kB, 0, stream_>>>(w_, lo, hi, counts_, offsets_, false);
+        DIO_CK(cudaMemsetAsync(counts_ + n, 0, 4, stream_));
+        size_t tb = cub_bytes_;
+        DIO_CK(cub::DeviceScan::ExclusiveSum(cub_tmp_, tb, counts_, offsets_, (int)n + 1, stream_));
+        k_dense<P, R, kB><<<gd, kB, 0, stream_>>>(w_, lo, hi, counts_, offsets_, true);
+        k_pairs_total<<<1, 1, 0, stream_>>>(ctr_, offsets_ + n, w_.max_pairs);
+        launches_ += 4;
+        return DIO_OK;
+    }
+
+    // narrow phase over np pairs (np_dev: device count, else np)
+    int run_narrow(uint32_t np, const uint32_t* np_dev) {
+        uint32_t per = cfg_.contacts_per_pair;
+        w_.per_pair = per;
+        int g = np_dev ? sms_ * 8 : grid_for(np, 128);
+        k_narrow_main<P, R><<<g, 128, 0, stream_>>>(w_, np_dev, np);
+        k_gjk<P, R><<<sms_ * 4, 128, 0, stream_>>>(w_);
+        k_epa<P, R><<<sms_ * 4, 32 * kEpaWarps, 0, stream_>>>(w_);
+        launches_ += 3;
+        return DIO_OK;
+    }
+
+    // Rows from `groups` groups of `per` slots (+ container rows for bodies).
+    int build_rows(const PrepParams<R>& o, uint32_t groups, uint32_t per, const uint32_t* groups_dev, uint32_t n) {
+        uint32_t G = groups;
+        if (G) {
+            k_slot_count<R><<<grid_for(G, 256), 256, 0, stream_>>>(w_.slots, per, groups_dev, G, counts_);
+            DIO_CK(cudaMemsetAsync(counts_ + G, 0, 4, stream_));
+            size_t tb = cub_bytes_;
+            DIO_CK(cub::DeviceScan::ExclusiveSum(cub_tmp_, tb, counts_, offsets_, (int)G + 1, stream_));
+            k_slot_rows<P, R><<<grid_for(G, 128), 128, 0, stream_>>>(w_, w_.slots, per, groups_dev, G, offsets_, o);
+        } else {
+            DIO_CK(cudaMemsetAsync(offsets_, 0, 4, stream_));
+        }
+        const uint32_t* pair_rows = offsets_ + G;
+        if (n) {
+            k_cont_count<P, R><<<grid_for(n, 128), 128, 0, stream_>>>(w_, 0, n, o, counts2_);
+            DIO_CK(cudaMemsetAsync(counts2_ + n, 0, 4, stream_));
+            size_t tb = cub_bytes_;
+            DIO_CK(cub::DeviceScan::ExclusiveSum(cub_tmp_, tb, counts2_, offsets2_, (int)n + 1, stream_));
+            k_cont_rows<P, R><<<grid_for(n, 128), 128, 0, stream_>>>(w_, 0, n, o, offsets2_, pair_rows);
+        } else {
+            DIO_CK(cudaMemsetAsync(offsets2_, 0, 4, stream_));
+        }
+        k_sum_rows<<<1, 1, 0, stream_>>>(ctr_, pair_rows, offsets2_ + n, w_.max_rows);
+        launches_ += 5;
+        return DIO_OK;
+    }
+
+    // warm start + decay + CSR for M rows (host-known count)
+    int finish_rows(const PrepParams<R>& o, uint32_t M, uint32_t n) {
+        int pb = 1 - cur_;
+        if (M) {
+            k_row_keys<<<grid_for(M, 256), 256, 0, stream_>>>(w_.ab, &ctr_->rows, M, keys_raw_, ids_raw_, inc_body_,
+                                                              inc_row_, n);
+            size_t tb = cub_bytes_;
+            DIO_CK(cub::DeviceRadixSort::SortPairs(cub_tmp_, tb, keys_raw_, keys_s_[cur_], ids_raw_, ids_s_[cur_],
+                                                   (int)M, 0, 64, stream_));
+            k_warm<P, R><<<grid_for(M, 256), 256, 0, stream_>>>(w_, &ctr_->rows, keys_s_[cur_], ids_s_[cur_],
+                                                                keys_s_[pb], ids_s_[pb], n_prev_rows_, rd_[pb], o);
+            tb = cub_bytes_;
+            DIO_CK(cub::DeviceRadixSort::SortPairs(cub_tmp_, tb, inc_body_, inc_body_s_, inc_row_, inc_row_s_,
+                                                   (int)(2 * M), 0, (int)bits_for(n + 1), stream_));
+        }
+        DIO_CK(cudaMemsetAsync(counts2_, 0, ((size_t)n + 1) * 4, stream_));
+        if (M) k_inc_count<<<grid_for(2 * M, 256), 256, 0, stream_>>>(inc_body_s_, &ctr_->rows, n, counts2_);
+        size_t tb = cub_bytes_;
+        DIO_CK(cub::DeviceScan::ExclusiveSum(cub_tmp_, tb, counts2_, w_.row_off, (int)n + 1, stream_));
+        if (M) k_csr_fill<P, R><<<grid_for(2 * M, 256), 256, 0, stream_>>>(w_, inc_body_s_, inc_row_s_, &ctr_->rows);
+        launches_ += M ? 4 : 0;
+        return DIO_OK;
+    }
+
+    int solve(const SolveParams<R>& o, uint32_t n, uint32_t m) {
+        if (n == 0) return DIO_OK;
+        int gb = grid_for(n, 256);
+        int gp = grid_for(n, 128);
+        int gm = grid_for(std::max(m, 1u), 256);
+        k_init<P, R><<<gb, 256, 0, stream_>>>(w_, 0, n, o);
+        launches_ += 2;
+        for (uint32_t k = 0; k < o.iterations; ++k) {
+            int par = (int)(k % 2);
+            cudaEvent_t e0 = span_begin();
+            k_primal<P, R><<<gp, 128, 0, stream_>>>(w_, 0, n, par, 1 - par, o);
+            span_end(e0, 0);
+            ++launches_;
+            if (m) {
+                cudaEvent_t e1 = span_begin();
+                k_dual<P, R><<<gm, 256, 0, stream_>>>(w_, 0, m, nullptr, 1 - par, o);
+                span_end(e1, 1);
+                ++launches_;
+            }
+        }
+        uint32_t fp = (o.iterations - 1u) % 2u;
+        int rb = fp == 0 ? 1 : 0;
+        uint32_t fp_read = (o.iterations == 0 ? 0u : o.iterations - 1u) % 2u;
+        int final_buf = 1 - (int)fp_read;
+        k_recover<P, R><<<gb, 256, 0, stream_>>>(w_, 0, n, rb, final_buf, o);
+        DIO_CK(cudaGetLastError());
+        return DIO_OK;
+    }
+
+    // kernel timing with CUDA events on the launching stream (profile on)
+    cudaEvent_t take_event() {
+        if (ev_free_.empty()) {
+            cudaEvent_t e = nullptr;
+            cudaEventCreate(&e);
+            return e;
+        }
+        cudaEvent_t e = ev_free_.back();
+        ev_free_.pop_back();
+        return e;
+    }
+    cudaEvent_t span_begin() {
+        if (!cfg_.profile) return nullptr;
+        cudaEvent_t e = take_event();
+        cudaEventRecord(e, stream_);
+        return e;
+    }
+    void span_end(cudaEvent_t e0, int kind) {
+        if (!e0) return;
+        cudaEvent_t e1 = take_event();
+        cudaEventRecord(e1, stream_);
+        spans_.push_back({e0, e1, kind});
+    }
+    void collect_spans() {
+        if (spans_.empty()) return;
+        cudaStreamSynchronize(stream_);
+        for (auto& s : spans_) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, s.a, s.b);
+            if (s.kind == 0) {
+                primal_ms_ += ms;
+                ++primal_n_;
+            } else {
+                dual_ms_ += ms;
+                ++dual_n_;
+            }
+            ev_free_.push_back(s.a);
+            ev_free_.push_back(s.b);
+        }
+        spans_.clear();
+    }
+
+   public:
+    int reset_timers() override {
+        collect_spans();
+        primal_ms_ = dual_ms_ = 0.0;
+        primal_n_ = dual_n_ = 0;
+        launches_ = 0;
+        return DIO_OK;
+    }
+
+   private:
+
+    int step_once(const DioAvbdOptions& opt) {
+        uint32_t n = w_.n;
+        PrepParams<R> pp = opts_prep(opt);
+        set_rows(cur_);
+        DIO_CK(cudaMemsetAsync(ctr_, 0, offsetof(Counters, error_flags), stream_));
+        if (n) DIO_TRY(run_broad(0, n));
+        DIO_TRY(run_narrow(cap_.max_pairs, &ctr_->pairs));
+        // pair-row groups are the pairs (bounded by the device pair count)
+        DIO_TRY(build_rows(pp, cap_.max_pairs, cfg_.contacts_per_pair, &ctr_->pairs, n));
+        DIO_TRY(pull_counters());
+        if (hctr_->error_flags) DIO_TRY(check_flags());
+        uint32_t M = hctr_->rows;
+        DIO_TRY(finish_rows(pp, M, n));
+        SolveParams<R> so = solve_params(opt.dt, opt.gravity, opt.alpha, opt.beta_lin, opt.penalty_max, opt.iterations);
+        DIO_TRY(solve(so, n, M));
+        n_prev_rows_ = M;
+        cur_ = 1 - cur_;
+        set_rows(cur_);
+        ++steps_;
+        return DIO_OK;
+    }
+
+    DioCapacity cap_;
+    cudaStream_t stream_;
+    DioConfig cfg_;
+    DevWorld<P, R> w_{};
+    std::vector<void*> allocs_;
+    uint32_t per_cap_ = 4;
+    int sms_ = 152;
+    RowStatic<R>* rs_[2] = {};
+    RowDual<P, R>* rd_[2] = {};
+    uint2* ab_[2] = {};
+    unsigned long long* keys_s_[2] = {};
+    uint32_t* ids_s_[2] = {};
+    unsigned long long* keys_raw_ = nullptr;
+    uint32_t* ids_raw_ = nullptr;
+    uint32_t *inc_body_ = nullptr, *inc_row_ = nullptr, *inc_body_s_ = nullptr, *inc_row_s_ = nullptr;
+    DioConstraint* joints_ = nullptr;
+    uint32_t *joint_off_ = nullptr, *joint_idx_ = nullptr;
+    uint32_t *counts_ = nullptr, *offsets_ = nullptr, *counts2_ = nullptr, *offsets2_ = nullptr;
+    SceneDesc* scenes_ = nullptr;
+    std::vector<SceneDesc> scenes_host_;
+    A4<P>* origin_ = nullptr;
+    A4<R>* hull_ = nullptr;
+    Counters* ctr_ = nullptr;
+    Counters* hctr_ = nullptr;
+    void* cub_tmp_ = nullptr;
+    size_t cub_bytes_ = 0;
+    void* dstage_ = nullptr;
+    void* hstage_ = nullptr;
+    size_t stage_bytes_ = 0;
+    int cur_ = 0;
+    uint32_t n_prev_rows_ = 0;
+    uint32_t api_bodies_ = 0, api_n_ = 0, api_m_ = 0, api_iters_ = 0, last_np_ = 0;
+    uint64_t steps_ = 0;
+    bool world_ready_ = false;
+    struct Span {
+        cudaEvent_t a, b;
+        int kind;
+    };
+    std::vector<Span> spans_;
+    std::vector<cudaEvent_t> ev_free_;
+    double primal_ms_ = 0.0, dual_ms_ = 0.0;
+    uint32_t primal_n_ = 0, dual_n_ = 0;
+    uint64_t launches_ = 0;
+};
+
+static __global__ void k_keys_only(const uint2* ab, uint32_t m, unsigned long long* keys, uint32_t* ids) {
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) {
+        keys[r] = row_key(ab[r]);
+        ids[r] = r;
+    }
+}
+
+template <class P, class R>
+int Engine<P, R>::sort_keys_n(const uint2* ab, uint32_t m, unsigned long long* keys_out, uint32_t* ids_out) {
+    k_keys_only<<<grid_for(m, 256), 256, 0, stream_>>>(ab, m, keys_raw_, ids_raw_);
+    size_t tb = cub_bytes_;
+    DIO_CK(cub::DeviceRadixSort::SortPairs(cub_tmp_, tb, keys_raw_, keys_out, ids_raw_, ids_out, (int)m, 0, 64,
+                                           stream_));
+    return DIO_OK;
+}
+
+template <class P, class R>
+EngineBase* make_engine_t(const DioCapacity& cap, cudaStream_t s, const DioConfig& cfg) {
+    auto* e = new Engine<P, R>(cap, s, cfg);
+    int rc = e->init();
+    if (rc != DIO_OK) {
+        std::string msg = e->err;
+        delete e;
+        return nullptr;
+    }
+    return e;
+}
+
+}  // namespace dio

@@ -1,0 +1,353 @@
+// k_avbd.cuh -- AVBD init / primal / dual / recover on sm_103a.
+//
+// Restates engine/gpu_physics/avbd/src/lib.rs:202-699.  Differences in
+// structure (not in arithmetic):
+//   * SoA poses (16-byte vector loads) instead of AoS Vec4 buffers.
+//   * Contacts are read through a per-body CSR that also carries the other
+//     body and the a/b side, so the row's (a, b) never has to be fetched.
+//   * Joints are read through a per-body joint CSR in joint order instead of
+//     the reference's scan over every joint for every body (O(N J)); the
+//     accumulation order per body is unchanged.
+//   * P (pose precision) may be double: inertial targets, poses and lambda
+//     accumulate in FP64 while the 6x6 Hessian, LDL^T and rows stay in R.
+//   * The final pose is also left in buffer 0, so a device-resident world
+//     starts every step from buffer 0.
+#pragma once
+
+#include "engine.cuh"
+
+namespace dio {
+
+template <class R>
+struct Block6 {
+    R h[21];  // lower triangle, row-major: (0,0) (1,0) (1,1) (2,0) ...
+    R g[6];
+};
+
+__device__ __forceinline__ constexpr int tri(int i, int j) { return i * (i + 1) / 2 + j; }
+
+// H += J J^T k, g += J f (add_constraint_row, avbd/src/lib.rs:182-198)
+template <class R>
+__device__ __forceinline__ void stamp(Block6<R>& B, V3<R> jl, V3<R> ja, R k, R f) {
+    const R J[6] = {jl.x, jl.y, jl.z, ja.x, ja.y, ja.z};
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+        for (int j = 0; j <= i; ++j) B.h[tri(i, j)] = B.h[tri(i, j)] + J[i] * J[j] * k;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) B.g[i] = B.g[i] + J[i] * f;
+}
+
+// solve6, avbd/src/lib.rs:107-180 (unpivoted LDL^T); solves H x = -g.
+template <class R>
+__device__ __forceinline__ void solve6(const Block6<R>& B, R x[6]) {
+    const R* H = B.h;
+    R a11 = H[tri(0, 0)], a21 = H[tri(1, 0)], a31 = H[tri(2, 0)], a22 = H[tri(1, 1)], a32 = H[tri(2, 1)],
+      a33 = H[tri(2, 2)];
+    R a41 = H[tri(3, 0)], a51 = H[tri(4, 0)], a61 = H[tri(5, 0)], a42 = H[tri(3, 1)], a52 = H[tri(4, 1)],
+      a62 = H[tri(5, 1)];
+    R a43 = H[tri(3, 2)], a53 = H[tri(4, 2)], a63 = H[tri(5, 2)];
+    R a44 = H[tri(3, 3)], a54 = H[tri(4, 3)], a64 = H[tri(5, 3)], a55 = H[tri(4, 4)], a65 = H[tri(5, 4)],
+      a66 = H[tri(5, 5)];
+    R l21 = a21 / a11, l31 = a31 / a11, l41 = a41 / a11, l51 = a51 / a11, l61 = a61 / a11;
+    R d1 = a11;
+    R d2 = a22 - l21 * l21 * d1;
+    R l32 = (a32 - l21 * l31 * d1) / d2;
+    R l42 = (a42 - l21 * l41 * d1) / d2;
+    R l52 = (a52 - l21 * l51 * d1) / d2;
+    R l62 = (a62 - l21 * l61 * d1) / d2;
+    R d3 = a33 - (l31 * l31 * d1 + l32 * l32 * d2);
+    R l43 = (a43 - l31 * l41 * d1 - l32 * l42 * d2) / d3;
+    R l53 = (a53 - l31 * l51 * d1 - l32 * l52 * d2) / d3;
+    R l63 = (a63 - l31 * l61 * d1 - l32 * l62 * d2) / d3;
+    R d4 = a44 - (l41 * l41 * d1 + l42 * l42 * d2 + l43 * l43 * d3);
+    R l54 = (a54 - l41 * l51 * d1 - l42 * l52 * d2 - l43 * l53 * d3) / d4;
+    R l64 = (a64 - l41 * l61 * d1 - l42 * l62 * d2 - l43 * l63 * d3) / d4;
+    R d5 = a55 - (l51 * l51 * d1 + l52 * l52 * d2 + l53 * l53 * d3 + l54 * l54 * d4);
+    R l65 = (a65 - l51 * l61 * d1 - l52 * l62 * d2 - l53 * l63 * d3 - l54 * l64 * d4) / d5;
+    R d6 = a66 - (l61 * l61 * d1 + l62 * l62 * d2 + l63 * l63 * d3 + l64 * l64 * d4 + l65 * l65 * d5);
+    R b0 = -B.g[0], b1 = -B.g[1], b2 = -B.g[2], b3 = -B.g[3], b4 = -B.g[4], b5 = -B.g[5];
+    R y1 = b0;
+    R y2 = b1 - l21 * y1;
+    R y3 = b2 - l31 * y1 - l32 * y2;
+    R y4 = b3 - l41 * y1 - l42 * y2 - l43 * y3;
+    R y5 = b4 - l51 * y1 - l52 * y2 - l53 * y3 - l54 * y4;
+    R y6 = b5 - l61 * y1 - l62 * y2 - l63 * y3 - l64 * y4 - l65 * y5;
+    R z1 = y1 / d1, z2 = y2 / d2, z3 = y3 / d3, z4 = y4 / d4, z5 = y5 / d5, z6 = y6 / d6;
+    x[5] = z6;
+    x[4] = z5 - l65 * x[5];
+    x[3] = z4 - l54 * x[4] - l64 * x[5];
+    x[2] = z3 - l43 * x[3] - l53 * x[4] - l63 * x[5];
+    x[1] = z2 - l32 * x[2] - l42 * x[3] - l52 * x[4] - l62 * x[5];
+    x[0] = z1 - l21 * x[1] - l31 * x[2] - l41 * x[3] - l51 * x[4] - l61 * x[5];
+}
+
+// avbd_init, avbd/src/lib.rs:202-254 (+ seeding buffer 1 with the
+// un-warm-started pose, render/gpu_physics.rs:479-482)
+template <class P, class R>
+__device__ __forceinline__ void init_body(const DevWorld<P, R>& w, uint32_t i, const SolveParams<R>& o) {
+    A4<P> p4 = w.pos[0][i];
+    A4<P> q4 = w.rot[0][i];
+    w.pos[1][i] = p4;
+    w.rot[1][i] = q4;
+    V3<P> pos = xyz(p4);
+    Q4<P> rot = quat(q4);
+    V3<P> vel = xyz(w.vel[i]);
+    V3<P> ang = xyz(w.ang[i]);
+    R inv_mass = w.inv[i].w;
+    P dt = P(o.dt);
+    V3<P> g{P(o.gx), P(o.gy), P(o.gz)};
+    w.init_pos[i] = pack(pos);
+    w.init_rot[i] = q4;
+    V3<P> ip = add(pos, scale(vel, dt));
+    if (inv_mass > R(0)) ip = add(ip, scale(g, dt * dt));
+    w.inert_pos[i] = pack(ip);
+    Q4<P> irot = quat_step(rot, scale(ang, dt));
+    w.inert_rot[i] = packq(irot);
+    if (inv_mass > R(0)) {
+        V3<P> accel = divs(sub(vel, xyz(w.prev_vel[i])), dt);
+        P gm = length(g);
+        P wgt = P(0);
+        if (gm > P(0)) {
+            wgt = dot(accel, divs(g, gm)) / gm;
+            wgt = wgt < P(0) ? P(0) : (wgt > P(1) ? P(1) : wgt);
+        }
+        w.pos[0][i] = pack(add(add(pos, scale(vel, dt)), scale(g, wgt * dt * dt)));
+        w.rot[0][i] = packq(quat_step(rot, scale(ang, dt)));
+    }
+}
+
+template <class P, class R>
+__global__ void __launch_bounds__(256) k_init(DevWorld<P, R> w, uint32_t lo, uint32_t hi, SolveParams<R> o) {
+    for (uint32_t i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += gridDim.x * blockDim.x)
+        init_body(w, i, o);
+}
+
+// One contact row seen from body i (avbd/src/lib.rs:321-418).
+template <class P, class R>
+__device__ __forceinline__ void primal_row(const DevWorld<P, R>& w, uint32_t r, uint32_t oth, int rd, Q4<R> sqr,
+                                           V3<R> dqsl, V3<R> dqsa, R k_alpha, Block6<R>& B) {
+    const RowStatic<R> rs = w.rs[r];
+    const RowDual<P, R> du = w.rd[r];
+    const bool container = oth == kContainer;
+    const bool is_a = container || !(oth & kIsB);
+    const uint32_t other = oth & ~kIsB;
+    V3<R> n = xyz(rs.n), t1 = xyz(rs.t1), t2 = xyz(rs.t2);
+    V3<R> r0 = is_a ? n : neg(n);
+    V3<R> r1 = is_a ? t1 : neg(t1);
+    V3<R> r2 = is_a ? t2 : neg(t2);
+    V3<R> rw = rotate(sqr, is_a ? xyz(rs.ra) : xyz(rs.rb));
+    V3<R> dol{R(0), R(0), R(0)}, doa{R(0), R(0), R(0)}, rot_other{R(0), R(0), R(0)};
+    if (!container) {
+        A4<P> op = w.pos[rd][other];
+        A4<P> oq = w.rot[rd][other];
+        dol = cast3<R>(sub(xyz(op), xyz(w.init_pos[other])));
+        doa = cast3<R>(ang_diff(quat(oq), quat(w.init_rot[other])));
+        rot_other = rotate(castq<R>(quat(oq)), is_a ? xyz(rs.rb) : xyz(rs.ra));
+    }
+    V3<R> j0 = cross(rw, r0), j1 = cross(rw, r1), j2 = cross(rw, r2);
+    R c0 = rs.ra.w * k_alpha, c1 = rs.rb.w * k_alpha, c2 = rs.t1.w * k_alpha;
+    c0 = c0 + (dot(r0, dqsl) + dot(j0, dqsa) - dot(r0, dol) - dot(cross(rot_other, r0), doa));
+    c1 = c1 + (dot(r1, dqsl) + dot(j1, dqsa) - dot(r1, dol) - dot(cross(rot_other, r1), doa));
+    c2 = c2 + (dot(r2, dqsl) + dot(j2, dqsa) - dot(r2, dol) - dot(cross(rot_other, r2), doa));
+    P f0 = fmin_(P(du.penalty.x * c0) + du.lambda.x, P(0));
+    P f1r = P(du.penalty.y * c1) + du.lambda.y;
+    P f2r = P(du.penalty.z * c2) + du.lambda.z;
+    P bounds = dabs(f0) * P(rs.n.w);
+    P tm = dsqrt(f1r * f1r + f2r * f2r);
+    P f1 = f1r, f2 = f2r;
+    if (tm > bounds && tm > P(0)) {
+        P s = bounds / tm;
+        f1 = f1r * s;
+        f2 = f2r * s;
+    }
+    stamp(B, r0, j0, du.penalty.x, R(f0));
+    stamp(B, r1, j1, du.penalty.y, R(f1));
+    stamp(B, r2, j2, du.penalty.z, R(f2));
+}
+
+// One joint seen from body i (avbd/src/lib.rs:425-537).
+template <class P, class R>
+__device__ __forceinline__ void primal_joint(const DevWorld<P, R>& w, const DioConstraint& jt, uint32_t i, int rd,
+                                             V3<P> sp, Q4<P> sq, Q4<R> sqr, Block6<R>& B) {
+    const bool is_a = jt.a == i;
+    V3<R> anc_a{R(jt.anchor_a[0]), R(jt.anchor_a[1]), R(jt.anchor_a[2])};
+    V3<R> anc_b{R(jt.anchor_b[0]), R(jt.anchor_b[1]), R(jt.anchor_b[2])};
+    V3<P> pa = is_a ? sp : xyz(w.pos[rd][jt.a]);
+    V3<P> pb = !is_a ? sp : xyz(w.pos[rd][jt.b]);
+    Q4<P> qa = is_a ? sq : quat(w.rot[rd][jt.a]);
+    Q4<P> qb = !is_a ? sq : quat(w.rot[rd][jt.b]);
+    V3<P> wpa = add(pa, rotate(qa, cast3<P>(anc_a)));
+    V3<P> wpb = add(pb, rotate(qb, cast3<P>(anc_b)));
+    V3<R> self_anchor = is_a ? anc_a : anc_b;
+    R sign = is_a ? R(1) : R(-1);
+    V3<R> delta = cast3<R>(sub(wpa, wpb));
+    V3<R> r_self = rotate(sqr, self_anchor);
+    R stiff = R(jt.anchor_b[3]);
+    if (jt.kind == DIO_CONSTRAINT_BALL_SOCKET) {
+        V3<R> jx = scale(V3<R>{R(1), R(0), R(0)}, sign);
+        V3<R> jy = scale(V3<R>{R(0), R(1), R(0)}, sign);
+        V3<R> jz = scale(V3<R>{R(0), R(0), R(1)}, sign);
+        stamp(B, jx, cross(r_self, jx), stiff, delta.x * stiff);
+        stamp(B, jy, cross(r_self, jy), stiff, delta.y * stiff);
+        stamp(B, jz, cross(r_self, jz), stiff, delta.z * stiff);
+    } else {
+        R len = length(delta);
+        R target = R(jt.anchor_a[3]);
+        bool active = len > R(1.0e-6) && (jt.kind != DIO_CONSTRAINT_ROPE || len > target);
+        if (active) {
+            V3<R> nn = divs(delta, len);
+            V3<R> jl = scale(nn, sign);
+            V3<R> ja = cross(r_self, jl);
+            stamp(B, jl, ja, stiff, stiff * (len - target));
+        }
+    }
+}
+
+// avbd_primal for one body: reads buffer rd, writes buffer wr.
+template <class P, class R>
+__device__ __forceinline__ void primal_body(const DevWorld<P, R>& w, uint32_t i, int rd, int wr,
+                                            const SolveParams<R>& o) {
+    const A4<R> inv = w.inv[i];
+    if (inv.w == R(0)) return;
+    const V3<P> sp = xyz(w.pos[rd][i]);
+    const Q4<P> sq = quat(w.rot[rd][i]);
+    const Q4<R> sqr = castq<R>(sq);
+    const R dt = o.dt;
+    const R mass = R(1) / inv.w;
+    const V3<R> moment{R(1) / inv.x, R(1) / inv.y, R(1) / inv.z};
+    const R dt2 = dt * dt;
+    const R mdt2 = mass / dt2;
+    const V3<R> idt2 = divs(moment, dt2);
+    Block6<R> B;
+#pragma unroll
+    for (int k = 0; k < 21; ++k) B.h[k] = R(0);
+    B.h[tri(0, 0)] = mdt2;
+    B.h[tri(1, 1)] = mdt2;
+    B.h[tri(2, 2)] = mdt2;
+    B.h[tri(3, 3)] = idt2.x;
+    B.h[tri(4, 4)] = idt2.y;
+    B.h[tri(5, 5)] = idt2.z;
+    const V3<R> rl = mulv(V3<R>{mdt2, mdt2, mdt2}, cast3<R>(sub(sp, xyz(w.inert_pos[i]))));
+    const V3<R> ra = mulv(idt2, cast3<R>(ang_diff(sq, quat(w.inert_rot[i]))));
+    B.g[0] = rl.x;
+    B.g[1] = rl.y;
+    B.g[2] = rl.z;
+    B.g[3] = ra.x;
+    B.g[4] = ra.y;
+    B.g[5] = ra.z;
+    const V3<R> dqsl = cast3<R>(sub(sp, xyz(w.init_pos[i])));
+    const V3<R> dqsa = cast3<R>(ang_diff(sq, quat(w.init_rot[i])));
+    const R k_alpha = R(1) - o.alpha;
+    const uint32_t j0 = w.row_off[i], j1 = w.row_off[i + 1];
+    for (uint32_t j = j0; j < j1; ++j) primal_row(w, w.row_idx[j], w.row_oth[j], rd, sqr, dqsl, dqsa, k_alpha, B);
+    if (w.n_joints) {
+        const uint32_t k0 = w.joint_off[i], k1 = w.joint_off[i + 1];
+        for (uint32_t k = k0; k < k1; ++k) {
+            const DioConstraint jt = w.joints[w.joint_idx[k]];
+            primal_joint(w, jt, i, rd, sp, sq, sqr, B);
+        }
+    }
+    R dx[6];
+    solve6(B, dx);
+    w.pos[wr][i] = pack(add(sp, cast3<P>(V3<R>{dx[0], dx[1], dx[2]})));
+    w.rot[wr][i] = packq(quat_step(sq, cast3<P>(V3<R>{dx[3], dx[4], dx[5]})));
+}
+
+template <class P, class R>
+__global__ void __launch_bounds__(128) k_primal(DevWorld<P, R> w, uint32_t lo, uint32_t hi, int rd, int wr,
+                                                SolveParams<R> o) {
+    for (uint32_t i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += gridDim.x * blockDim.x)
+        primal_body(w, i, rd, wr, o);
+}
+
+// Coloured Gauss-Seidel sweep: bodies color_order[c0 .. c1) in place.
+template <class P, class R>
+__global__ void __launch_bounds__(128) k_primal_color(DevWorld<P, R> w, uint32_t c0, uint32_t c1, SolveParams<R> o) {
+    for (uint32_t t = c0 + blockIdx.x * blockDim.x + threadIdx.x; t < c1; t += gridDim.x * blockDim.x)
+        primal_body(w, w.color_order[t], 0, 0, o);
+}
+
+// avbd_dual, avbd/src/lib.rs:565-663, for one row; `rd` holds the new state.
+template <class P, class R>
+__device__ __forceinline__ void dual_row(const DevWorld<P, R>& w, uint32_t c, int rd, const SolveParams<R>& o) {
+    const uint2 ab = w.ab[c];
+    const RowStatic<R> rs = w.rs[c];
+    RowDual<P, R> du = w.rd[c];
+    A4<P> pa4 = w.pos[rd][ab.x];
+    A4<P> qa4 = w.rot[rd][ab.x];
+    V3<R> dal = cast3<R>(sub(xyz(pa4), xyz(w.init_pos[ab.x])));
+    V3<R> daa = cast3<R>(ang_diff(quat(qa4), quat(w.init_rot[ab.x])));
+    V3<R> dbl{R(0), R(0), R(0)}, dba{R(0), R(0), R(0)}, rbw{R(0), R(0), R(0)};
+    if (ab.y != kContainer) {
+        A4<P> pb4 = w.pos[rd][ab.y];
+        A4<P> qb4 = w.rot[rd][ab.y];
+        dbl = cast3<R>(sub(xyz(pb4), xyz(w.init_pos[ab.y])));
+        dba = cast3<R>(ang_diff(quat(qb4), quat(w.init_rot[ab.y])));
+        rbw = rotate(castq<R>(quat(qb4)), xyz(rs.rb));
+    }
+    V3<R> raw = rotate(castq<R>(quat(qa4)), xyz(rs.ra));
+    V3<R> r0 = xyz(rs.n), r1 = xyz(rs.t1), r2 = xyz(rs.t2);
+    const R k_alpha = R(1) - o.alpha;
+    R c0 = rs.ra.w * k_alpha, c1 = rs.rb.w * k_alpha, c2 = rs.t1.w * k_alpha;
+    c0 = c0 + (dot(r0, dal) + dot(cross(raw, r0), daa) - dot(r0, dbl) - dot(cross(rbw, r0), dba));
+    c1 = c1 + (dot(r1, dal) + dot(cross(raw, r1), daa) - dot(r1, dbl) - dot(cross(rbw, r1), dba));
+    c2 = c2 + (dot(r2, dal) + dot(cross(raw, r2), daa) - dot(r2, dbl) - dot(cross(rbw, r2), dba));
+    P f0 = fmin_(P(du.penalty.x * c0) + du.lambda.x, P(0));
+    P f1r = P(du.penalty.y * c1) + du.lambda.y;
+    P f2r = P(du.penalty.z * c2) + du.lambda.z;
+    P bounds = dabs(f0) * P(rs.n.w);
+    P tm = dsqrt(f1r * f1r + f2r * f2r);
+    P f1 = f1r, f2 = f2r;
+    if (tm > bounds && tm > P(0)) {
+        P s = bounds / tm;
+        f1 = f1r * s;
+        f2 = f2r * s;
+    }
+    du.lambda.x = f0;
+    du.lambda.y = f1;
+    du.lambda.z = f2;
+    if (f0 < P(0)) du.penalty.x = fmin_(du.penalty.x + o.beta_lin * dabs(c0), o.penalty_max);
+    if (tm <= bounds) {
+        du.penalty.y = fmin_(du.penalty.y + o.beta_lin * dabs(c1), o.penalty_max);
+        du.penalty.z = fmin_(du.penalty.z + o.beta_lin * dabs(c2), o.penalty_max);
+    }
+    w.rd[c] = du;
+}
+
+template <class P, class R>
+__global__ void __launch_bounds__(256) k_dual(DevWorld<P, R> w, uint32_t lo, uint32_t hi, const uint32_t* dyn_hi,
+                                              int rd, SolveParams<R> o) {
+    uint32_t end = dyn_hi ? *dyn_hi : hi;
+    for (uint32_t c = lo + blockIdx.x * blockDim.x + threadIdx.x; c < end; c += gridDim.x * blockDim.x)
+        dual_row(w, c, rd, o);
+}
+
+// avbd_recover, avbd/src/lib.rs:667-699; also leaves the final pose in
+// buffer 0 when it lives in buffer 1.
+template <class P, class R>
+__device__ __forceinline__ void recover_body(const DevWorld<P, R>& w, uint32_t i, int rb, const SolveParams<R>& o) {
+    if (w.inv[i].w == R(0)) return;
+    A4<P> p4 = w.pos[rb][i];
+    A4<P> q4 = w.rot[rb][i];
+    P dt = P(o.dt);
+    A4<P> v = w.vel[i];
+    w.prev_vel[i] = v;
+    w.vel[i] = pack(divs(sub(xyz(p4), xyz(w.init_pos[i])), dt));
+    Q4<P> rel = qmul(quat(q4), conj(quat(w.init_rot[i])));
+    w.ang[i] = pack(divs(V3<P>{P(2) * rel.x, P(2) * rel.y, P(2) * rel.z}, dt));
+}
+
+template <class P, class R>
+__global__ void __launch_bounds__(256) k_recover(DevWorld<P, R> w, uint32_t lo, uint32_t hi, int rb, int final_buf,
+                                                 SolveParams<R> o) {
+    for (uint32_t i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += gridDim.x * blockDim.x) {
+        recover_body(w, i, rb, o);
+        if (final_buf != 0) {
+            w.pos[0][i] = w.pos[final_buf][i];
+            w.rot[0][i] = w.rot[final_buf][i];
+        }
+    }
+}
+
+}  // namespace dio

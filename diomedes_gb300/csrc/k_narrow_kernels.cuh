@@ -1,0 +1,119 @@
+// k_narrow_kernels.cuh -- narrowphase_main (narrowphase/src/lib.rs:89-158)
+// split into three stages: per-pair SAT / sphere, per-pair GJK, per-warp EPA.
+#pragma once
+
+#include "k_rows.cuh"
+
+namespace dio {
+
+template <class R>
+__device__ __forceinline__ void put_slot(Slot<R>* s, uint32_t a, uint32_t b, V3<R> n, R depth, V3<R> pa, V3<R> pb) {
+    Slot<R> o;
+    o.valid = 1;
+    o.a = a;
+    o.b = b;
+    o.pad = 0;
+    o.normal = pack(n);
+    o.depth = depth;
+    o.pad2[0] = o.pad2[1] = o.pad2[2] = R(0);
+    o.pa = pack(pa);
+    o.pb = pack(pb);
+    *s = o;
+}
+
+template <class R>
+__device__ __forceinline__ void clear_slot(Slot<R>* s) {
+    Slot<R> o;
+    o.valid = 0;
+    o.a = o.b = o.pad = 0;
+    o.normal = A4<R>{R(0), R(0), R(0), R(0)};
+    o.depth = R(0);
+    o.pad2[0] = o.pad2[1] = o.pad2[2] = R(0);
+    o.pa = o.normal;
+    o.pb = o.normal;
+    *s = o;
+}
+
+// Stage 1: one thread per pair.  `np_dev` (device pair count) bounds the
+// work when non-null, so the launch does not depend on a host read.
+template <class P, class R>
+__global__ void __launch_bounds__(128) k_narrow_main(DevWorld<P, R> w, const uint32_t* np_dev, uint32_t np_cap) {
+    uint32_t np = np_dev ? min(*np_dev, np_cap) : np_cap;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
+        Slot<R>* slots = w.slots + (size_t)p * w.per_pair;
+        for (uint32_t k = 0; k < w.per_pair; ++k) clear_slot(&slots[k]);
+        DioPair pr = w.pairs[p];
+        if (pr.a >= w.n || pr.b >= w.n) {
+            atomicOr(&w.ctr->error_flags, kErrBadIndex);
+            continue;
+        }
+        NB<R> a = load_nb(w, pr.a);
+        NB<R> b = load_nb(w, pr.b);
+        bool a_box = a.shape.tag == DIO_SHAPE_CUBE || a.shape.tag == DIO_SHAPE_BOX;
+        bool b_box = b.shape.tag == DIO_SHAPE_CUBE || b.shape.tag == DIO_SHAPE_BOX;
+        if (a_box && b_box) {
+            Manifold<R> m;
+            if (collide_manifold(a, b, w.per_pair, m))
+                for (uint32_t k = 0; k < m.count; ++k) put_slot(&slots[k], pr.a, pr.b, m.normal, m.depth, m.pa[k], m.pb[k]);
+        } else if (a.shape.tag == DIO_SHAPE_SPHERE && b.shape.tag == DIO_SHAPE_SPHERE) {
+            V3<R> delta = sub(b.pos, a.pos);
+            R dist = length(delta);
+            R radius = a.shape.c[0].x + b.shape.c[0].x;
+            if (!(dist >= radius || dist <= R(1.1920928955078125e-7))) {
+                V3<R> n = divs(delta, dist);
+                put_slot(&slots[0], pr.a, pr.b, n, radius - dist, add(a.pos, scale(n, a.shape.c[0].x)),
+                         sub(b.pos, scale(n, b.shape.c[0].x)));
+            }
+        } else {
+            uint32_t e = atomicAdd(&w.ctr->gjk_work, 1u);
+            w.gjk_list[e] = p;
+        }
+    }
+}
+
+// Stage 2: GJK, one thread per queued pair; intersecting pairs queue their
+// simplex (4 points then 4 witnesses) for EPA.
+template <class P, class R>
+__global__ void __launch_bounds__(128) k_gjk(DevWorld<P, R> w) {
+    uint32_t nw = w.ctr->gjk_work;
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < nw; e += gridDim.x * blockDim.x) {
+        uint32_t p = w.gjk_list[e];
+        DioPair pr = w.pairs[p];
+        NB<R> a = load_nb(w, pr.a);
+        NB<R> b = load_nb(w, pr.b);
+        Simplex<R> s;
+        if (gjk(a, b, w.hull, s)) {
+            uint32_t q = atomicAdd(&w.ctr->epa_work, 1u);
+            w.epa_list[q] = p;
+            A4<R>* dst = w.simplex + (size_t)q * 8;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                dst[k] = pack(s.p[k]);
+                dst[4 + k] = pack(s.w[k]);
+            }
+        }
+    }
+}
+
+// Stage 3: EPA, one warp per queued pair, polytope in shared memory.
+template <class P, class R>
+__global__ void __launch_bounds__(32 * kEpaWarps) k_epa(DevWorld<P, R> w) {
+    __shared__ EpaSmem<R> smem[kEpaWarps];
+    const uint32_t warp = threadIdx.x >> 5;
+    const uint32_t lane = threadIdx.x & 31;
+    EpaSmem<R>& S = smem[warp];
+    uint32_t nw = w.ctr->epa_work;
+    for (uint32_t q = blockIdx.x * kEpaWarps + warp; q < nw; q += gridDim.x * kEpaWarps) {
+        uint32_t p = w.epa_list[q];
+        DioPair pr = w.pairs[p];
+        NB<R> a = load_nb(w, pr.a);
+        NB<R> b = load_nb(w, pr.b);
+        V3<R> n, pa, pb;
+        R depth;
+        bool ok = epa_warp(S, a, b, w.simplex + (size_t)q * 8, w.hull, &w.ctr->error_flags, n, depth, pa, pb);
+        if (ok && lane == 0) put_slot(&w.slots[(size_t)p * w.per_pair], pr.a, pr.b, n, depth, pa, pb);
+        __syncwarp();
+    }
+}
+
+}  // namespace dio

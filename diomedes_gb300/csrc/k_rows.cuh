@@ -1,0 +1,308 @@
+// k_rows.cuh -- contact rows on the device.
+//
+// The reference builds rows on the host each frame: AvbdSolver::raw_contact
+// (engine/src/physics/gpu.rs:239-264), container_contacts (:352-404),
+// finalize_contacts (:266-311: warm start by (a, b), decay, CSR).  Here each
+// piece is a kernel over slots / bodies / rows:
+//   k_slot_count + scan  -> k_slot_rows      rows from valid narrow slots
+//   k_cont_count + scan  -> k_cont_rows      container (wall / floor) rows
+//   k_row_keys                               64-bit (a, b) keys + incidences
+//   (radix sorts of keys / incidences)
+//   k_warm                                   warm start + decay
+//   k_csr_fill                               CSR idx / other-body arrays
+#pragma once
+
+#include "k_narrow.cuh"
+
+namespace dio {
+
+// Detection-space body: pose rebased to the scene origin and rounded to R.
+template <class P, class R>
+__device__ __forceinline__ NB<R> load_nb(const DevWorld<P, R>& w, uint32_t i) {
+    NB<R> b;
+    V3<P> org{P(0), P(0), P(0)};
+    if (w.origin) org = xyz(w.origin[w.scene[i]]);
+    b.pos = cast3<R>(sub(xyz(w.pos[0][i]), org));
+    b.rot = castq<R>(quat(w.rot[0][i]));
+    b.shape = load_shape<R>(&w.shape[i]);
+    return b;
+}
+
+// tangents, engine/src/physics/gpu.rs:406-414
+template <class R>
+__device__ __forceinline__ void tangents(V3<R> n, V3<R>& t1, V3<R>& t2) {
+    V3<R> c = dabs(n.x) > R(0.9) ? cross(n, V3<R>{R(0), R(1), R(0)}) : cross(n, V3<R>{R(1), R(0), R(0)});
+    t1 = normalize(c);
+    t2 = cross(n, t1);
+}
+
+template <class P, class R>
+__device__ __forceinline__ void write_row(const DevWorld<P, R>& w, uint32_t r, uint32_t a, uint32_t b, V3<R> n,
+                                          V3<R> t1, V3<R> t2, V3<R> ra, V3<R> rb, V3<R> c0, R friction, R kmin) {
+    RowStatic<R> rs;
+    rs.n = pack(n, friction);
+    rs.t1 = pack(t1, c0.z);
+    rs.t2 = pack(t2, R(0));
+    rs.ra = pack(ra, c0.x);
+    rs.rb = pack(rb, c0.y);
+    w.rs[r] = rs;
+    RowDual<P, R> du;
+    du.penalty = A4<R>{kmin, kmin, kmin, R(0)};
+    du.lambda = A4<P>{P(0), P(0), P(0), P(0)};
+    w.rd[r] = du;
+    w.ab[r] = make_uint2(a, b);
+}
+
+// Valid slots of the first `n_groups` groups of `per` slots.
+template <class R>
+__global__ void k_slot_count(const Slot<R>* slots, uint32_t per, const uint32_t* n_groups_dev, uint32_t n_groups,
+                             uint32_t* counts) {
+    uint32_t ng = n_groups_dev ? *n_groups_dev : n_groups;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n_groups; p += gridDim.x * blockDim.x) {
+        uint32_t c = 0;
+        if (p < ng)
+            for (uint32_t k = 0; k < per; ++k) c += slots[p * per + k].valid ? 1u : 0u;
+        counts[p] = c;
+    }
+}
+
+// raw_contact for every valid slot, rows at `offsets[group]` in slot order.
+template <class P, class R>
+__global__ void k_slot_rows(DevWorld<P, R> w, const Slot<R>* slots, uint32_t per, const uint32_t* n_groups_dev,
+                            uint32_t n_groups, const uint32_t* offsets, PrepParams<R> o) {
+    uint32_t ng = n_groups_dev ? *n_groups_dev : n_groups;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < ng && p < n_groups; p += gridDim.x * blockDim.x) {
+        uint32_t r = offsets[p];
+        for (uint32_t k = 0; k < per; ++k) {
+            const Slot<R> s = slots[p * per + k];
+            if (!s.valid) continue;
+            if (s.a >= w.n || s.b >= w.n) {
+                atomicOr(&w.ctr->error_flags, kErrBadIndex);
+                continue;
+            }
+            if (r >= w.max_rows) {
+                atomicOr(&w.ctr->error_flags, kErrRowOverflow);
+                return;
+            }
+            NB<R> A = load_nb(w, s.a), B = load_nb(w, s.b);
+            V3<R> nrm = xyz(s.normal);
+            V3<R> t1, t2;
+            tangents(nrm, t1, t2);
+            V3<R> ra = rotate(conj(A.rot), sub(xyz(s.pa), A.pos));
+            V3<R> rb = rotate(conj(B.rot), sub(xyz(s.pb), B.pos));
+            write_row(w, r, s.a, s.b, neg(nrm), t1, t2, ra, rb, V3<R>{o.margin - s.depth, R(0), R(0)}, o.friction,
+                      o.penalty_min);
+            ++r;
+        }
+    }
+}
+
+// cube_support_face, engine/src/physics/gpu.rs:314-350 (per-axis for BOX)
+template <class R>
+__device__ __forceinline__ void support_face(const NB<R>& b, V3<R> outward, V3<R> pts[4]) {
+    V3<R> ax[3];
+    axes_of(b.rot, ax);
+    uint32_t ai = 0;
+    R best = dabs(dot(ax[0], outward));
+    for (uint32_t i = 1; i < 3; ++i) {
+        R al = dabs(dot(ax[i], outward));
+        if (al > best) {
+            ai = i;
+            best = al;
+        }
+    }
+    V3<R> h = box_half(b.shape);
+    V3<R> center, u, v;
+    R eu, ev;
+    face_frame(b.pos, ax, h, ai, outward, pts, center, u, v, eu, ev);
+}
+
+// container_contacts for one body (engine/src/physics/gpu.rs:352-404):
+// counts (write == false) or writes rows starting at `r`.
+template <class P, class R>
+__device__ __forceinline__ uint32_t container_rows(const DevWorld<P, R>& w, uint32_t i, const SceneDesc& sc,
+                                                   const PrepParams<R>& o, bool write_out, uint32_t r) {
+    NB<R> b = load_nb(w, i);
+    V3<P> org{P(0), P(0), P(0)};
+    if (w.origin) org = xyz(w.origin[w.scene[i]]);
+    V3<R> center = cast3<R>(sub(V3<P>{P(sc.center[0]), P(sc.center[1]), P(sc.center[2])}, org));
+    Q4<R> crot{R(sc.rotation[0]), R(sc.rotation[1]), R(sc.rotation[2]), R(sc.rotation[3])};
+    R half = R(sc.half_extent);
+    V3<R> vel = cast3<R>(xyz(w.vel[i]));
+    const bool boxy = b.shape.tag == DIO_SHAPE_CUBE || b.shape.tag == DIO_SHAPE_BOX;
+    uint32_t count = 0;
+#pragma unroll 1
+    for (int k = 0; k < 6; ++k) {
+        V3<R> axis = k < 2 ? V3<R>{R(1), R(0), R(0)} : (k < 4 ? V3<R>{R(0), R(1), R(0)} : V3<R>{R(0), R(0), R(1)});
+        R sign = (k & 1) ? R(-1) : R(1);
+        V3<R> outward = rotate(crot, scale(axis, sign));
+        R plane = dot(center, outward) + half;
+        V3<R> pts[4];
+        uint32_t np;
+        if (boxy) {
+            support_face(b, outward, pts);
+            np = 4;
+        } else {
+            V3<R> local = rotate(conj(b.rot), outward);
+            pts[0] = add(rotate(b.rot, support(b.shape, local, w.hull)), b.pos);
+            np = 1;
+        }
+        V3<R> normal = neg(outward);
+        V3<R> t1, t2;
+        if (write_out) tangents(normal, t1, t2);
+        for (uint32_t p = 0; p < np; ++p) {
+            V3<R> cp = pts[p];
+            R cur = dot(cp, outward) - plane;
+            V3<R> pred = add(cp, scale(vel, o.dt));
+            R pd = dot(pred, outward) - plane;
+            R depth = fmax_(cur, pd);
+            if (depth > R(0)) {
+                if (write_out) {
+                    if (r + count < w.max_rows) {
+                        V3<R> ra = rotate(conj(b.rot), sub(cp, b.pos));
+                        write_row(w, r + count, i, kContainer, normal, t1, t2, ra, V3<R>{R(0), R(0), R(0)},
+                                  V3<R>{o.margin - depth, R(0), R(0)}, o.friction, o.penalty_min);
+                    } else {
+                        atomicOr(&w.ctr->error_flags, kErrRowOverflow);
+                    }
+                }
+                ++count;
+            }
+        }
+    }
+    return count;
+}
+
+template <class P, class R>
+__global__ void k_cont_count(DevWorld<P, R> w, uint32_t lo, uint32_t hi, PrepParams<R> o, uint32_t* counts) {
+    for (uint32_t i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += gridDim.x * blockDim.x) {
+        uint32_t c = 0;
+        const SceneDesc sc = w.scenes[w.scene[i]];
+        if (w.inv[i].w != R(0) && sc.has_container) c = container_rows(w, i, sc, o, false, 0);
+        counts[i - lo] = c;
+    }
+}
+
+template <class P, class R>
+__global__ void k_cont_rows(DevWorld<P, R> w, uint32_t lo, uint32_t hi, PrepParams<R> o, const uint32_t* offsets,
+                            const uint32_t* base_dev) {
+    uint32_t base = *base_dev;
+    for (uint32_t i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += gridDim.x * blockDim.x) {
+        const SceneDesc sc = w.scenes[w.scene[i]];
+        if (w.inv[i].w != R(0) && sc.has_container) container_rows(w, i, sc, o, true, base + offsets[i - lo]);
+    }
+}
+
+__device__ __forceinline__ unsigned long long row_key(uint2 ab) {
+    return ((unsigned long long)ab.x << 32) | (unsigned long long)ab.y;
+}
+
+// Keys + row ids for the warm-start sorts, and the (body, row) incidences of
+// the CSR (two per row; b == CONTAINER becomes the sentinel body `n`).
+static __global__ void k_row_keys(const uint2* ab, const uint32_t* m_dev, uint32_t cap, unsigned long long* keys,
+                           uint32_t* ids, uint32_t* inc_body, uint32_t* inc_row, uint32_t n_sentinel) {
+    uint32_t m = *m_dev;
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < cap; r += gridDim.x * blockDim.x) {
+        if (r < m) {
+            uint2 v = ab[r];
+            if (keys) {
+                keys[r] = row_key(v);
+                ids[r] = r;
+            }
+            if (inc_body) {
+                inc_body[2 * r] = v.x;
+                inc_row[2 * r] = r;
+                inc_body[2 * r + 1] = v.y == kContainer ? n_sentinel : v.y;
+                inc_row[2 * r + 1] = r;
+            }
+        } else {
+            if (keys) {
+                keys[r] = ~0ull;
+                ids[r] = r;
+            }
+            if (inc_body) {
+                inc_body[2 * r] = n_sentinel;
+                inc_row[2 * r] = r;
+                inc_body[2 * r + 1] = n_sentinel;
+                inc_row[2 * r + 1] = r;
+            }
+        }
+    }
+}
+
+// Warm start + decay (finalize_contacts, gpu.rs:266-283).  new_keys/new_ids
+// are the new rows' keys stably sorted; prev_keys/prev_ids the previous
+// rows'.  The first new row of each key takes (lambda, penalty) of the LAST
+// previous row with that key; every row then decays.
+template <class P, class R>
+__global__ void k_warm(DevWorld<P, R> w, const uint32_t* m_dev, const unsigned long long* new_keys,
+                       const uint32_t* new_ids, const unsigned long long* prev_keys, const uint32_t* prev_ids,
+                       uint32_t n_prev, const RowDual<P, R>* prev_dual, PrepParams<R> o) {
+    uint32_t m = *m_dev;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < m; t += gridDim.x * blockDim.x) {
+        unsigned long long key = new_keys[t];
+        uint32_t r = new_ids[t];
+        RowDual<P, R> du = w.rd[r];
+        bool first = t == 0 || new_keys[t - 1] != key;
+        if (first && n_prev > 0) {
+            // upper bound of key in prev_keys -> last occurrence is ub - 1
+            uint32_t lo = 0, hi = n_prev;
+            while (lo < hi) {
+                uint32_t mid = (lo + hi) >> 1;
+                if (prev_keys[mid] <= key)
+                    lo = mid + 1;
+                else
+                    hi = mid;
+            }
+            if (lo > 0 && prev_keys[lo - 1] == key) {
+                const RowDual<P, R> pd = prev_dual[prev_ids[lo - 1]];
+                du.lambda = pd.lambda;
+                du.penalty = pd.penalty;
+            }
+        }
+        P ag = P(o.alpha_gamma);
+        du.lambda.x = du.lambda.x * ag;
+        du.lambda.y = du.lambda.y * ag;
+        du.lambda.z = du.lambda.z * ag;
+        R kx = du.penalty.x * o.gamma, ky = du.penalty.y * o.gamma, kz = du.penalty.z * o.gamma;
+        du.penalty.x = fmin_(fmax_(kx, o.penalty_min), o.penalty_max);
+        du.penalty.y = fmin_(fmax_(ky, o.penalty_min), o.penalty_max);
+        du.penalty.z = fmin_(fmax_(kz, o.penalty_min), o.penalty_max);
+        w.rd[r] = du;
+    }
+}
+
+// Per-body counts of the sorted incidences -> offsets are the exclusive
+// scan; the fill keeps the sorted (row-ascending) order per body.
+static __global__ void k_inc_count(const uint32_t* inc_body_sorted, const uint32_t* m_dev, uint32_t n, uint32_t* counts) {
+    uint32_t total = 2 * *m_dev;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < total; j += gridDim.x * blockDim.x) {
+        uint32_t b = inc_body_sorted[j];
+        if (b < n) atomicAdd(&counts[b], 1u);
+    }
+}
+
+template <class P, class R>
+__global__ void k_csr_fill(DevWorld<P, R> w, const uint32_t* inc_body_sorted, const uint32_t* inc_row_sorted,
+                           const uint32_t* m_dev) {
+    uint32_t total = 2 * *m_dev;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < total; j += gridDim.x * blockDim.x) {
+        uint32_t b = inc_body_sorted[j];
+        if (b >= w.n) continue;  // container sentinels sort last
+        uint32_t r = inc_row_sorted[j];
+        uint2 ab = w.ab[r];
+        uint32_t oth;
+        if (ab.y == kContainer)
+            oth = kContainer;
+        else if (ab.x == b)
+            oth = ab.y;
+        else
+            oth = ab.x | kIsB;
+        if (j < w.max_incid) {
+            w.row_idx[j] = r;
+            w.row_oth[j] = oth;
+        }
+    }
+}
+
+}  // namespace dio

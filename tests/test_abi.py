@@ -1,0 +1,69 @@
+"""CPU checks of the boundary: the library loads, exports every symbol the
+header declares, and the record layouts match the reference's byte sizes."""
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from diomedes_gb300 import abi, physics as ph
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "dio_cuda.h")
+
+
+def _declared():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"^(?:int|const char\*)\s+(dio_\w+)\(", text, re.M)))
+
+
+@pytest.fixture(scope="module")
+def library():
+    if not os.path.exists(abi.LIB_PATH):
+        from diomedes_gb300 import build
+
+        build.build()
+    return ctypes.CDLL(abi.LIB_PATH)
+
+
+def test_library_exports_every_declared_symbol(library):
+    names = _declared()
+    assert len(names) >= 25
+    for n in names:
+        assert hasattr(library, n), n
+    # and the ctypes table covers the whole header
+    assert set(names) == set(abi._PROTOS), set(names) ^ set(abi._PROTOS)
+
+
+def test_exported_symbols_are_plain_c(library):
+    out = subprocess.run(["nm", "-D", "--defined-only", abi.LIB_PATH], capture_output=True, text=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    for n in _declared():
+        assert n in exported, n  # unmangled extern "C"
+
+
+def test_record_sizes_match_the_reference_layouts():
+    # compute.rs GpuShape 80, GpuBody 112, GpuPair 8, GpuContactOut 80;
+    # gpu_physics.rs GpuAvbdBodyState 80, GpuAvbdContact 144, GpuAvbdConstraint 48
+    assert [abi.SHAPE.itemsize, abi.BODY.itemsize, abi.PAIR.itemsize, abi.CONTACT_OUT.itemsize] == [80, 112, 8, 80]
+    assert [abi.BODY_STATE.itemsize, abi.CONTACT.itemsize, abi.CONSTRAINT.itemsize] == [80, 144, 48]
+    assert ctypes.sizeof(abi.RunOptions) == 32 and ctypes.sizeof(abi.AvbdOptions) == 48
+
+
+def test_body_constructors_follow_the_reference():
+    b, s = ph.sphere((0, 0, 0), 0.3, 1.0)
+    assert s["inv_mass"] == np.float32(1.0)
+    assert s["inv_moment"][0] == np.float32(1.0) / (np.float32(0.4) * np.float32(1.0) * np.float32(0.3) * np.float32(0.3))
+    b, s = ph.cube((0, 0, 0), 0.5, 2.0)
+    assert b["shape"]["tag"] == abi.CUBE and b["shape"]["corners"][0, :3].tolist() == [0.5, 0.5, 0.5]
+    assert s["friction"] == np.float32(0.8)
+    b, s = ph.cube((0, 0, 0), 0.5, 0.0)
+    assert s["inv_mass"] == 0 and (s["inv_moment"] == 0).all()
+
+
+def test_default_options_match_avbd_options_default():
+    o = ph.avbd_options()
+    assert (o.iterations, round(o.alpha, 6), o.beta_lin, round(o.margin, 6), o.penalty_min) == (10, 0.99, 1e4, 0.01, 1.0)
+    assert list(o.gravity) == [0.0, -10.0, 0.0]

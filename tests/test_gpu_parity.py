@@ -1,0 +1,208 @@
+"""CUDA path vs the CPU oracle through the C ABI, on identical inputs.
+
+Integer results (pair sets, slot validity, row counts, CSR) must match bit
+for bit; float results are compared bit for bit where the kernels evaluate
+the same expressions in the same order (they are built with --fmad=false),
+and otherwise within the stated tolerance."""
+import numpy as np
+import pytest
+
+import oracle_lib as O
+from diomedes_gb300 import abi, compute, physics as ph, scenes
+
+pytestmark = pytest.mark.gpu
+
+# one-step state tolerance (relative, with an absolute floor) for paths whose
+# summation order is not forced to match the oracle's
+REL_TOL = 1e-5
+
+
+def small_scenes():
+    return [
+        scenes.pyramid(levels=4),
+        scenes.constraints_demo(),
+        scenes.box_demo(),
+        scenes.cube_field(nx=6, nz=6, ny=3),
+        scenes.mixed_pile(n=600, extent=6.0),
+    ]
+
+
+def _bits(a):
+    return np.ascontiguousarray(a).view(np.uint8)
+
+
+def test_broad_pair_sets_bit_exact():
+    for sc in small_scenes():
+        ref, nref = O.broad(sc.bodies, hull=sc.hull_vertices)
+        with compute.NarrowPhaseCompute(sc.n, max(16, 64 * sc.n), max_hull_vertices=max(1, len(sc.hull_vertices) if sc.hull_vertices is not None else 1)) as npc:
+            if sc.hull_vertices is not None:
+                npc.set_hull_vertices(sc.hull_vertices)
+            npc.submit_broad(sc.bodies)
+            count = npc.read_pair_count()
+            pairs = npc.read_pairs(count)
+        assert count == nref, sc.name
+        assert np.array_equal(pairs, ref), sc.name
+
+
+def test_narrow_slots_bit_exact():
+    for sc in small_scenes():
+        pairs, _ = O.broad(sc.bodies, hull=sc.hull_vertices)
+        if len(pairs) == 0:
+            continue
+        ref = O.narrow(sc.bodies, pairs, hull=sc.hull_vertices)
+        hv = sc.hull_vertices if sc.hull_vertices is not None else np.zeros((1, 4), np.float32)
+        with compute.NarrowPhaseCompute(sc.n, len(pairs), max_hull_vertices=len(hv)) as npc:
+            npc.set_hull_vertices(hv)
+            got = npc.run(sc.bodies, pairs)
+        assert np.array_equal(got["valid"], ref["valid"]), sc.name
+        assert np.array_equal(_bits(got), _bits(ref)), sc.name
+
+
+def test_broad_then_narrow_on_device_pairs():
+    sc = scenes.cube_field(nx=5, nz=5, ny=2)
+    with compute.NarrowPhaseCompute(sc.n, 64 * sc.n) as npc:
+        npc.submit_broad(sc.bodies)
+        count = npc.read_pair_count()
+        npc.submit_narrow(count)
+        got = npc.read()
+    pairs, _ = O.broad(sc.bodies)
+    ref = O.narrow(sc.bodies, pairs)
+    assert np.array_equal(_bits(got), _bits(ref))
+
+
+def _prep_inputs(sc):
+    pairs, _ = O.broad(sc.bodies, hull=sc.hull_vertices)
+    slots = O.narrow(sc.bodies, pairs, hull=sc.hull_vertices)
+    return slots
+
+
+def test_prepare_contacts_rows_and_csr_bit_exact():
+    for sc in [scenes.pyramid(levels=4), scenes.box_demo(), scenes.cube_field(nx=4, nz=4, ny=2)]:
+        slots = _prep_inputs(sc)
+        cont = sc.containers[0] if sc.containers else None
+        o = sc.options
+        rows0, off0, idx0 = O.prepare_contacts(sc.bodies, sc.state, slots, None, cont, o)
+        # a previous step's rows with non-trivial lambda / penalty
+        prev = rows0.copy()
+        prev["lambda"][:, :3] = -np.arange(len(prev) * 3, dtype=np.float32).reshape(-1, 3)
+        prev["penalty"][:, :3] = 5.0 + np.arange(len(prev) * 3, dtype=np.float32).reshape(-1, 3)
+        ref, roff, ridx = O.prepare_contacts(sc.bodies, sc.state, slots, prev, cont, o)
+        with compute.AvbdCompute(sc.n, max(64, 4 * len(ref) + 64), max_pairs=max(16, len(slots))) as ac:
+            got, goff, gidx = ac.prepare_contacts(sc.bodies, sc.state, slots, prev, cont, o)
+        assert len(got) == len(ref), sc.name
+        assert np.array_equal(goff, roff) and np.array_equal(gidx, ridx), sc.name
+        assert np.array_equal(_bits(got), _bits(ref)), sc.name
+
+
+def _avbd_inputs(sc):
+    slots = _prep_inputs(sc)
+    cont = sc.containers[0] if sc.containers else None
+    rows, off, idx = O.prepare_contacts(sc.bodies, sc.state, slots, None, cont, sc.options)
+    return rows, off, idx
+
+
+def test_avbd_run_matches_oracle():
+    for sc in [scenes.pyramid(levels=4), scenes.constraints_demo(), scenes.box_demo(),
+               scenes.cube_field(nx=4, nz=4, ny=2)]:
+        rows, off, idx = _avbd_inputs(sc)
+        ro = ph.run_options(sc.options)
+        args = (sc.state, sc.bodies["position"][:, :3], sc.bodies["orientation"], rows, sc.constraints, off, idx, ro)
+        ref = O.avbd_run(*args)
+        with compute.AvbdCompute(sc.n, max(64, len(rows)), max_joints=max(1, len(sc.constraints))) as ac:
+            got = ac.run(*args)
+        for k in ref:
+            assert np.array_equal(_bits(got[k]), _bits(ref[k])), (sc.name, k)
+
+
+def _world(sc, **cfg):
+    cap = compute.capacity(sc.n, max_pairs=max(64, 40 * sc.n), max_contacts=max(256, 200 * sc.n),
+                           max_joints=max(1, len(sc.constraints)), max_scenes=sc.n_scenes,
+                           max_hull_vertices=max(1, len(sc.hull_vertices) if sc.hull_vertices is not None else 1))
+    w = compute.World(cap, **cfg)
+    w.upload(sc.bodies, sc.state, **sc.upload_kwargs())
+    return w
+
+
+@pytest.mark.parametrize("steps", [1, 60])
+def test_world_steps_match_oracle(steps):
+    for sc in small_scenes():
+        ow = O.World(sc)
+        ow.step(sc.options, steps)
+        rb, rs = ow.download()
+        rc = ow.contacts()
+        with _world(sc) as w:
+            w.step(sc.options, steps)
+            gb, gs = w.download()
+            gc = w.contacts()
+            st = w.stats()
+        assert st["error_flags"] == 0
+        assert len(gc) == len(rc), sc.name
+        assert np.array_equal(_bits(gb), _bits(rb)), (sc.name, steps)
+        assert np.array_equal(_bits(gs), _bits(rs)), (sc.name, steps)
+        assert np.array_equal(_bits(gc), _bits(rc)), (sc.name, steps)
+
+
+def test_batched_world_equals_each_scene_alone():
+    parts = [scenes.pyramid(levels=3), scenes.constraints_demo(), scenes.box_demo(),
+             scenes.cube_field(nx=3, nz=3, ny=2)]
+    for p in parts:
+        p.options = parts[0].options
+    packed = scenes.pack(parts)
+    with _world(packed) as w:
+        w.step(packed.options, 5)
+        gb, gs = w.download()
+    for k, p in enumerate(parts):
+        lo, hi = packed.scene_offsets[k], packed.scene_offsets[k + 1]
+        if not p.containers:
+            p.containers = [packed.containers[k]]
+        with _world(p) as w1:
+            w1.step(packed.options, 5)
+            b1, s1 = w1.download()
+        assert np.array_equal(_bits(gb[lo:hi]), _bits(b1)), p.name
+        assert np.array_equal(_bits(gs[lo:hi]), _bits(s1)), p.name
+
+
+def test_empty_inputs():
+    with compute.NarrowPhaseCompute(8, 64) as npc:
+        npc.submit_broad(np.zeros(0, abi.BODY))
+        assert npc.read_pair_count() == 0
+        assert len(npc.run(np.zeros(0, abi.BODY), np.zeros(0, abi.PAIR))) == 0
+    with compute.AvbdCompute(8, 64) as ac:
+        out = ac.run(np.zeros(0, abi.BODY_STATE), np.zeros((0, 3), np.float32), np.zeros((0, 4), np.float32),
+                     np.zeros(0, abi.CONTACT), np.zeros(0, abi.CONSTRAINT), np.zeros(1, np.uint32),
+                     np.zeros(0, np.uint32), ph.run_options(ph.avbd_options()))
+        assert len(out["positions"]) == 0
+
+
+def test_capacity_errors_are_reported():
+    sc = scenes.cube_field(nx=4, nz=4, ny=2)
+    with compute.NarrowPhaseCompute(sc.n, 4) as npc:
+        npc.submit_broad(sc.bodies)
+        with pytest.raises(abi.DioError) as e:
+            npc.read_pair_count()
+        assert e.value.status == abi.DIO_ERR_CAPACITY
+    with pytest.raises(abi.DioError) as e:
+        with compute.NarrowPhaseCompute(4, 64) as npc:
+            npc.submit_broad(sc.bodies)
+    assert e.value.status == abi.DIO_ERR_CAPACITY
+
+
+def test_bad_indices_are_rejected():
+    sc = scenes.pyramid(levels=2)
+    with compute.NarrowPhaseCompute(sc.n, 64) as npc:
+        with pytest.raises(abi.DioError) as e:
+            npc.run(sc.bodies, np.array([(0, 99)], abi.PAIR))
+        assert e.value.status == abi.DIO_ERR_INVALID
+
+
+def test_zero_iterations_follow_reference_parities():
+    sc = scenes.pyramid(levels=3)
+    rows, off, idx = _avbd_inputs(sc)
+    o = ph.avbd_options(iterations=0)
+    ro = ph.run_options(o)
+    args = (sc.state, sc.bodies["position"][:, :3], sc.bodies["orientation"], rows, sc.constraints, off, idx, ro)
+    ref = O.avbd_run(*args)
+    with compute.AvbdCompute(sc.n, max(64, len(rows))) as ac:
+        got = ac.run(*args)
+    for k in ref:
+        assert np.array_equal(_bits(got[k]), _bits(ref[k])), k
