@@ -160,13 +160,18 @@ def joint_scene(rng, n_bodies):
     n_loose = int(rng.integers(0, min(200, n_bodies // 2) + 1))
     budget = n_bodies - n_loose
     link_r = 0.05
-    x = -0.5 * budget * 0.02
+    # chains hang from static anchors on a 2 m grid in x-z (all inside the
+    # container, clear of each other's swing at rest)
+    grid = int(np.ceil(np.sqrt(max(1, budget / 8.0))))
+    slot = 0
     kind = 0
     while budget > 0:
         length = int(min(budget, rng.integers(2, 21)))
         base = len(items)
-        top = 6.0 + rng.uniform(0.0, 2.0)
-        z = rng.uniform(-5.0, 5.0)
+        x = (slot % grid - grid / 2.0) * 2.0
+        z = (slot // grid - grid / 2.0) * 2.0
+        slot += 1
+        top = 12.0 + rng.uniform(0.0, 2.0)
         items.append(ph.sphere((x, top, z), link_r, 0.0))  # static anchor
         for k in range(1, length):
             if kind == 0:  # rope chain
@@ -185,12 +190,13 @@ def joint_scene(rng, n_bodies):
                 joints.append(ph.spring(a, b, (0, 0, 0), (0, 0, 0), 1e3, 0.5))
         budget -= length
         kind = (kind + 1) % 3
-        x += 1.0
+    # loose boxes on a 0.5 m grid beside the chain grid
     side = int(np.ceil(np.sqrt(max(n_loose, 1))))
+    x0 = grid + 4.0
     for k in range(n_loose):
         i, j = k % side, k // side
         h = float(rng.uniform(0.1, 0.2))
-        p = (-20.0 + i * 0.5 + rng.uniform(-0.02, 0.02), h + 0.02 + rng.uniform(0, 0.5), -10.0 + j * 0.5)
+        p = (x0 + i * 0.5 + rng.uniform(-0.02, 0.02), h + 0.02 + rng.uniform(0, 0.5), -4.0 + j * 0.5)
         items.append(ph.cube(p, h, 8 * h ** 3 * 1000.0))
     return items, joints
 
@@ -215,7 +221,7 @@ def batched(n_scenes=1024, lo=16, hi=2048, seed=4):
     cons = ph.pack_joints(all_joints)
     o = ph.avbd_options(gravity=(0, -9.81, 0), iterations=10)
     return Scene(f"batched{n_scenes}", b, st, constraints=cons, scene_offsets=np.array(offsets, np.uint32),
-                 containers=[ground(100.0)] * n_scenes, options=o, steps=600)
+                 containers=[ground(1000.0)] * n_scenes, options=o, steps=600)
 
 
 def wall_throw(cols=400, rows=500, projectiles=1000, offset=1.0e5, seed=5):
