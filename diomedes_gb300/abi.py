@@ -124,6 +124,8 @@ _PROTOS = {
     "dio_avbd_submit": [_P, _vp, _vp, _vp, _u32, _vp, _u32, _vp, _u32, _vp, _vp,
                         ctypes.POINTER(RunOptions)],
     "dio_avbd_read": [_P, ctypes.POINTER(AvbdResult)],
+    "dio_avbd_solve_noalloc": [_vp, _vp, _vp, _u32, _vp, _u32, _vp, _u32, _vp, _vp, ctypes.POINTER(RunOptions),
+                               _vp, _vp, _vp, _vp],
     "dio_world_upload": [_P, ctypes.POINTER(WorldDesc)],
     "dio_step": [_P, ctypes.POINTER(AvbdOptions), _u32],
     "dio_world_set_state": [_P, _vp, _vp],

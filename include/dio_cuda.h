@@ -321,6 +321,31 @@ int dio_avbd_submit(DioCtx* ctx, const DioBodyState* state,
 /* AvbdCompute::read, engine/src/render/gpu_physics.rs:565-622 */
 int dio_avbd_read(DioCtx* ctx, const DioAvbdResult* out);
 
+/* No counterpart in the reference.  The AVBD solve of dio_avbd_submit for
+ * callers that may not allocate device memory (a host that owns its device
+ * memory through another allocator, or a real-time loop that must not
+ * allocate once running).  Needs no context; every pointer is DEVICE
+ * memory the caller owns: state (n), positions (n * 3), orientations
+ * (n * 4), contacts (m; lambda and penalty are updated in place),
+ * constraints, offsets (n + 1) and indices (offsets[n]).  Results go to
+ * out_positions (n * 3), out_orientations (n * 4) and out_state (n; may
+ * alias state).  Scratch lives in a fixed device array of the library
+ * (about 3 MB per GPU, held until exit): at most 4096 bodies, 16384
+ * contacts and 4096 joints, else DIO_ERR_CAPACITY.  Joints are scanned per
+ * body as in the reference.  Calls share that array, so calls that overlap
+ * on the GPU race.  The first call on each device looks up the array's
+ * address; make it before any stream capture.  Synchronous: returns once
+ * the solve on `cuda_stream` (NULL = default stream) has finished. */
+int dio_avbd_solve_noalloc(const DioBodyState* state, const float* positions,
+                           const float* orientations, uint32_t n,
+                           DioContact* contacts, uint32_t m,
+                           const DioConstraint* constraints,
+                           uint32_t n_constraints, const uint32_t* offsets,
+                           const uint32_t* indices,
+                           const DioRunOptions* options, float* out_positions,
+                           float* out_orientations, DioBodyState* out_state,
+                           void* cuda_stream);
+
 /* ------------------------------------------- fused device-resident step */
 /* Upload a world (one or many packed scenes).  Replaces the per-frame
  * uploads of demos/avbd_box/src/main.rs:232-271. */
