@@ -84,7 +84,7 @@ class Capacity(ctypes.Structure):
 class Config(ctypes.Structure):
     _fields_ = [("solver_mode", _u32), ("precision", _u32), ("contacts_per_pair", _u32),
                 ("use_graph", _u32), ("primal_group", _u32), ("block_size", _u32),
-                ("batched_solver", _u32), ("profile", _u32)]
+                ("batched_solver", _u32), ("profile", _u32), ("broad_phase", _u32), ("reserved", _u32 * 3)]
 
 
 class WorldDesc(ctypes.Structure):
@@ -97,7 +97,9 @@ class WorldDesc(ctypes.Structure):
 class StepStats(ctypes.Structure):
     _fields_ = [("pairs", _u32), ("contacts", _u32), ("colors", _u32), ("error_flags", _u32),
                 ("steps", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64), ("primal_launches", _u32),
-                ("dual_launches", _u32), ("primal_ms", ctypes.c_double), ("dual_ms", ctypes.c_double)]
+                ("dual_launches", _u32), ("primal_ms", ctypes.c_double), ("dual_ms", ctypes.c_double),
+                ("broad_ms", ctypes.c_double), ("narrow_ms", ctypes.c_double), ("rows_ms", ctypes.c_double),
+                ("solve_ms", ctypes.c_double)]
 
 
 # every symbol include/dio_cuda.h declares, with its argument types

@@ -277,7 +277,8 @@ class World(Context):
         check(self.L.dio_world_stats(self.h, ctypes.byref(s)), self.h, "stats")
         return {"pairs": s.pairs, "contacts": s.contacts, "colors": s.colors, "error_flags": s.error_flags,
                 "steps": s.steps, "kernel_launches": s.kernel_launches, "primal_launches": s.primal_launches,
-                "dual_launches": s.dual_launches, "primal_ms": s.primal_ms, "dual_ms": s.dual_ms}
+                "dual_launches": s.dual_launches, "primal_ms": s.primal_ms, "dual_ms": s.dual_ms,
+                "broad_ms": s.broad_ms, "narrow_ms": s.narrow_ms, "rows_ms": s.rows_ms, "solve_ms": s.solve_ms}
 
     def reset_timers(self):
         check(self.L.dio_world_reset_timers(self.h), self.h, "reset_timers")

@@ -32,7 +32,7 @@ DioConfig default_config() {
     c.solver_mode = DIO_SOLVER_JACOBI;
     c.precision = DIO_PREC_F32;
     c.contacts_per_pair = DIO_CONTACTS_PER_PAIR;
-    c.use_graph = 0;
+    c.use_graph = 1;
     c.primal_group = 1;
     c.block_size = 128;
     c.batched_solver = 0;

@@ -52,7 +52,10 @@ struct Counters {
     uint32_t colors;
     uint32_t color_remaining;
     uint32_t scene_cursor;
-    uint32_t pad[6];
+    uint32_t prev_rows;       // rows of the previous step (warm-start source)
+    uint32_t prev_pair_rows;  // of which from narrow-phase slots
+    uint32_t long_count;      // CSR segments too long for the in-thread sort
+    uint32_t pad[3];
 };
 
 // Static part of one contact row (80 B at R = float):

@@ -13,6 +13,7 @@
 #include "engine_base.h"
 #include "k_avbd.cuh"
 #include "k_broad.cuh"
+#include "k_lbvh.cuh"
 #include "k_narrow_kernels.cuh"
 #include "k_rows.cuh"
 
@@ -300,6 +301,7 @@ class Engine final : public EngineBase {
    public:
     Engine(const DioCapacity& cap, cudaStream_t s, const DioConfig& cfg) : cap_(cap), stream_(s), cfg_(cfg) {}
     ~Engine() override {
+        drop_graphs();
         collect_spans();
         for (auto e : ev_free_) cudaEventDestroy(e);
         release();
@@ -339,6 +341,22 @@ class Engine final : public EngineBase {
         DIO_TRY(alloc(&w_.gjk_list, PP));
         DIO_TRY(alloc(&w_.epa_list, PP));
         DIO_TRY(alloc(&w_.simplex, (size_t)PP * 8));
+        // LBVH
+        DIO_TRY(alloc(&lb_bounds_, 6ull * S));
+        DIO_TRY(alloc(&lb_keys_, N));
+        DIO_TRY(alloc(&lb_keys_s_, N));
+        DIO_TRY(alloc(&lb_vals_, N));
+        DIO_TRY(alloc(&lb_leaf_, N));
+        DIO_TRY(alloc(&lb_children_, N));
+        DIO_TRY(alloc(&lb_parent_, 2ull * N));
+        DIO_TRY(alloc(&lb_visits_, N));
+        DIO_TRY(alloc(&lb_leaf_min_, N));
+        DIO_TRY(alloc(&lb_leaf_max_, N));
+        DIO_TRY(alloc(&lb_node_min_, N));
+        DIO_TRY(alloc(&lb_node_max_, N));
+        DIO_TRY(alloc(&lb_pb_, PP));
+        DIO_TRY(alloc(&lb_long_, N));
+        DIO_TRY(alloc(&lb_long_count_, 1));
         for (int b = 0; b < 2; ++b) {
             DIO_TRY(alloc(&rs_[b], M));
             DIO_TRY(alloc(&rd_[b], M));
@@ -370,8 +388,8 @@ class Engine final : public EngineBase {
         DIO_CK(cudaMallocHost(&hctr_, sizeof(Counters)));
         // CUB temporary storage for the largest sort / scan
         size_t t1 = 0, t2 = 0, t3 = 0;
-        cub::DeviceRadixSort::SortPairs(nullptr, t1, keys_raw_, keys_s_[0], ids_raw_, ids_s_[0], (int)M, 0, 64,
-                                        stream_);
+        cub::DeviceRadixSort::SortPairs(nullptr, t1, keys_raw_, keys_s_[0], ids_raw_, ids_s_[0], (int)std::max(M, N),
+                                        0, 64, stream_);
         cub::DeviceRadixSort::SortPairs(nullptr, t2, inc_body_, inc_body_s_, inc_row_, inc_row_s_, (int)INC, 0, 32,
                                         stream_);
         cub::DeviceScan::ExclusiveSum(nullptr, t3, counts_, offsets_, (int)CNT, stream_);
@@ -409,6 +427,7 @@ class Engine final : public EngineBase {
 
     void set_stream(cudaStream_t s) override { stream_ = s; }
     void set_config(const DioConfig& c) override {
+        drop_graphs();
         uint32_t per = cfg_.contacts_per_pair;
         cfg_ = c;
         if (c.contacts_per_pair != 4 && c.contacts_per_pair != 8) cfg_.contacts_per_pair = per;
@@ -623,6 +642,7 @@ class Engine final : public EngineBase {
         if (ns > cap_.max_scenes) return cap_err("too many scenes");
         if (d->n_hull_vertices > cap_.max_hull_vertices) return cap_err("too many hull vertices");
         if (n && (!d->bodies || !d->state)) return inval("null bodies/state");
+        drop_graphs();
         DIO_TRY(upload_bodies(d->bodies, n));
         if (d->positions_f64 || d->orientations_f64) {
             double* dp = reinterpret_cast<double*>(dstage_);
@@ -682,8 +702,14 @@ class Engine final : public EngineBase {
     int step(const DioAvbdOptions* options, uint32_t steps) override {
         if (!options) return inval("null options");
         if (!world_ready_) return state_err("no world uploaded");
-        for (uint32_t k = 0; k < steps; ++k) DIO_TRY(step_once(*options));
-        return DIO_OK;
+        for (uint32_t k = 0; k < steps; ++k) {
+            if (cfg_.use_graph)
+                DIO_TRY(step_graph(*options));
+            else
+                DIO_TRY(step_once_dev(*options));
+        }
+        // one synchronisation per call: device-side error flags
+        return check_flags();
     }
 
     int set_state(const DioGpuBody* bodies, const DioBodyState* state) override {
@@ -733,7 +759,8 @@ class Engine final : public EngineBase {
     int contacts(DioContact* out, uint32_t cap, uint32_t* m) override {
         // rows of the last step live in the "previous" buffer after the swap
         int pb = 1 - cur_;
-        uint32_t M = n_prev_rows_;
+        DIO_TRY(pull_counters());
+        uint32_t M = steps_ ? hctr_->rows : 0;
         if (m) *m = M;
         if (M > cap) return cap_err("output buffer smaller than the row count");
         if (!M) return DIO_OK;
@@ -771,6 +798,10 @@ class Engine final : public EngineBase {
         out->dual_launches = dual_n_;
         out->primal_ms = primal_ms_;
         out->dual_ms = dual_ms_;
+        out->broad_ms = phase_ms_[0];
+        out->narrow_ms = phase_ms_[1];
+        out->rows_ms = phase_ms_[2];
+        out->solve_ms = phase_ms_[3];
         return DIO_OK;
     }
 
@@ -927,6 +958,7 @@ class Engine final : public EngineBase {
         uint32_t n = hi - lo;
         int g = grid_for(n, 128);
         k_aabb<P, R><<<g, 128, 0, stream_>>>(w_, lo, hi);
+        if (cfg_.broad_phase == 0 && lo == 0) return run_lbvh(n);
         constexpr int kB = 128;
         int gd = grid_for(n, kB);
         k_dense<P, R, kB><<<gd, kB, 0, stream_>>>(w_, lo, hi, counts_, offsets_, false);
@@ -936,6 +968,43 @@ class Engine final : public EngineBase {
         k_dense<P, R, kB><<<gd, kB, 0, stream_>>>(w_, lo, hi, counts_, offsets_, true);
         k_pairs_total<<<1, 1, 0, stream_>>>(ctr_, offsets_ + n, w_.max_pairs);
         launches_ += 4;
+        return DIO_OK;
+    }
+
+    // LBVH over every scene of bodies [0, n); AABBs already computed
+    int run_lbvh(uint32_t n) {
+        uint32_t ns = std::max(1u, w_.n_scenes);
+        int g = grid_for(n, 256);
+        k_bounds_init<<<grid_for(ns, 128), 128, 0, stream_>>>(lb_bounds_, ns);
+        k_scene_bounds<R><<<g, 256, 0, stream_>>>(w_.aabb_min, w_.aabb_max, w_.scene, n, lb_bounds_);
+        const uint32_t sbits = ns > 1 ? bits_for(ns - 1) : 0;
+        const uint32_t abits = std::min(10u, (32u - sbits) / 3u);
+        k_morton<R><<<g, 256, 0, stream_>>>(w_.aabb_min, w_.aabb_max, w_.scene, n, lb_bounds_, sbits, abits, lb_keys_,
+                                            lb_vals_);
+        size_t tb = cub_bytes_;
+        DIO_CK(cub::DeviceRadixSort::SortPairs(cub_tmp_, tb, lb_keys_, lb_keys_s_, lb_vals_, lb_leaf_, (int)n, 0,
+                                               (int)(sbits + 3 * abits), stream_));
+        DIO_CK(cudaMemsetAsync(lb_visits_, 0, (size_t)n * 4, stream_));
+        k_karras<<<g, 256, 0, stream_>>>(lb_keys_s_, scenes_, w_.scene, n, lb_children_, lb_parent_);
+        k_refit<R><<<g, 256, 0, stream_>>>(w_.aabb_min, w_.aabb_max, lb_leaf_, scenes_, w_.scene, n, lb_children_,
+                                           lb_parent_, lb_leaf_min_, lb_leaf_max_, lb_node_min_, lb_node_max_,
+                                           lb_visits_);
+        int gt = grid_for(n, 128);
+        k_traverse<R><<<gt, 128, 0, stream_>>>(lb_leaf_, scenes_, w_.scene, n, lb_children_, lb_leaf_min_,
+                                               lb_leaf_max_, lb_node_min_, lb_node_max_, counts_, offsets_, lb_pb_,
+                                               w_.max_pairs, false, &ctr_->error_flags);
+        DIO_CK(cudaMemsetAsync(counts_ + n, 0, 4, stream_));
+        tb = cub_bytes_;
+        DIO_CK(cub::DeviceScan::ExclusiveSum(cub_tmp_, tb, counts_, offsets_, (int)n + 1, stream_));
+        k_traverse<R><<<gt, 128, 0, stream_>>>(lb_leaf_, scenes_, w_.scene, n, lb_children_, lb_leaf_min_,
+                                               lb_leaf_max_, lb_node_min_, lb_node_max_, counts_, offsets_, lb_pb_,
+                                               w_.max_pairs, true, &ctr_->error_flags);
+        k_pairs_total<<<1, 1, 0, stream_>>>(ctr_, offsets_ + n, w_.max_pairs);
+        DIO_CK(cudaMemsetAsync(lb_long_count_, 0, 4, stream_));
+        k_sort_segments<<<g, 256, 0, stream_>>>(offsets_, n, w_.max_pairs, lb_pb_, lb_long_, lb_long_count_);
+        k_sort_long<<<sms_, 512, 0, stream_>>>(offsets_, lb_pb_, lb_long_, lb_long_count_, &ctr_->error_flags);
+        k_pairs_from_segments<<<g, 256, 0, stream_>>>(offsets_, n, lb_pb_, w_.pairs, w_.max_pairs);
+        launches_ += 12;
         return DIO_OK;
     }
 
@@ -1002,11 +1071,13 @@ class Engine final : public EngineBase {
         return DIO_OK;
     }
 
-    int solve(const SolveParams<R>& o, uint32_t n, uint32_t m) {
+    // m_dev: device row count (fixed grid, device-bounded loops) or null (host m)
+    int solve(const SolveParams<R>& o, uint32_t n, uint32_t m, const uint32_t* m_dev = nullptr) {
         if (n == 0) return DIO_OK;
         int gb = grid_for(n, 256);
         int gp = grid_for(n, 128);
-        int gm = grid_for(std::max(m, 1u), 256);
+        int gm = m_dev ? std::min(grid_for(cap_.max_contacts, 256), sms_ * 8) : grid_for(std::max(m, 1u), 256);
+        if (m_dev) m = cap_.max_contacts;
         k_init<P, R><<<gb, 256, 0, stream_>>>(w_, 0, n, o);
         launches_ += 2;
         for (uint32_t k = 0; k < o.iterations; ++k) {
@@ -1017,7 +1088,7 @@ class Engine final : public EngineBase {
             ++launches_;
             if (m) {
                 cudaEvent_t e1 = span_begin();
-                k_dual<P, R><<<gm, 256, 0, stream_>>>(w_, 0, m, nullptr, 1 - par, o);
+                k_dual<P, R><<<gm, 256, 0, stream_>>>(w_, 0, m, m_dev, 1 - par, o);
                 span_end(e1, 1);
                 ++launches_;
             }
@@ -1042,17 +1113,27 @@ class Engine final : public EngineBase {
         ev_free_.pop_back();
         return e;
     }
+    // inside a capture an event record must be external to become a graph node
+    void record(cudaEvent_t e) {
+        if (capturing_)
+            cudaEventRecordWithFlags(e, stream_, cudaEventRecordExternal);
+        else
+            cudaEventRecord(e, stream_);
+    }
     cudaEvent_t span_begin() {
         if (!cfg_.profile) return nullptr;
         cudaEvent_t e = take_event();
-        cudaEventRecord(e, stream_);
+        record(e);
         return e;
     }
     void span_end(cudaEvent_t e0, int kind) {
         if (!e0) return;
         cudaEvent_t e1 = take_event();
-        cudaEventRecord(e1, stream_);
-        spans_.push_back({e0, e1, kind});
+        record(e1);
+        if (capturing_)
+            cap_spans_.push_back({e0, e1, kind});  // placeholders, rebound per replay
+        else
+            spans_.push_back({e0, e1, kind});
     }
     void collect_spans() {
         if (spans_.empty()) return;
@@ -1063,9 +1144,11 @@ class Engine final : public EngineBase {
             if (s.kind == 0) {
                 primal_ms_ += ms;
                 ++primal_n_;
-            } else {
+            } else if (s.kind == 1) {
                 dual_ms_ += ms;
                 ++dual_n_;
+            } else {
+                phase_ms_[s.kind - 2] += ms;
             }
             ev_free_.push_back(s.a);
             ev_free_.push_back(s.b);
@@ -1078,27 +1161,182 @@ class Engine final : public EngineBase {
         collect_spans();
         primal_ms_ = dual_ms_ = 0.0;
         primal_n_ = dual_n_ = 0;
+        for (double& x : phase_ms_) x = 0.0;
         launches_ = 0;
         return DIO_OK;
     }
 
    private:
 
+    // One step with every count kept on the device: no host synchronisation,
+    // fixed launch shapes, so the whole step can be captured in a graph.
+    int step_body_dev(const DioAvbdOptions& opt) {
+        uint32_t n = w_.n;
+        PrepParams<R> pp = opts_prep(opt);
+        set_rows(cur_);
+        k_roll_counters<<<1, 1, 0, stream_>>>(ctr_);
+        ++launches_;
+        cudaEvent_t e = span_begin();
+        if (n) DIO_TRY(run_broad(0, n));
+        span_end(e, 2);
+        e = span_begin();
+        DIO_TRY(run_narrow(cap_.max_pairs, &ctr_->pairs));
+        span_end(e, 3);
+        e = span_begin();
+        DIO_TRY(build_rows(pp, cap_.max_pairs, cfg_.contacts_per_pair, &ctr_->pairs, n));
+        DIO_TRY(finish_rows_world(pp, n));
+        span_end(e, 4);
+        SolveParams<R> so = solve_params(opt.dt, opt.gravity, opt.alpha, opt.beta_lin, opt.penalty_max, opt.iterations);
+        e = span_begin();
+        DIO_TRY(solve(so, n, 0, &ctr_->rows));
+        span_end(e, 5);
+        return DIO_OK;
+    }
+
+    int step_once_dev(const DioAvbdOptions& opt) {
+        DIO_TRY(step_body_dev(opt));
+        cur_ = 1 - cur_;
+        set_rows(cur_);
+        ++steps_;
+        return DIO_OK;
+    }
+
+    // warm start + decay + dynamic-body CSR, all bounded by device counts
+    int finish_rows_world(const PrepParams<R>& o, uint32_t n) {
+        int pb = 1 - cur_;
+        const int gf = std::min(grid_for(cap_.max_contacts, 256), sms_ * 8);
+        k_warm_sections<P, R><<<gf, 256, 0, stream_>>>(w_, ab_[pb], rd_[pb], o);
+        DIO_CK(cudaMemsetAsync(counts2_, 0, ((size_t)n + 1) * 4, stream_));
+        k_csr_count_dyn<P, R><<<gf, 256, 0, stream_>>>(w_, counts2_);
+        size_t tb = cub_bytes_;
+        DIO_CK(cub::DeviceScan::ExclusiveSum(cub_tmp_, tb, counts2_, w_.row_off, (int)n + 1, stream_));
+        DIO_CK(cudaMemsetAsync(counts2_, 0, ((size_t)n + 1) * 4, stream_));
+        k_csr_scatter_dyn<P, R><<<gf, 256, 0, stream_>>>(w_, counts2_);
+        int gn = grid_for(n, 256);
+        k_sort_segments<<<gn, 256, 0, stream_>>>(w_.row_off, n, w_.max_incid, w_.row_idx, lb_long_,
+                                                &ctr_->long_count);
+        k_sort_long<<<sms_, 512, 0, stream_>>>(w_.row_off, w_.row_idx, lb_long_, &ctr_->long_count,
+                                              &ctr_->error_flags);
+        k_csr_other_dyn<P, R><<<gn, 256, 0, stream_>>>(w_);
+        launches_ += 6;
+        return DIO_OK;
+    }
+
+    // ---- CUDA graph of one step, one per row-buffer parity ------------
+    struct GraphSlot {
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        DioAvbdOptions opt{};
+        std::vector<std::pair<cudaGraphNode_t, cudaGraphNode_t>> span_nodes;
+        std::vector<int> span_kinds;
+    };
+    GraphSlot graphs_[2];
+
+    void drop_graphs() {
+        for (auto& g : graphs_) {
+            if (g.exec) cudaGraphExecDestroy(g.exec);
+            if (g.graph) cudaGraphDestroy(g.graph);
+            g = GraphSlot();
+        }
+    }
+
+    int capture(GraphSlot& g, const DioAvbdOptions& opt) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        if (g.graph) cudaGraphDestroy(g.graph);
+        g = GraphSlot();
+        cap_spans_.clear();
+        DIO_CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+        capturing_ = true;
+        const uint64_t l0 = launches_;
+        int rc = step_body_dev(opt);
+        launches_per_step_ = launches_ - l0;  // counted at replay, not capture
+        launches_ = l0;
+        capturing_ = false;
+        cudaGraph_t graph = nullptr;
+        cudaError_t ce = cudaStreamEndCapture(stream_, &graph);
+        if (rc != DIO_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+        }
+        DIO_CK(ce);
+        // map the captured event-record nodes back to their spans
+        size_t count = 0;
+        DIO_CK(cudaGraphGetNodes(graph, nullptr, &count));
+        std::vector<cudaGraphNode_t> nodes(count);
+        DIO_CK(cudaGraphGetNodes(graph, nodes.data(), &count));
+        std::vector<std::pair<cudaEvent_t, cudaGraphNode_t>> ev_nodes;
+        for (auto nd : nodes) {
+            cudaGraphNodeType t;
+            DIO_CK(cudaGraphNodeGetType(nd, &t));
+            if (t == cudaGraphNodeTypeEventRecord) {
+                cudaEvent_t ev;
+                DIO_CK(cudaGraphEventRecordNodeGetEvent(nd, &ev));
+                ev_nodes.push_back({ev, nd});
+            }
+        }
+        auto find = [&](cudaEvent_t ev) -> cudaGraphNode_t {
+            for (auto& p : ev_nodes)
+                if (p.first == ev) return p.second;
+            return nullptr;
+        };
+        for (auto& s : cap_spans_) {
+            g.span_nodes.push_back({find(s.a), find(s.b)});
+            g.span_kinds.push_back(s.kind);
+        }
+        DIO_CK(cudaGraphInstantiate(&g.exec, graph, 0));
+        g.graph = graph;  // its node handles address the exec's event nodes
+        g.opt = opt;
+        // the placeholder events now belong to the graph's nodes only
+        for (auto& s : cap_spans_) {
+            ev_free_.push_back(s.a);
+            ev_free_.push_back(s.b);
+        }
+        cap_spans_.clear();
+        return DIO_OK;
+    }
+
+    int step_graph(const DioAvbdOptions& opt) {
+        GraphSlot& g = graphs_[cur_];
+        if (!g.exec || std::memcmp(&g.opt, &opt, sizeof opt) != 0) DIO_TRY(capture(g, opt));
+        for (size_t k = 0; k < g.span_nodes.size(); ++k) {
+            if (!g.span_nodes[k].first || !g.span_nodes[k].second) continue;
+            cudaEvent_t e0 = take_event(), e1 = take_event();
+            DIO_CK(cudaGraphExecEventRecordNodeSetEvent(g.exec, g.span_nodes[k].first, e0));
+            DIO_CK(cudaGraphExecEventRecordNodeSetEvent(g.exec, g.span_nodes[k].second, e1));
+            spans_.push_back({e0, e1, g.span_kinds[k]});
+        }
+        DIO_CK(cudaGraphLaunch(g.exec, stream_));
+        launches_ += launches_per_step_;
+        cur_ = 1 - cur_;
+        set_rows(cur_);
+        ++steps_;
+        return DIO_OK;
+    }
+    uint64_t launches_per_step_ = 0;
+
     int step_once(const DioAvbdOptions& opt) {
         uint32_t n = w_.n;
         PrepParams<R> pp = opts_prep(opt);
         set_rows(cur_);
         DIO_CK(cudaMemsetAsync(ctr_, 0, offsetof(Counters, error_flags), stream_));
+        cudaEvent_t e = span_begin();
         if (n) DIO_TRY(run_broad(0, n));
+        span_end(e, 2);
+        e = span_begin();
         DIO_TRY(run_narrow(cap_.max_pairs, &ctr_->pairs));
+        span_end(e, 3);
         // pair-row groups are the pairs (bounded by the device pair count)
+        e = span_begin();
         DIO_TRY(build_rows(pp, cap_.max_pairs, cfg_.contacts_per_pair, &ctr_->pairs, n));
         DIO_TRY(pull_counters());
         if (hctr_->error_flags) DIO_TRY(check_flags());
         uint32_t M = hctr_->rows;
         DIO_TRY(finish_rows(pp, M, n));
+        span_end(e, 4);
         SolveParams<R> so = solve_params(opt.dt, opt.gravity, opt.alpha, opt.beta_lin, opt.penalty_max, opt.iterations);
+        e = span_begin();
         DIO_TRY(solve(so, n, M));
+        span_end(e, 5);
         n_prev_rows_ = M;
         cur_ = 1 - cur_;
         set_rows(cur_);
@@ -1145,8 +1383,18 @@ class Engine final : public EngineBase {
         int kind;
     };
     std::vector<Span> spans_;
+    bool capturing_ = false;
+    std::vector<Span> cap_spans_;
     std::vector<cudaEvent_t> ev_free_;
+    // LBVH buffers
+    uint32_t* lb_bounds_ = nullptr;
+    uint32_t *lb_keys_ = nullptr, *lb_keys_s_ = nullptr;
+    uint32_t *lb_vals_ = nullptr, *lb_leaf_ = nullptr, *lb_parent_ = nullptr, *lb_visits_ = nullptr;
+    uint2* lb_children_ = nullptr;
+    A4<R>*lb_leaf_min_ = nullptr, *lb_leaf_max_ = nullptr, *lb_node_min_ = nullptr, *lb_node_max_ = nullptr;
+    uint32_t *lb_pb_ = nullptr, *lb_long_ = nullptr, *lb_long_count_ = nullptr;
     double primal_ms_ = 0.0, dual_ms_ = 0.0;
+    double phase_ms_[4] = {0.0, 0.0, 0.0, 0.0};  // broad, narrow, rows, solve
     uint32_t primal_n_ = 0, dual_n_ = 0;
     uint64_t launches_ = 0;
 };

@@ -1,0 +1,342 @@
+// k_lbvh.cuh -- LBVH broad phase (replaces broad_sweep_dense,
+// engine/gpu_physics/broadphase/src/lib.rs:171-216, at scale).
+//
+// Per step, for every scene at once:
+//   k_scene_bounds   centroid bounds per scene (ordered-int atomics)
+//   k_morton         30-bit Morton code of each AABB centre within its scene's
+//                    bounds; key = scene << 32 | code (scenes stay contiguous)
+//   radix sort       (key, body) pairs
+//   k_karras         binary radix tree per scene (Karras 2012), internal node
+//                    k of a scene covers a key range; children are leaves or
+//                    internal nodes of the same scene
+//   k_refit          bottom-up AABB union (second arrival at a node continues)
+//   k_traverse       stack traversal per leaf; a pair (i, j) is reported only
+//                    by its smaller body i, so each overlap is found once;
+//                    count pass, scan, write pass
+//   k_sort_segments  each body's partners sorted ascending, giving the pair
+//                    list in (a, b) order, the same set and order as the
+//                    dense sweep
+// The overlap test is the reference's closed-interval test on the same
+// support AABBs, and tree boxes are exact unions, so the pair set equals the
+// dense sweep's bit for bit.
+#pragma once
+
+#include "k_broad.cuh"
+
+namespace dio {
+
+__device__ __forceinline__ uint32_t f2ord(float f) {
+    uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(uint32_t u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u);
+}
+__device__ __forceinline__ uint64_t d2ord(double f) {
+    uint64_t u = (uint64_t)__double_as_longlong(f);
+    return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
+}
+
+// per-scene centroid bounds: 6 ordered uints (min xyz, max xyz); the Morton
+// grid only needs to be monotone in the centre, so FP32 bounds suffice
+template <class R>
+__global__ void k_scene_bounds(const A4<R>* mn, const A4<R>* mx, const uint32_t* scene, uint32_t n, uint32_t* bounds) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        A4<R> a = mn[i], b = mx[i];
+        uint32_t ox = f2ord(float(a.x * R(0.5) + b.x * R(0.5)));
+        uint32_t oy = f2ord(float(a.y * R(0.5) + b.y * R(0.5)));
+        uint32_t oz = f2ord(float(a.z * R(0.5) + b.z * R(0.5)));
+        const uint32_t s = scene[i];
+        // lanes of one scene reduce first; their leader issues the atomics
+        const uint32_t grp = __match_any_sync(__activemask(), s);
+        const uint32_t nx = __reduce_min_sync(grp, ox), ny = __reduce_min_sync(grp, oy),
+                       nz = __reduce_min_sync(grp, oz);
+        const uint32_t xx = __reduce_max_sync(grp, ox), xy = __reduce_max_sync(grp, oy),
+                       xz = __reduce_max_sync(grp, oz);
+        if ((threadIdx.x & 31) == (uint32_t)(__ffs(grp) - 1)) {
+            uint32_t* bs = bounds + 6 * s;
+            atomicMin(&bs[0], nx);
+            atomicMin(&bs[1], ny);
+            atomicMin(&bs[2], nz);
+            atomicMax(&bs[3], xx);
+            atomicMax(&bs[4], xy);
+            atomicMax(&bs[5], xz);
+        }
+    }
+}
+
+__device__ __forceinline__ uint32_t spread10(uint32_t v) {
+    v &= 0x3FFu;
+    v = (v | (v << 16)) & 0x030000FFu;
+    v = (v | (v << 8)) & 0x0300F00Fu;
+    v = (v | (v << 4)) & 0x030C30C3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+// 32-bit key: scene index in the top `scene_bits`, then a Morton code with
+// `axis_bits` per axis (10 for one scene, 7 for up to 2048 scenes); the key
+// only has to keep scenes contiguous and order bodies spatially within one
+template <class R>
+__global__ void k_morton(const A4<R>* mn, const A4<R>* mx, const uint32_t* scene, uint32_t n, const uint32_t* bounds,
+                         uint32_t scene_bits, uint32_t axis_bits, uint32_t* keys, uint32_t* vals) {
+    const float cells = float(1u << axis_bits);
+    const uint32_t top = (1u << axis_bits) - 1u;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        A4<R> a = mn[i], b = mx[i];
+        float c[3] = {float(a.x * R(0.5) + b.x * R(0.5)), float(a.y * R(0.5) + b.y * R(0.5)),
+                      float(a.z * R(0.5) + b.z * R(0.5))};
+        uint32_t s = scene[i];
+        const uint32_t* bs = bounds + 6 * s;
+        uint32_t q[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            float lo = ord2f(bs[k]), hi = ord2f(bs[3 + k]);
+            float ext = hi - lo;
+            float t = ext > 0.f ? (c[k] - lo) / ext : 0.f;
+            t = fminf(fmaxf(t, 0.f), 1.f);
+            q[k] = min((uint32_t)(t * cells), top);
+        }
+        uint32_t code = (spread10(q[0]) << 2) | (spread10(q[1]) << 1) | spread10(q[2]);
+        keys[i] = scene_bits ? ((s << (3 * axis_bits)) | code) : code;
+        vals[i] = i;
+    }
+}
+
+// Karras prefix length of sorted positions a, b within a segment of length
+// n (local indices); duplicates tie-break on the index.
+__device__ __forceinline__ int kdelta(const uint32_t* keys, uint32_t lo, int n, int a, int b) {
+    if (b < 0 || b >= n) return -1;
+    uint32_t ka = keys[lo + a], kb = keys[lo + b];
+    if (ka == kb) return 32 + __clz((uint32_t)(a ^ b));
+    return __clz(ka ^ kb);
+}
+
+constexpr uint32_t kLeafFlag = 0x80000000u;
+
+// L1-bypassing loads (data produced by other CTAs of the same launch)
+template <class R>
+__device__ __forceinline__ A4<R> ldcg4(const A4<R>* p);
+template <>
+__device__ __forceinline__ A4<float> ldcg4(const A4<float>* p) {
+    float4 v = __ldcg(reinterpret_cast<const float4*>(p));
+    return {v.x, v.y, v.z, v.w};
+}
+template <>
+__device__ __forceinline__ A4<double> ldcg4(const A4<double>* p) {
+    const double2* q = reinterpret_cast<const double2*>(p);
+    double2 a = __ldcg(q), b = __ldcg(q + 1);
+    return {a.x, a.y, b.x, b.y};
+}
+
+// internal node k of scene s lives at global slot lo_s + k; child codes are
+// global slots, leaves flagged with kLeafFlag (leaf = sorted position)
+static __global__ void k_karras(const uint32_t* keys, const SceneDesc* scenes, const uint32_t* scene_of_pos,
+                         uint32_t n, uint2* children, uint32_t* parent) {
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        const SceneDesc sc = scenes[scene_of_pos[p]];
+        const uint32_t lo = sc.body_lo;
+        const int ns = (int)(sc.body_hi - sc.body_lo);
+        const int k = (int)(p - lo);
+        if (k >= ns - 1) continue;  // ns - 1 internal nodes
+        int d = (kdelta(keys, lo, ns, k, k + 1) - kdelta(keys, lo, ns, k, k - 1)) >= 0 ? 1 : -1;
+        int dmin = kdelta(keys, lo, ns, k, k - d);
+        int lmax = 2;
+        while (kdelta(keys, lo, ns, k, k + lmax * d) > dmin) lmax <<= 1;
+        int l = 0;
+        for (int t = lmax >> 1; t >= 1; t >>= 1)
+            if (kdelta(keys, lo, ns, k, k + (l + t) * d) > dmin) l += t;
+        int j = k + l * d;
+        int dnode = kdelta(keys, lo, ns, k, j);
+        int s = 0;
+        int t = l;
+        do {
+            t = (t + 1) >> 1;
+            if (kdelta(keys, lo, ns, k, k + (s + t) * d) > dnode) s += t;
+        } while (t > 1);
+        int gamma = k + s * d + min(d, 0);
+        uint32_t left = (min(k, j) == gamma) ? ((lo + gamma) | kLeafFlag) : (lo + gamma);
+        uint32_t right = (max(k, j) == gamma + 1) ? ((lo + gamma + 1) | kLeafFlag) : (lo + gamma + 1);
+        children[lo + k] = make_uint2(left, right);
+        // parents: internal slots in [0, n), leaves in [n, 2n)
+        parent[(left & kLeafFlag) ? n + (left & ~kLeafFlag) : left] = lo + k;
+        parent[(right & kLeafFlag) ? n + (right & ~kLeafFlag) : right] = lo + k;
+    }
+}
+
+// leaf boxes in sorted order, then bottom-up unions
+template <class R>
+__global__ void k_refit(const A4<R>* mn, const A4<R>* mx, const uint32_t* leaf_body, const SceneDesc* scenes,
+                        const uint32_t* scene_of_pos, uint32_t n, const uint2* children, const uint32_t* parent,
+                        A4<R>* leaf_min, A4<R>* leaf_max, A4<R>* node_min, A4<R>* node_max, uint32_t* visits) {
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        uint32_t b = leaf_body[p];
+        leaf_min[p] = mn[b];
+        leaf_max[p] = mx[b];
+        const SceneDesc sc = scenes[scene_of_pos[p]];
+        if (sc.body_hi - sc.body_lo < 2) continue;
+        __threadfence();
+        uint32_t node = parent[n + p];
+        while (true) {
+            if (atomicAdd(&visits[node], 1u) == 0) break;  // first arrival stops
+            __threadfence();
+            uint2 c = children[node];
+            const A4<R>* lmn = (c.x & kLeafFlag) ? leaf_min : node_min;
+            const A4<R>* lmx = (c.x & kLeafFlag) ? leaf_max : node_max;
+            const A4<R>* rmn = (c.y & kLeafFlag) ? leaf_min : node_min;
+            const A4<R>* rmx = (c.y & kLeafFlag) ? leaf_max : node_max;
+            uint32_t li = c.x & ~kLeafFlag, ri = c.y & ~kLeafFlag;
+            // boxes written by other CTAs in this launch: read through L2
+            A4<R> a0 = ldcg4(&lmn[li]), a1 = ldcg4(&lmx[li]), b0 = ldcg4(&rmn[ri]), b1 = ldcg4(&rmx[ri]);
+            node_min[node] = A4<R>{fmin_(a0.x, b0.x), fmin_(a0.y, b0.y), fmin_(a0.z, b0.z), R(0)};
+            node_max[node] = A4<R>{fmax_(a1.x, b1.x), fmax_(a1.y, b1.y), fmax_(a1.z, b1.z), R(0)};
+            __threadfence();
+            if (node == sc.body_lo) break;  // scene root
+            node = parent[node];
+        }
+    }
+}
+
+constexpr int kStack = 64;
+
+// count (write_out false) or write partner lists; per body i the partners j
+// land unsorted in pb[offsets[i] ...]
+template <class R>
+__global__ void __launch_bounds__(128) k_traverse(const uint32_t* leaf_body, const SceneDesc* scenes,
+                                                  const uint32_t* scene_of_pos, uint32_t n, const uint2* children,
+                                                  const A4<R>* leaf_min, const A4<R>* leaf_max,
+                                                  const A4<R>* node_min, const A4<R>* node_max, uint32_t* counts,
+                                                  const uint32_t* offsets, uint32_t* pb, uint32_t cap, bool write_out,
+                                                  uint32_t* err) {
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        const uint32_t i = leaf_body[p];
+        const SceneDesc sc = scenes[scene_of_pos[p]];
+        uint32_t found = 0;
+        uint32_t out = write_out ? offsets[i] : 0;
+        if (sc.body_hi - sc.body_lo >= 2) {
+            const A4<R> qmn = leaf_min[p], qmx = leaf_max[p];
+            uint32_t stack[kStack];
+            int sp = 0;
+            uint32_t node = sc.body_lo;  // root
+            while (true) {
+                uint2 c = children[node];
+                uint32_t ch[2] = {c.x, c.y};
+                uint32_t push = 0;
+                uint32_t next[2];
+#pragma unroll
+                for (int k = 0; k < 2; ++k) {
+                    uint32_t x = ch[k];
+                    uint32_t idx = x & ~kLeafFlag;
+                    if (x & kLeafFlag) {
+                        if (overlap(qmn, qmx, leaf_min[idx], leaf_max[idx])) {
+                            uint32_t j = leaf_body[idx];
+                            if (j > i) {
+                                if (write_out) {
+                                    if (out < cap) pb[out] = j;
+                                    ++out;
+                                } else {
+                                    ++found;
+                                }
+                            }
+                        }
+                    } else if (overlap(qmn, qmx, node_min[idx], node_max[idx])) {
+                        next[push++] = idx;
+                    }
+                }
+                if (push == 0) {
+                    if (sp == 0) break;
+                    node = stack[--sp];
+                } else {
+                    node = next[0];
+                    if (push == 2) {
+                        if (sp < kStack)
+                            stack[sp++] = next[1];
+                        else
+                            atomicOr(err, kErrIndexOverflow);
+                    }
+                }
+            }
+        }
+        if (!write_out) counts[i] = found;
+    }
+}
+
+// sort each body's partner list ascending; short lists in-thread, long
+// lists (> 32) by one CTA in shared memory (bitonic, up to 4096 entries)
+static __global__ void k_bounds_init(uint32_t* b, uint32_t ns) {
+    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x) {
+        b[6 * s + 0] = b[6 * s + 1] = b[6 * s + 2] = 0xFFFFFFFFu;
+        b[6 * s + 3] = b[6 * s + 4] = b[6 * s + 5] = 0u;
+    }
+}
+
+static __global__ void k_sort_segments(const uint32_t* offsets, uint32_t n, uint32_t cap, uint32_t* pb, uint32_t* long_list,
+                                uint32_t* long_count) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t a = offsets[i], b = offsets[i + 1];
+        uint32_t len = b - a;
+        if (len <= 1 || b > cap) continue;  // overflow is reported by the pair count
+        if (len > 32) {
+            long_list[atomicAdd(long_count, 1u)] = i;
+            continue;
+        }
+        uint32_t v[32];
+        for (uint32_t k = 0; k < len; ++k) v[k] = pb[a + k];
+        for (uint32_t k = 1; k < len; ++k) {
+            uint32_t x = v[k];
+            int m = (int)k - 1;
+            while (m >= 0 && v[m] > x) {
+                v[m + 1] = v[m];
+                --m;
+            }
+            v[m + 1] = x;
+        }
+        for (uint32_t k = 0; k < len; ++k) pb[a + k] = v[k];
+    }
+}
+
+constexpr int kLongSort = 4096;
+
+static __global__ void __launch_bounds__(512) k_sort_long(const uint32_t* offsets, uint32_t* pb, const uint32_t* long_list,
+                                                   const uint32_t* long_count, uint32_t* err) {
+    __shared__ uint32_t s[kLongSort];
+    uint32_t cnt = *long_count;
+    for (uint32_t q = blockIdx.x; q < cnt; q += gridDim.x) {
+        uint32_t i = long_list[q];
+        uint32_t a = offsets[i], len = offsets[i + 1] - a;
+        if (len > (uint32_t)kLongSort) {
+            if (threadIdx.x == 0) atomicOr(err, kErrIndexOverflow);
+            continue;
+        }
+        uint32_t p2 = 1;
+        while (p2 < len) p2 <<= 1;
+        for (uint32_t k = threadIdx.x; k < p2; k += blockDim.x) s[k] = k < len ? pb[a + k] : 0xFFFFFFFFu;
+        __syncthreads();
+        for (uint32_t size = 2; size <= p2; size <<= 1) {
+            for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+                for (uint32_t t = threadIdx.x; t < p2; t += blockDim.x) {
+                    uint32_t u = t ^ stride;
+                    if (u > t) {
+                        bool up = (t & size) == 0;
+                        uint32_t x = s[t], y = s[u];
+                        if ((x > y) == up) {
+                            s[t] = y;
+                            s[u] = x;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        for (uint32_t k = threadIdx.x; k < len; k += blockDim.x) pb[a + k] = s[k];
+        __syncthreads();
+    }
+}
+
+static __global__ void k_pairs_from_segments(const uint32_t* offsets, uint32_t n, const uint32_t* pb, DioPair* pairs,
+                                      uint32_t cap) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        for (uint32_t k = offsets[i]; k < offsets[i + 1] && k < cap; ++k) pairs[k] = DioPair{i, pb[k]};
+}
+
+}  // namespace dio

@@ -130,6 +130,33 @@ __device__ __forceinline__ uint32_t container_rows(const DevWorld<P, R>& w, uint
     R half = R(sc.half_extent);
     V3<R> vel = cast3<R>(xyz(w.vel[i]));
     const bool boxy = b.shape.tag == DIO_SHAPE_CUBE || b.shape.tag == DIO_SHAPE_BOX;
+    // Quick reject: every support point lies within an L1 bounding radius of
+    // the body centre, so a body whose centre plus that radius plus this
+    // step's travel is (with rounding slack) inside all six walls has no
+    // row with depth > 0 -- the same empty set the full test produces.
+    R rbound = R(-1);
+    if (boxy) {
+        rbound = dabs(b.shape.c[0].x) + dabs(b.shape.c[0].y) + dabs(b.shape.c[0].z);
+    } else if (b.shape.tag == DIO_SHAPE_SPHERE) {
+        rbound = dabs(b.shape.c[0].x);
+    } else if (b.shape.tag == DIO_SHAPE_TETRAHEDRON) {
+        rbound = R(0);
+        for (int k = 0; k < 4; ++k)
+            rbound = fmax_(rbound, dabs(b.shape.c[k].x) + dabs(b.shape.c[k].y) + dabs(b.shape.c[k].z));
+    }
+    if (rbound >= R(0)) {
+        const R travel = length(vel) * o.dt;
+        bool inside = true;
+        for (int k = 0; k < 6 && inside; ++k) {
+            V3<R> axis = k < 2 ? V3<R>{R(1), R(0), R(0)} : (k < 4 ? V3<R>{R(0), R(1), R(0)} : V3<R>{R(0), R(0), R(1)});
+            V3<R> outward = rotate(crot, scale(axis, (k & 1) ? R(-1) : R(1)));
+            R plane = dot(center, outward) + half;
+            R d = dot(b.pos, outward);
+            R slack = R(1e-4) * (R(1) + dabs(plane) + dabs(d));
+            if (!(d + rbound + travel + slack < plane)) inside = false;
+        }
+        if (inside) return 0;
+    }
     uint32_t count = 0;
 #pragma unroll 1
     for (int k = 0; k < 6; ++k) {
@@ -301,6 +328,112 @@ __global__ void k_csr_fill(DevWorld<P, R> w, const uint32_t* inc_body_sorted, co
         if (j < w.max_incid) {
             w.row_idx[j] = r;
             w.row_oth[j] = oth;
+        }
+    }
+}
+
+// ---- device-driven variants for the resident world (no host-known counts)
+//
+// The world's rows are in canonical order: pair rows follow the pair list,
+// which is sorted by (a, b), and container rows follow the body index, so
+// each section of the row list is sorted by key with equal keys adjacent.
+// The warm start therefore needs no sort: a row is the first of its key when
+// its predecessor in the section has another key, and the last previous row
+// with that key is found by binary search in the previous step's section.
+
+__device__ __forceinline__ bool key_less(uint2 a, uint2 b) { return a.x < b.x || (a.x == b.x && a.y < b.y); }
+__device__ __forceinline__ bool key_eq(uint2 a, uint2 b) { return a.x == b.x && a.y == b.y; }
+
+// roll the per-step counters: the finished step's row counts become the
+// warm-start source, the per-step counts restart at zero
+static __global__ void k_roll_counters(Counters* c) {
+    c->prev_rows = c->rows;
+    c->prev_pair_rows = c->pair_rows;
+    c->pairs = 0;
+    c->rows = 0;
+    c->pair_rows = 0;
+    c->container_rows = 0;
+    c->gjk_work = 0;
+    c->epa_work = 0;
+    c->long_count = 0;
+}
+
+template <class P, class R>
+__global__ void k_warm_sections(DevWorld<P, R> w, const uint2* prev_ab, const RowDual<P, R>* prev_dual,
+                                PrepParams<R> o) {
+    const uint32_t m = w.ctr->rows, pair_rows = w.ctr->pair_rows;
+    const uint32_t prev_m = w.ctr->prev_rows, prev_pair = w.ctr->prev_pair_rows;
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) {
+        const uint2 key = w.ab[r];
+        const bool cont = key.y == kContainer;
+        const uint32_t sec_lo = cont ? pair_rows : 0;
+        RowDual<P, R> du = w.rd[r];
+        bool first = r == sec_lo || !key_eq(w.ab[r - 1], key);
+        if (first) {
+            uint32_t lo = cont ? prev_pair : 0, hi = cont ? prev_m : prev_pair;
+            const uint32_t base = lo;
+            while (lo < hi) {  // upper bound of key
+                uint32_t mid = (lo + hi) >> 1;
+                if (!key_less(key, prev_ab[mid]))
+                    lo = mid + 1;
+                else
+                    hi = mid;
+            }
+            if (lo > base && key_eq(prev_ab[lo - 1], key)) {
+                const RowDual<P, R> pd = prev_dual[lo - 1];
+                du.lambda = pd.lambda;
+                du.penalty = pd.penalty;
+            }
+        }
+        P ag = P(o.alpha_gamma);
+        du.lambda.x = du.lambda.x * ag;
+        du.lambda.y = du.lambda.y * ag;
+        du.lambda.z = du.lambda.z * ag;
+        R kx = du.penalty.x * o.gamma, ky = du.penalty.y * o.gamma, kz = du.penalty.z * o.gamma;
+        du.penalty.x = fmin_(fmax_(kx, o.penalty_min), o.penalty_max);
+        du.penalty.y = fmin_(fmax_(ky, o.penalty_min), o.penalty_max);
+        du.penalty.z = fmin_(fmax_(kz, o.penalty_min), o.penalty_max);
+        w.rd[r] = du;
+    }
+}
+
+// CSR of the dynamic bodies only (the primal never visits a static body):
+// counts, then an atomic scatter, then each segment sorted by row index,
+// which restores the reference's fill order (finalize_contacts, gpu.rs:
+// 286-310) without a sort over all incidences.
+template <class P, class R>
+__global__ void k_csr_count_dyn(DevWorld<P, R> w, uint32_t* counts) {
+    const uint32_t m = w.ctr->rows;
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) {
+        uint2 ab = w.ab[r];
+        if (w.inv[ab.x].w != R(0)) atomicAdd(&counts[ab.x], 1u);
+        if (ab.y != kContainer && w.inv[ab.y].w != R(0)) atomicAdd(&counts[ab.y], 1u);
+    }
+}
+
+template <class P, class R>
+__global__ void k_csr_scatter_dyn(DevWorld<P, R> w, uint32_t* cursor) {
+    const uint32_t m = w.ctr->rows;
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) {
+        uint2 ab = w.ab[r];
+        if (w.inv[ab.x].w != R(0)) {
+            uint32_t j = w.row_off[ab.x] + atomicAdd(&cursor[ab.x], 1u);
+            if (j < w.max_incid) w.row_idx[j] = r;
+        }
+        if (ab.y != kContainer && w.inv[ab.y].w != R(0)) {
+            uint32_t j = w.row_off[ab.y] + atomicAdd(&cursor[ab.y], 1u);
+            if (j < w.max_incid) w.row_idx[j] = r;
+        }
+    }
+}
+
+template <class P, class R>
+__global__ void k_csr_other_dyn(DevWorld<P, R> w) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < w.n; i += gridDim.x * blockDim.x) {
+        uint32_t j0 = w.row_off[i], j1 = min(w.row_off[i + 1], w.max_incid);
+        for (uint32_t j = j0; j < j1; ++j) {
+            uint2 v = w.ab[w.row_idx[j]];
+            w.row_oth[j] = v.y == kContainer ? kContainer : (v.x == i ? v.y : (v.x | kIsB));
         }
     }
 }

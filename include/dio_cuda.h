@@ -215,6 +215,8 @@ typedef struct DioConfig {
     uint32_t block_size;        /* threads per CTA for per-body kernels   */
     uint32_t batched_solver;    /* 1: one CTA-per-scene persistent solve  */
     uint32_t profile;           /* time primal / dual launches with events */
+    uint32_t broad_phase;       /* 0: LBVH (default), 1: dense sweep        */
+    uint32_t reserved[3];
 } DioConfig;
 
 /* World description for the fused device-resident step (extension of the
@@ -245,6 +247,10 @@ typedef struct DioStepStats {
     uint32_t dual_launches;   /* dual launches timed                       */
     double primal_ms;         /* summed primal kernel time (CUDA events)   */
     double dual_ms;           /* summed dual kernel time                   */
+    double broad_ms;          /* summed broad-phase time (AABB .. pairs)   */
+    double narrow_ms;         /* summed narrow-phase time                  */
+    double rows_ms;           /* summed row build + warm start + CSR time  */
+    double solve_ms;          /* summed init .. recover time               */
 } DioStepStats;
 
 typedef struct DioCtx DioCtx;

@@ -123,15 +123,16 @@ def _world(sc, **cfg):
     return w
 
 
-@pytest.mark.parametrize("steps", [1, 60])
-def test_world_steps_match_oracle(steps):
+@pytest.mark.parametrize("steps,use_graph", [(1, 1), (60, 1), (60, 0)])
+def test_world_steps_match_oracle(steps, use_graph):
     for sc in small_scenes():
         ow = O.World(sc)
         ow.step(sc.options, steps)
         rb, rs = ow.download()
         rc = ow.contacts()
-        with _world(sc) as w:
-            w.step(sc.options, steps)
+        with _world(sc, use_graph=use_graph) as w:
+            for _ in range(steps):  # one dio_step per step: graph replay per call
+                w.step(sc.options, 1)
             gb, gs = w.download()
             gc = w.contacts()
             st = w.stats()
@@ -206,3 +207,43 @@ def test_zero_iterations_follow_reference_parities():
         got = ac.run(*args)
     for k in ref:
         assert np.array_equal(_bits(got[k]), _bits(ref[k])), k
+
+
+def _gpu_pairs(bodies, hull=None, broad_phase=0):
+    n = len(bodies)
+    hv = hull if hull is not None else np.zeros((1, 4), np.float32)
+    with compute.NarrowPhaseCompute(n, max(64, 64 * n), max_hull_vertices=len(hv)) as npc:
+        npc.configure(broad_phase=broad_phase)
+        npc.set_hull_vertices(hv)
+        npc.submit_broad(bodies)
+        c = npc.read_pair_count()
+        return npc.read_pairs(c)
+
+
+@pytest.mark.parametrize("broad_phase", [0, 1])
+def test_lbvh_and_dense_pair_sets_at_scale(broad_phase):
+    """The LBVH (default) and the dense sweep give the oracle's pair set in
+    (a, b) order on larger scenes, including coincident and nested bodies."""
+    cases = [scenes.cube_field(nx=16, nz=16, ny=4), scenes.mixed_pile(n=3000, extent=12.0)]
+    # degenerate: many bodies at the same centre (equal Morton codes) plus a big one
+    b, s = ph.pack_bodies([ph.sphere((0, 0, 0), 0.5, 1.0) for _ in range(40)] + [ph.cube((0, 0, 0), 5.0, 1.0)]
+                          + [ph.sphere((20, 0, 0), 0.5, 1.0)])
+    cases.append(scenes.Scene("coincident", b, s))
+    for sc in cases:
+        ref, _ = O.broad(sc.bodies, hull=sc.hull_vertices)
+        got = _gpu_pairs(sc.bodies, sc.hull_vertices, broad_phase)
+        assert np.array_equal(got, ref), sc.name
+
+
+@pytest.mark.parametrize("use_graph", [0, 1])
+def test_profiled_world_times_every_primal_launch(use_graph):
+    sc = scenes.box_demo()
+    with _world(sc, use_graph=use_graph, profile=1) as w:
+        w.step(sc.options, 3)
+        w.reset_timers()
+        w.step(sc.options, 4)
+        st = w.stats()
+    iters = sc.options.iterations
+    assert st["primal_launches"] == 4 * iters
+    assert st["primal_ms"] > 0 and st["solve_ms"] >= st["primal_ms"]
+    assert st["kernel_launches"] > 4 * 2 * iters
