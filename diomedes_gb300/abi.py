@@ -83,7 +83,7 @@ class Capacity(ctypes.Structure):
 
 class Config(ctypes.Structure):
     _fields_ = [("solver_mode", _u32), ("precision", _u32), ("contacts_per_pair", _u32),
-                ("use_graph", _u32), ("primal_group", _u32), ("block_size", _u32),
+                ("use_graph", _u32), ("primal_variant", _u32), ("block_size", _u32),
                 ("batched_solver", _u32), ("profile", _u32), ("broad_phase", _u32), ("reserved", _u32 * 3)]
 
 

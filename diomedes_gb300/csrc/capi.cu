@@ -33,8 +33,8 @@ DioConfig default_config() {
     c.precision = DIO_PREC_F32;
     c.contacts_per_pair = DIO_CONTACTS_PER_PAIR;
     c.use_graph = 1;
-    c.primal_group = 1;
-    c.block_size = 128;
+    c.primal_variant = 2;
+    c.block_size = 0;
     c.batched_solver = 0;
     return c;
 }

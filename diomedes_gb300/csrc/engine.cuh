@@ -88,9 +88,22 @@ struct SceneDesc {
     float rotation[4];
 };
 
+// One joint seen from one of its bodies (built once per upload from the
+// joint list and the per-body joint CSR, joint order kept per body).
+struct JView {
+    float4 self_anchor;   // xyz; w = rest length / max length
+    float4 other_anchor;  // xyz; w = stiffness
+    uint32_t other;       // the other body
+    uint32_t kind;        // constraint kind | kIsB when this body is `b`
+    uint32_t pad[2];
+};
+
 template <class P, class R>
 struct DevWorld {
     uint32_t n;  // bodies
+    const uint32_t* dyn_list;  // dynamic bodies in index order
+    uint32_t n_dyn;
+    const JView* jview;        // per-body joint views (joint CSR order)
     // poses
     A4<P>* pos[2];
     A4<P>* rot[2];
@@ -102,6 +115,7 @@ struct DevWorld {
     A4<P>* ang;
     A4<P>* prev_vel;
     A4<R>* inv;  // inv_moment xyz, inv_mass w
+    A4<R>* mdt2;  // per step: m/dt^2 in x, I/dt^2 in y..w (dynamic bodies)
     R* friction;
     DioShape* shape;
     uint32_t* scene;

@@ -262,6 +262,37 @@ __global__ void k_pack_world(DevWorld<P, R> w, DioGpuBody* bodies, DioBodyState*
     }
 }
 
+template <class P, class R>
+__global__ void k_dyn_flags(DevWorld<P, R> w, uint32_t n, uint32_t* flags) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        flags[i] = w.inv[i].w != R(0) ? 1u : 0u;
+}
+
+static __global__ void k_dyn_fill(const uint32_t* flags, const uint32_t* pos, uint32_t n, uint32_t* list) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        if (flags[i]) list[pos[i]] = i;
+}
+
+// one JView per (body, joint) incidence in the body's joint-CSR order
+static __global__ void k_build_jview(const DioConstraint* joints, const uint32_t* joff, const uint32_t* jidx,
+                                     uint32_t n, JView* out) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        for (uint32_t k = joff[i]; k < joff[i + 1]; ++k) {
+            const DioConstraint j = joints[jidx[k]];
+            const bool is_a = j.a == i;
+            JView v;
+            const float* sa = is_a ? j.anchor_a : j.anchor_b;
+            const float* oa = is_a ? j.anchor_b : j.anchor_a;
+            v.self_anchor = make_float4(sa[0], sa[1], sa[2], j.anchor_a[3]);
+            v.other_anchor = make_float4(oa[0], oa[1], oa[2], j.anchor_b[3]);
+            v.other = is_a ? j.b : j.a;
+            v.kind = j.kind | (is_a ? 0u : kIsB);
+            v.pad[0] = v.pad[1] = 0u;
+            out[k] = v;
+        }
+    }
+}
+
 // joint incidences (body, joint id) for the per-body joint CSR
 static __global__ void k_joint_inc(const DioConstraint* j, uint32_t nj, uint32_t n, uint32_t* body, uint32_t* id,
                             uint32_t* err) {
@@ -327,6 +358,7 @@ class Engine final : public EngineBase {
         DIO_TRY(alloc(&w_.ang, N));
         DIO_TRY(alloc(&w_.prev_vel, N));
         DIO_TRY(alloc(&w_.inv, N));
+        DIO_TRY(alloc(&w_.mdt2, N));
         DIO_TRY(alloc(&w_.friction, N));
         DIO_TRY(alloc(&w_.shape, N));
         DIO_TRY(alloc(&w_.scene, N));
@@ -377,6 +409,8 @@ class Engine final : public EngineBase {
         DIO_TRY(alloc(&joints_, J));
         DIO_TRY(alloc(&joint_off_, (size_t)N + 1));
         DIO_TRY(alloc(&joint_idx_, 2ull * J));
+        DIO_TRY(alloc(&jview_, 2ull * J));
+        DIO_TRY(alloc(&dyn_list_, N));
         const size_t CNT = std::max<size_t>(std::max<size_t>(N, (size_t)PP * per_cap_), 2ull * M) + 2;
         DIO_TRY(alloc(&counts_, CNT));
         DIO_TRY(alloc(&offsets_, CNT));
@@ -881,6 +915,21 @@ class Engine final : public EngineBase {
                                                            align256((size_t)n * sizeof(DioGpuBody)));
         DIO_CK(cudaMemcpyAsync(ds, state, (size_t)n * sizeof(DioBodyState), cudaMemcpyHostToDevice, stream_));
         k_unpack_state<P, R><<<grid_for(n, 256), 256, 0, stream_>>>(w_, ds, n);
+        return build_dyn_list(n);
+    }
+    // compacted list of dynamic bodies (inverse mass != 0), index order
+    int build_dyn_list(uint32_t n) {
+        k_dyn_flags<P, R><<<grid_for(n, 256), 256, 0, stream_>>>(w_, n, counts2_);
+        DIO_CK(cudaMemsetAsync(counts2_ + n, 0, 4, stream_));
+        size_t tb = cub_bytes_;
+        DIO_CK(cub::DeviceScan::ExclusiveSum(cub_tmp_, tb, counts2_, offsets2_, (int)n + 1, stream_));
+        k_dyn_fill<<<grid_for(n, 256), 256, 0, stream_>>>(counts2_, offsets2_, n, dyn_list_);
+        uint32_t nd = 0;
+        DIO_CK(cudaMemcpyAsync(&nd, offsets2_ + n, 4, cudaMemcpyDeviceToHost, stream_));
+        DIO_CK(cudaStreamSynchronize(stream_));
+        if (w_.n_dyn != nd) drop_graphs();  // launch shapes depend on it
+        w_.n_dyn = nd;
+        w_.dyn_list = dyn_list_;
         return DIO_OK;
     }
     int single_scene(uint32_t n, const DioContainer* c) {
@@ -922,6 +971,8 @@ class Engine final : public EngineBase {
         tb = cub_bytes_;
         DIO_CK(cub::DeviceScan::ExclusiveSum(cub_tmp_, tb, counts2_, joint_off_, (int)n + 1, stream_));
         DIO_CK(cudaMemcpyAsync(joint_idx_, inc_row_s_, (size_t)total * 4, cudaMemcpyDeviceToDevice, stream_));
+        k_build_jview<<<grid_for(n, 128), 128, 0, stream_>>>(joints_, joint_off_, joint_idx_, n, jview_);
+        w_.jview = jview_;
         return DIO_OK;
     }
     int sort_keys(const uint2* ab, uint32_t m, unsigned long long* keys_out, uint32_t* ids_out) {
@@ -1075,7 +1126,6 @@ class Engine final : public EngineBase {
     int solve(const SolveParams<R>& o, uint32_t n, uint32_t m, const uint32_t* m_dev = nullptr) {
         if (n == 0) return DIO_OK;
         int gb = grid_for(n, 256);
-        int gp = grid_for(n, 128);
         int gm = m_dev ? std::min(grid_for(cap_.max_contacts, 256), sms_ * 8) : grid_for(std::max(m, 1u), 256);
         if (m_dev) m = cap_.max_contacts;
         k_init<P, R><<<gb, 256, 0, stream_>>>(w_, 0, n, o);
@@ -1083,7 +1133,7 @@ class Engine final : public EngineBase {
         for (uint32_t k = 0; k < o.iterations; ++k) {
             int par = (int)(k % 2);
             cudaEvent_t e0 = span_begin();
-            k_primal<P, R><<<gp, 128, 0, stream_>>>(w_, 0, n, par, 1 - par, o);
+            launch_primal<P, R>((int)cfg_.primal_variant, 0, sms_, w_, par, 1 - par, o, stream_);
             span_end(e0, 0);
             ++launches_;
             if (m) {
@@ -1361,6 +1411,8 @@ class Engine final : public EngineBase {
     uint32_t *inc_body_ = nullptr, *inc_row_ = nullptr, *inc_body_s_ = nullptr, *inc_row_s_ = nullptr;
     DioConstraint* joints_ = nullptr;
     uint32_t *joint_off_ = nullptr, *joint_idx_ = nullptr;
+    JView* jview_ = nullptr;
+    uint32_t* dyn_list_ = nullptr;
     uint32_t *counts_ = nullptr, *offsets_ = nullptr, *counts2_ = nullptr, *offsets2_ = nullptr;
     SceneDesc* scenes_ = nullptr;
     std::vector<SceneDesc> scenes_host_;

@@ -14,6 +14,8 @@
 //     starts every step from buffer 0.
 #pragma once
 
+#include <type_traits>
+
 #include "engine.cuh"
 
 namespace dio {
@@ -104,6 +106,15 @@ __device__ __forceinline__ void init_body(const DevWorld<P, R>& w, uint32_t i, c
     w.inert_pos[i] = pack(ip);
     Q4<P> irot = quat_step(rot, scale(ang, dt));
     w.inert_rot[i] = packq(irot);
+    if (w.mdt2 && inv_mass != R(0)) {
+        // the primal's diagonal, constant over the step (avbd/src/lib.rs:293-296)
+        const A4<R> inv = w.inv[i];
+        const R mass = R(1) / inv.w;
+        const V3<R> moment{R(1) / inv.x, R(1) / inv.y, R(1) / inv.z};
+        const R dt2 = o.dt * o.dt;
+        const V3<R> idt2 = divs(moment, dt2);
+        w.mdt2[i] = A4<R>{mass / dt2, idt2.x, idt2.y, idt2.z};
+    }
     if (inv_mass > R(0)) {
         V3<P> accel = divs(sub(vel, xyz(w.prev_vel[i])), dt);
         P gm = length(g);
@@ -204,6 +215,48 @@ __device__ __forceinline__ void primal_joint(const DevWorld<P, R>& w, const DioC
     }
 }
 
+// The same joint row from a JView: p_a - p_b is formed exactly as the
+// reference forms it (joint a's anchor point minus joint b's).
+template <class P, class R>
+__device__ __forceinline__ void primal_jview(const DevWorld<P, R>& w, const JView& jv, int rd, V3<P> sp, Q4<P> sq,
+                                             Q4<R> sqr, Block6<R>& B) {
+    const bool is_a = !(jv.kind & kIsB);
+    const uint32_t kind = jv.kind & ~kIsB;
+    const V3<R> anc_s{R(jv.self_anchor.x), R(jv.self_anchor.y), R(jv.self_anchor.z)};
+    const V3<R> anc_o{R(jv.other_anchor.x), R(jv.other_anchor.y), R(jv.other_anchor.z)};
+    V3<R> r_self;
+    V3<P> p_self;
+    if constexpr (std::is_same<P, R>::value) {
+        r_self = rotate(sqr, anc_s);  // identical expression: evaluate once
+        p_self = add(sp, r_self);
+    } else {
+        p_self = add(sp, rotate(sq, cast3<P>(anc_s)));
+        r_self = rotate(sqr, anc_s);
+    }
+    const V3<P> p_other = add(xyz(w.pos[rd][jv.other]), rotate(quat(w.rot[rd][jv.other]), cast3<P>(anc_o)));
+    const V3<R> delta = cast3<R>(is_a ? sub(p_self, p_other) : sub(p_other, p_self));
+    const R sign = is_a ? R(1) : R(-1);
+    const R stiff = R(jv.other_anchor.w);
+    if (kind == DIO_CONSTRAINT_BALL_SOCKET) {
+        V3<R> jx = scale(V3<R>{R(1), R(0), R(0)}, sign);
+        V3<R> jy = scale(V3<R>{R(0), R(1), R(0)}, sign);
+        V3<R> jz = scale(V3<R>{R(0), R(0), R(1)}, sign);
+        stamp(B, jx, cross(r_self, jx), stiff, delta.x * stiff);
+        stamp(B, jy, cross(r_self, jy), stiff, delta.y * stiff);
+        stamp(B, jz, cross(r_self, jz), stiff, delta.z * stiff);
+    } else {
+        R len = length(delta);
+        R target = R(jv.self_anchor.w);
+        bool active = len > R(1.0e-6) && (kind != DIO_CONSTRAINT_ROPE || len > target);
+        if (active) {
+            V3<R> nn = divs(delta, len);
+            V3<R> jl = scale(nn, sign);
+            V3<R> ja = cross(r_self, jl);
+            stamp(B, jl, ja, stiff, stiff * (len - target));
+        }
+    }
+}
+
 // avbd_primal for one body: reads buffer rd, writes buffer wr.
 template <class P, class R>
 __device__ __forceinline__ void primal_body(const DevWorld<P, R>& w, uint32_t i, int rd, int wr,
@@ -213,12 +266,19 @@ __device__ __forceinline__ void primal_body(const DevWorld<P, R>& w, uint32_t i,
     const V3<P> sp = xyz(w.pos[rd][i]);
     const Q4<P> sq = quat(w.rot[rd][i]);
     const Q4<R> sqr = castq<R>(sq);
-    const R dt = o.dt;
-    const R mass = R(1) / inv.w;
-    const V3<R> moment{R(1) / inv.x, R(1) / inv.y, R(1) / inv.z};
-    const R dt2 = dt * dt;
-    const R mdt2 = mass / dt2;
-    const V3<R> idt2 = divs(moment, dt2);
+    R mdt2;
+    V3<R> idt2;
+    if (w.mdt2) {
+        const A4<R> d = w.mdt2[i];  // stored by init: the same divisions, once per step
+        mdt2 = d.x;
+        idt2 = V3<R>{d.y, d.z, d.w};
+    } else {
+        const R mass = R(1) / inv.w;
+        const V3<R> moment{R(1) / inv.x, R(1) / inv.y, R(1) / inv.z};
+        const R dt2 = o.dt * o.dt;
+        mdt2 = mass / dt2;
+        idt2 = divs(moment, dt2);
+    }
     Block6<R> B;
 #pragma unroll
     for (int k = 0; k < 21; ++k) B.h[k] = R(0);
@@ -244,8 +304,8 @@ __device__ __forceinline__ void primal_body(const DevWorld<P, R>& w, uint32_t i,
     if (w.n_joints) {
         const uint32_t k0 = w.joint_off[i], k1 = w.joint_off[i + 1];
         for (uint32_t k = k0; k < k1; ++k) {
-            const DioConstraint jt = w.joints[w.joint_idx[k]];
-            primal_joint(w, jt, i, rd, sp, sq, sqr, B);
+            const JView jv = w.jview[k];
+            primal_jview(w, jv, rd, sp, sq, sqr, B);
         }
     }
     R dx[6];
@@ -254,11 +314,47 @@ __device__ __forceinline__ void primal_body(const DevWorld<P, R>& w, uint32_t i,
     w.rot[wr][i] = packq(quat_step(sq, cast3<P>(V3<R>{dx[3], dx[4], dx[5]})));
 }
 
+// One thread per dynamic body (static bodies are never solved,
+// avbd/src/lib.rs:280-282, so they are left out of the launch).
+// BLOCK threads per CTA, at least MINB CTAs per SM (a register bound); the
+// variants are chosen per world by the autotuner.
+template <class P, class R, int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) k_primal(DevWorld<P, R> w, int rd, int wr, SolveParams<R> o) {
+    for (uint32_t t = blockIdx.x * BLOCK + threadIdx.x; t < w.n_dyn; t += gridDim.x * BLOCK)
+        primal_body(w, w.dyn_list[t], rd, wr, o);
+}
+
+// launch-shape variants of k_primal: {threads per CTA, min CTAs per SM}
+constexpr int kPrimalVariants = 6;
+constexpr int kPrimalShape[kPrimalVariants][2] = {{128, 4}, {128, 5}, {128, 6}, {256, 2}, {256, 3}, {64, 10}};
+
 template <class P, class R>
-__global__ void __launch_bounds__(128) k_primal(DevWorld<P, R> w, uint32_t lo, uint32_t hi, int rd, int wr,
-                                                SolveParams<R> o) {
-    for (uint32_t i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += gridDim.x * blockDim.x)
-        primal_body(w, i, rd, wr, o);
+inline void launch_primal(int variant, int blocks_per_sm_hint, int sms, const DevWorld<P, R>& w, int rd, int wr,
+                          const SolveParams<R>& o, cudaStream_t s) {
+    (void)blocks_per_sm_hint;
+    const uint32_t nd = w.n_dyn > 0 ? w.n_dyn : 1;
+    auto grid = [&](int block) { return grid_for(nd, block); };
+    switch (variant) {
+        case 0:
+            k_primal<P, R, 128, 4><<<grid(128), 128, 0, s>>>(w, rd, wr, o);
+            break;
+        case 2:
+            k_primal<P, R, 128, 6><<<grid(128), 128, 0, s>>>(w, rd, wr, o);
+            break;
+        case 3:
+            k_primal<P, R, 256, 2><<<grid(256), 256, 0, s>>>(w, rd, wr, o);
+            break;
+        case 4:
+            k_primal<P, R, 256, 3><<<grid(256), 256, 0, s>>>(w, rd, wr, o);
+            break;
+        case 5:
+            k_primal<P, R, 64, 10><<<grid(64), 64, 0, s>>>(w, rd, wr, o);
+            break;
+        default:
+            k_primal<P, R, 128, 5><<<grid(128), 128, 0, s>>>(w, rd, wr, o);
+            break;
+    }
+    (void)sms;
 }
 
 // Coloured Gauss-Seidel sweep: bodies color_order[c0 .. c1) in place.

@@ -210,9 +210,9 @@ typedef struct DioConfig {
     uint32_t solver_mode;       /* DioSolverMode                          */
     uint32_t precision;         /* DioPrecision (fixed at world upload)   */
     uint32_t contacts_per_pair; /* 4 (reference) or 8 (extended manifold) */
-    uint32_t use_graph;         /* capture the solve loop in a CUDA graph */
-    uint32_t primal_group;      /* lanes per body in the primal: 1,2,4,8  */
-    uint32_t block_size;        /* threads per CTA for per-body kernels   */
+    uint32_t use_graph;         /* replay each step as a CUDA graph       */
+    uint32_t primal_variant;    /* primal launch shape 0..5 (autotuned)   */
+    uint32_t block_size;        /* reserved (0)                           */
     uint32_t batched_solver;    /* 1: one CTA-per-scene persistent solve  */
     uint32_t profile;           /* time primal / dual launches with events */
     uint32_t broad_phase;       /* 0: LBVH (default), 1: dense sweep        */
