@@ -13,6 +13,7 @@
 #include "engine_base.h"
 #include "k_avbd.cuh"
 #include "k_broad.cuh"
+#include "k_color.cuh"
 #include "k_lbvh.cuh"
 #include "k_narrow_kernels.cuh"
 #include "k_rows.cuh"
@@ -411,6 +412,7 @@ class Engine final : public EngineBase {
         DIO_TRY(alloc(&joint_idx_, 2ull * J));
         DIO_TRY(alloc(&jview_, 2ull * J));
         DIO_TRY(alloc(&dyn_list_, N));
+        DIO_TRY(alloc(&color_hist_, kMaxColors + 2));
         const size_t CNT = std::max<size_t>(std::max<size_t>(N, (size_t)PP * per_cap_), 2ull * M) + 2;
         DIO_TRY(alloc(&counts_, CNT));
         DIO_TRY(alloc(&offsets_, CNT));
@@ -737,7 +739,9 @@ class Engine final : public EngineBase {
         if (!options) return inval("null options");
         if (!world_ready_) return state_err("no world uploaded");
         for (uint32_t k = 0; k < steps; ++k) {
-            if (cfg_.use_graph)
+            if (cfg_.solver_mode == DIO_SOLVER_COLORED)
+                DIO_TRY(step_once_colored(*options));
+            else if (cfg_.use_graph)
                 DIO_TRY(step_graph(*options));
             else
                 DIO_TRY(step_once_dev(*options));
@@ -1243,6 +1247,91 @@ class Engine final : public EngineBase {
         return DIO_OK;
     }
 
+    // Coloured Gauss-Seidel step: same detection and rows, then a colouring
+    // and per-colour primal sweeps in place (host-driven colour loop).
+    int step_once_colored(const DioAvbdOptions& opt) {
+        uint32_t n = w_.n;
+        PrepParams<R> pp = opts_prep(opt);
+        set_rows(cur_);
+        k_roll_counters<<<1, 1, 0, stream_>>>(ctr_);
+        cudaEvent_t e = span_begin();
+        if (n) DIO_TRY(run_broad(0, n));
+        span_end(e, 2);
+        e = span_begin();
+        DIO_TRY(run_narrow(cap_.max_pairs, &ctr_->pairs));
+        span_end(e, 3);
+        e = span_begin();
+        DIO_TRY(build_rows(pp, cap_.max_pairs, cfg_.contacts_per_pair, &ctr_->pairs, n));
+        DIO_TRY(finish_rows_world(pp, n));
+        span_end(e, 4);
+        DIO_TRY(color_world(n));
+        SolveParams<R> so = solve_params(opt.dt, opt.gravity, opt.alpha, opt.beta_lin, opt.penalty_max, opt.iterations);
+        e = span_begin();
+        if (n) {
+            const int gb = grid_for(n, 256);
+            const int gf = std::min(grid_for(cap_.max_contacts, 256), sms_ * 8);
+            k_init<P, R><<<gb, 256, 0, stream_>>>(w_, 0, n, so);
+            for (uint32_t it = 0; it < so.iterations; ++it) {
+                for (uint32_t c = 0; c < ncolors_; ++c) {
+                    uint32_t c0 = color_off_h_[c], c1 = color_off_h_[c + 1];
+                    if (c1 <= c0) continue;
+                    cudaEvent_t e0 = span_begin();
+                    k_primal_color<P, R><<<grid_for(c1 - c0, 128), 128, 0, stream_>>>(w_, c0, c1, so);
+                    span_end(e0, 0);
+                    ++launches_;
+                }
+                cudaEvent_t e1 = span_begin();
+                k_dual<P, R><<<gf, 256, 0, stream_>>>(w_, 0, cap_.max_contacts, &ctr_->rows, 0, so);
+                span_end(e1, 1);
+                ++launches_;
+            }
+            k_recover<P, R><<<gb, 256, 0, stream_>>>(w_, 0, n, 0, 0, so);
+            launches_ += 2;
+        }
+        span_end(e, 5);
+        DIO_CK(cudaGetLastError());
+        cur_ = 1 - cur_;
+        set_rows(cur_);
+        ++steps_;
+        return DIO_OK;
+    }
+
+    // Jones-Plassmann rounds until every dynamic body has a colour, then
+    // the per-colour body lists (colour counts read back to the host).
+    int color_world(uint32_t n) {
+        if (!n) {
+            ncolors_ = 0;
+            return DIO_OK;
+        }
+        const int g = grid_for(std::max(1u, w_.n_dyn), 256);
+        k_color_init<P, R><<<grid_for(n, 256), 256, 0, stream_>>>(w_);
+        k_set_u32<<<1, 1, 0, stream_>>>(&ctr_->color_remaining, w_.n_dyn);
+        k_set_u32<<<1, 1, 0, stream_>>>(&ctr_->colors, 0);
+        uint32_t remaining = w_.n_dyn, rounds = 0;
+        while (remaining) {
+            for (int r = 0; r < 4; ++r) {
+                k_color_select<P, R><<<g, 256, 0, stream_>>>(w_, counts_);
+                k_color_assign<P, R><<<g, 256, 0, stream_>>>(w_, counts_);
+                launches_ += 2;
+            }
+            rounds += 4;
+            DIO_CK(cudaMemcpyAsync(&remaining, &ctr_->color_remaining, 4, cudaMemcpyDeviceToHost, stream_));
+            DIO_CK(cudaStreamSynchronize(stream_));
+            if (rounds > 4096) return cap_err("colouring did not converge");
+        }
+        DIO_CK(cudaMemsetAsync(color_hist_, 0, (kMaxColors + 1) * 4, stream_));
+        k_color_hist<P, R><<<g, 256, 0, stream_>>>(w_, color_hist_);
+        size_t tb = cub_bytes_;
+        DIO_CK(cub::DeviceScan::ExclusiveSum(cub_tmp_, tb, color_hist_, w_.color_off, (int)kMaxColors + 1, stream_));
+        DIO_CK(cudaMemsetAsync(color_hist_, 0, (kMaxColors + 1) * 4, stream_));
+        k_color_fill<P, R><<<g, 256, 0, stream_>>>(w_, color_hist_);
+        launches_ += 3;
+        DIO_CK(cudaMemcpyAsync(&ncolors_, &ctr_->colors, 4, cudaMemcpyDeviceToHost, stream_));
+        DIO_CK(cudaMemcpyAsync(color_off_h_, w_.color_off, (kMaxColors + 1) * 4, cudaMemcpyDeviceToHost, stream_));
+        DIO_CK(cudaStreamSynchronize(stream_));
+        return DIO_OK;
+    }
+
     int step_once_dev(const DioAvbdOptions& opt) {
         DIO_TRY(step_body_dev(opt));
         cur_ = 1 - cur_;
@@ -1413,6 +1502,9 @@ class Engine final : public EngineBase {
     uint32_t *joint_off_ = nullptr, *joint_idx_ = nullptr;
     JView* jview_ = nullptr;
     uint32_t* dyn_list_ = nullptr;
+    uint32_t* color_hist_ = nullptr;
+    uint32_t ncolors_ = 0;
+    uint32_t color_off_h_[kMaxColors + 1] = {};
     uint32_t *counts_ = nullptr, *offsets_ = nullptr, *counts2_ = nullptr, *offsets2_ = nullptr;
     SceneDesc* scenes_ = nullptr;
     std::vector<SceneDesc> scenes_host_;

@@ -247,3 +247,33 @@ def test_profiled_world_times_every_primal_launch(use_graph):
     assert st["primal_launches"] == 4 * iters
     assert st["primal_ms"] > 0 and st["solve_ms"] >= st["primal_ms"]
     assert st["kernel_launches"] > 4 * 2 * iters
+
+
+def _independent(colors, rows, joints, dyn):
+    for a, b in list(zip(rows["a"], rows["b"])) + list(zip(joints["a"], joints["b"])):
+        if b == abi.CONTAINER or a == b or not (dyn[a] and dyn[b]):
+            continue
+        if colors[a] == colors[b]:
+            return False
+    return True
+
+
+def test_colored_world_matches_oracle():
+    """Coloured Gauss-Seidel mode: the colouring (Jones-Plassmann, hashed
+    priorities) and the resulting states equal the oracle's bit for bit."""
+    for sc in [scenes.pyramid(levels=5), scenes.constraints_demo(), scenes.box_demo(),
+               scenes.cube_field(nx=6, nz=6, ny=3)]:
+        ow = O.World(sc, solver_mode=1)
+        with _world(sc, solver_mode=1) as w:
+            for step in range(30):
+                ow.step(sc.options, 1)
+                w.step(sc.options, 1)
+                gc, rc = w.colors(), ow.colors()
+                assert np.array_equal(gc, rc), (sc.name, step)
+            gb, gs = w.download()
+            rows = w.contacts()
+        rb, rs = ow.download()
+        assert np.array_equal(_bits(gb), _bits(rb)), sc.name
+        assert np.array_equal(_bits(gs), _bits(rs)), sc.name
+        dyn = sc.state["inv_mass"] != 0
+        assert _independent(gc, rows, sc.constraints, dyn), sc.name
