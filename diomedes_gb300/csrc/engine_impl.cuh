@@ -1070,7 +1070,7 @@ class Engine final : public EngineBase {
         int g = np_dev ? sms_ * 8 : grid_for(np, 128);
         k_narrow_main<P, R><<<g, 128, 0, stream_>>>(w_, np_dev, np);
         k_gjk<P, R><<<sms_ * 4, 128, 0, stream_>>>(w_);
-        k_epa<P, R><<<sms_ * 4, 32 * kEpaWarps, 0, stream_>>>(w_);
+        k_epa<P, R><<<sms_ * 4, 32 * epa_warps<R>(), 0, stream_>>>(w_);
         launches_ += 3;
         return DIO_OK;
     }

@@ -438,7 +438,8 @@ __device__ bool gjk(const NB<R>& a, const NB<R>& b, const A4<R>* hull, Simplex<R
 constexpr int kEpaV = 68;   // 4 simplex points + one per iteration (64)
 constexpr int kEpaF = 256;  // face capacity (reference: 512; overflow flagged)
 constexpr int kEpaH = 256;  // horizon capacity (reference: 512; overflow flagged)
-constexpr int kEpaWarps = 4;
+template <class R>
+__host__ __device__ constexpr int epa_warps() { return sizeof(R) == 8 ? 2 : 4; }  // FP64 polytopes are twice the size
 
 template <class R>
 struct EpaSmem {

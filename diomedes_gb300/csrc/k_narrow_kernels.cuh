@@ -97,7 +97,8 @@ __global__ void __launch_bounds__(128) k_gjk(DevWorld<P, R> w) {
 
 // Stage 3: EPA, one warp per queued pair, polytope in shared memory.
 template <class P, class R>
-__global__ void __launch_bounds__(32 * kEpaWarps) k_epa(DevWorld<P, R> w) {
+__global__ void __launch_bounds__(32 * epa_warps<R>()) k_epa(DevWorld<P, R> w) {
+    constexpr int kEpaWarps = epa_warps<R>();
     __shared__ EpaSmem<R> smem[kEpaWarps];
     const uint32_t warp = threadIdx.x >> 5;
     const uint32_t lane = threadIdx.x & 31;
