@@ -84,7 +84,8 @@ class Capacity(ctypes.Structure):
 class Config(ctypes.Structure):
     _fields_ = [("solver_mode", _u32), ("precision", _u32), ("contacts_per_pair", _u32),
                 ("use_graph", _u32), ("primal_variant", _u32), ("block_size", _u32),
-                ("batched_solver", _u32), ("profile", _u32), ("broad_phase", _u32), ("reserved", _u32 * 3)]
+                ("batched_solver", _u32), ("profile", _u32), ("broad_phase", _u32),
+                ("bvh_rebuild_period", _u32), ("reserved", _u32 * 2)]
 
 
 class WorldDesc(ctypes.Structure):
@@ -137,6 +138,7 @@ _PROTOS = {
     "dio_world_colors": [_P, _vp, _u32, ctypes.POINTER(_u32)],
     "dio_world_stats": [_P, ctypes.POINTER(StepStats)],
     "dio_world_reset_timers": [_P],
+    "dio_autotune": [_P, ctypes.POINTER(AvbdOptions), _u32, ctypes.c_char_p, ctypes.POINTER(Config)],
 }
 
 _LIB = None

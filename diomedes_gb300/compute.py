@@ -280,5 +280,14 @@ class World(Context):
                 "dual_launches": s.dual_launches, "primal_ms": s.primal_ms, "dual_ms": s.dual_ms,
                 "broad_ms": s.broad_ms, "narrow_ms": s.narrow_ms, "rows_ms": s.rows_ms, "solve_ms": s.solve_ms}
 
+    def autotune(self, options, trial_steps=5, cache_path=None):
+        """dio_autotune: pick the fastest launch shape / LBVH rebuild period
+        for this world (state unchanged); returns the chosen config."""
+        c = abi.Config()
+        path = cache_path.encode() if cache_path else None
+        check(self.L.dio_autotune(self.h, ctypes.byref(options), trial_steps, path, ctypes.byref(c)), self.h,
+              "autotune")
+        return {name: getattr(c, name) for name, _ in abi.Config._fields_ if name != "reserved"}
+
     def reset_timers(self):
         check(self.L.dio_world_reset_timers(self.h), self.h, "reset_timers")

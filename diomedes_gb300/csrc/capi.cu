@@ -7,6 +7,8 @@
 // configured precision behind dio_world_* / dio_step.
 #include <cuda_runtime.h>
 
+#include <chrono>
+#include <cstdio>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -276,6 +278,122 @@ int dio_world_stats(DioCtx* ctx, DioStepStats* out) {
 }
 int dio_world_reset_timers(DioCtx* ctx) {
     return with_world(ctx, false, [&](dio::EngineBase* e) { return e->reset_timers(); });
+}
+
+}  // extern "C"
+
+namespace {
+
+std::string tune_key(DioCtx* ctx, dio::EngineBase* e) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceProp prop{};
+    cudaGetDeviceProperties(&prop, dev);
+    uint32_t n = 0, nd = 0, nj = 0, ns = 0;
+    e->world_sizes(&n, &nd, &nj, &ns);
+    std::string name(prop.name);
+    for (char& c : name)
+        if (c == ' ') c = '_';
+    return name + "|" + std::to_string(n) + "|" + std::to_string(nd) + "|" + std::to_string(nj) + "|" +
+           std::to_string(ns) + "|p" + std::to_string(ctx->cfg.precision) + "|s" + std::to_string(ctx->cfg.solver_mode);
+}
+
+bool cache_lookup(const char* path, const std::string& key, uint32_t* variant, uint32_t* period) {
+    if (!path) return false;
+    FILE* f = std::fopen(path, "r");
+    if (!f) return false;
+    char line[512];
+    bool found = false;
+    while (std::fgets(line, sizeof line, f)) {
+        char k[400];
+        unsigned v = 0, p = 0;
+        if (std::sscanf(line, "%399s %u %u", k, &v, &p) == 3 && key == k) {
+            *variant = v;
+            *period = p;
+            found = true;  // the last entry wins
+        }
+    }
+    std::fclose(f);
+    return found;
+}
+
+// wall time of `steps` world steps (each dio_step call ends synchronised)
+int time_steps(DioCtx* ctx, dio::EngineBase* e, const DioAvbdOptions* o, uint32_t steps, double* ms) {
+    auto t0 = std::chrono::steady_clock::now();
+    int rc = e->step(o, steps);
+    auto t1 = std::chrono::steady_clock::now();
+    if (rc) return fail(ctx, rc, e->err);
+    *ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+    return DIO_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dio_autotune(DioCtx* ctx, const DioAvbdOptions* options, uint32_t trial_steps, const char* cache_path,
+                 DioConfig* best) {
+    if (!ctx || !options) return DIO_ERR_INVALID;
+    dio::EngineBase* e = nullptr;
+    int rc = world_engine(ctx, false, &e);
+    if (rc) return rc;
+    if (trial_steps == 0) trial_steps = 5;
+    const std::string key = tune_key(ctx, e);
+    DioConfig cfg = ctx->cfg;
+    uint32_t v = 0, p = 0;
+    if (cache_lookup(cache_path, key, &v, &p) && v < 10) {
+        cfg.primal_variant = v;
+        cfg.bvh_rebuild_period = p;
+        rc = dio_ctx_configure(ctx, &cfg);
+        if (!rc && best) *best = ctx->cfg;
+        return rc;
+    }
+    if ((rc = e->snapshot())) return fail(ctx, rc, e->err);
+    auto trial = [&](const DioConfig& c, double* ms) -> int {
+        int r = dio_ctx_configure(ctx, &c);
+        if (r) return r;
+        if ((r = e->restore())) return fail(ctx, r, e->err);
+        double warm = 0.0;
+        if ((r = time_steps(ctx, e, options, 2, &warm))) return r;  // captures the graphs
+        return time_steps(ctx, e, options, trial_steps, ms);
+    };
+    // 1) primal launch shape at the default rebuild period
+    double best_ms = 1e300;
+    DioConfig best_cfg = cfg;
+    for (uint32_t var = 0; var < 10; ++var) {
+        DioConfig c = cfg;
+        c.primal_variant = var;
+        double ms = 0.0;
+        if ((rc = trial(c, &ms))) return rc;
+        if (ms < best_ms) {
+            best_ms = ms;
+            best_cfg = c;
+        }
+    }
+    // 2) LBVH rebuild period with that shape
+    const uint32_t periods[] = {1, 2, 4, 8, 16};
+    DioConfig base = best_cfg;
+    for (uint32_t per : periods) {
+        DioConfig c = base;
+        c.bvh_rebuild_period = per;
+        double ms = 0.0;
+        if ((rc = trial(c, &ms))) return rc;
+        if (ms < best_ms) {
+            best_ms = ms;
+            best_cfg = c;
+        }
+    }
+    if ((rc = dio_ctx_configure(ctx, &best_cfg))) return rc;
+    if ((rc = e->restore())) return fail(ctx, rc, e->err);
+    if (cache_path) {
+        if (FILE* f = std::fopen(cache_path, "a")) {
+            std::fprintf(f, "%s %u %u %.4f\n", key.c_str(), best_cfg.primal_variant, best_cfg.bvh_rebuild_period,
+                         best_ms / trial_steps);
+            std::fclose(f);
+        }
+    }
+    if (best) *best = ctx->cfg;
+    return DIO_OK;
 }
 
 }  // extern "C"

@@ -42,6 +42,11 @@ struct EngineBase {
     virtual int colors(uint32_t* out, uint32_t cap, uint32_t* n) = 0;
     virtual int stats(DioStepStats* out) = 0;
     virtual int reset_timers() = 0;
+    // device copy of the world's evolving state (poses, velocities, rows,
+    // counters) and its restoration; used by the autotuner's trials
+    virtual int snapshot() = 0;
+    virtual int restore() = 0;
+    virtual int world_sizes(uint32_t* n, uint32_t* n_dyn, uint32_t* n_joints, uint32_t* n_scenes) = 0;
     virtual void set_stream(cudaStream_t s) = 0;
     virtual void set_config(const DioConfig& c) = 0;
 

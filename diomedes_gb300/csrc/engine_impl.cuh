@@ -335,6 +335,7 @@ class Engine final : public EngineBase {
     ~Engine() override {
         drop_graphs();
         collect_spans();
+        if (snap_) cudaFree(snap_);
         for (auto e : ev_free_) cudaEventDestroy(e);
         release();
     }
@@ -481,6 +482,8 @@ class Engine final : public EngineBase {
         DIO_TRY(upload_bodies(bodies, n));
         DIO_TRY(single_scene(n, nullptr));
         DIO_CK(cudaMemsetAsync(ctr_, 0, sizeof(Counters), stream_));
+        rebuild_now_ = true;
+        lbvh_valid_ = false;
         return run_broad(0, n);
     }
     int pair_count(uint32_t* count) override {
@@ -679,6 +682,7 @@ class Engine final : public EngineBase {
         if (d->n_hull_vertices > cap_.max_hull_vertices) return cap_err("too many hull vertices");
         if (n && (!d->bodies || !d->state)) return inval("null bodies/state");
         drop_graphs();
+        lbvh_valid_ = false;
         DIO_TRY(upload_bodies(d->bodies, n));
         if (d->positions_f64 || d->orientations_f64) {
             double* dp = reinterpret_cast<double*>(dstage_);
@@ -1030,6 +1034,7 @@ class Engine final : public EngineBase {
     int run_lbvh(uint32_t n) {
         uint32_t ns = std::max(1u, w_.n_scenes);
         int g = grid_for(n, 256);
+        if (!rebuild_now_) return run_lbvh_refit(n, g);
         k_bounds_init<<<grid_for(ns, 128), 128, 0, stream_>>>(lb_bounds_, ns);
         k_scene_bounds<R><<<g, 256, 0, stream_>>>(w_.aabb_min, w_.aabb_max, w_.scene, n, lb_bounds_);
         const uint32_t sbits = ns > 1 ? bits_for(ns - 1) : 0;
@@ -1039,8 +1044,16 @@ class Engine final : public EngineBase {
         size_t tb = cub_bytes_;
         DIO_CK(cub::DeviceRadixSort::SortPairs(cub_tmp_, tb, lb_keys_, lb_keys_s_, lb_vals_, lb_leaf_, (int)n, 0,
                                                (int)(sbits + 3 * abits), stream_));
-        DIO_CK(cudaMemsetAsync(lb_visits_, 0, (size_t)n * 4, stream_));
         k_karras<<<g, 256, 0, stream_>>>(lb_keys_s_, scenes_, w_.scene, n, lb_children_, lb_parent_);
+        launches_ += 4;
+        return run_lbvh_refit(n, g);
+    }
+
+    // Refit the current tree to this step's AABBs and traverse it.  Any
+    // valid tree over the scene's leaves yields the exact overlap set, so
+    // the topology is rebuilt only every bvh_rebuild_period steps.
+    int run_lbvh_refit(uint32_t n, int g) {
+        DIO_CK(cudaMemsetAsync(lb_visits_, 0, (size_t)n * 4, stream_));
         k_refit<R><<<g, 256, 0, stream_>>>(w_.aabb_min, w_.aabb_max, lb_leaf_, scenes_, w_.scene, n, lb_children_,
                                            lb_parent_, lb_leaf_min_, lb_leaf_max_, lb_node_min_, lb_node_max_,
                                            lb_visits_);
@@ -1049,7 +1062,7 @@ class Engine final : public EngineBase {
                                                lb_leaf_max_, lb_node_min_, lb_node_max_, counts_, offsets_, lb_pb_,
                                                w_.max_pairs, false, &ctr_->error_flags);
         DIO_CK(cudaMemsetAsync(counts_ + n, 0, 4, stream_));
-        tb = cub_bytes_;
+        size_t tb = cub_bytes_;
         DIO_CK(cub::DeviceScan::ExclusiveSum(cub_tmp_, tb, counts_, offsets_, (int)n + 1, stream_));
         k_traverse<R><<<gt, 128, 0, stream_>>>(lb_leaf_, scenes_, w_.scene, n, lb_children_, lb_leaf_min_,
                                                lb_leaf_max_, lb_node_min_, lb_node_max_, counts_, offsets_, lb_pb_,
@@ -1059,7 +1072,7 @@ class Engine final : public EngineBase {
         k_sort_segments<<<g, 256, 0, stream_>>>(offsets_, n, w_.max_pairs, lb_pb_, lb_long_, lb_long_count_);
         k_sort_long<<<sms_, 512, 0, stream_>>>(offsets_, lb_pb_, lb_long_, lb_long_count_, &ctr_->error_flags);
         k_pairs_from_segments<<<g, 256, 0, stream_>>>(offsets_, n, lb_pb_, w_.pairs, w_.max_pairs);
-        launches_ += 12;
+        launches_ += 8;
         return DIO_OK;
     }
 
@@ -1211,6 +1224,69 @@ class Engine final : public EngineBase {
     }
 
    public:
+    int snapshot() override {
+        if (!world_ready_) return state_err("no world uploaded");
+        const size_t nb = (size_t)std::max(1u, cap_.max_bodies), nr = (size_t)std::max(1u, cap_.max_contacts);
+        if (!snap_) {
+            snap_bytes_ = nb * sizeof(A4<P>) * 5 + nr * (sizeof(RowStatic<R>) + sizeof(RowDual<P, R>) + sizeof(uint2)) * 2 +
+                          sizeof(Counters) + 4096;
+            DIO_CK(cudaMalloc(&snap_, snap_bytes_));
+        }
+        DIO_TRY(snap_copy(true));
+        snap_cur_ = cur_;
+        snap_steps_ = steps_;
+        snap_valid_ = lbvh_valid_;
+        return DIO_OK;
+    }
+    int restore() override {
+        if (!snap_) return state_err("no snapshot");
+        DIO_TRY(snap_copy(false));
+        cur_ = snap_cur_;
+        set_rows(cur_);
+        steps_ = snap_steps_;
+        lbvh_valid_ = snap_valid_;
+        return DIO_OK;
+    }
+    int world_sizes(uint32_t* n, uint32_t* n_dyn, uint32_t* n_joints, uint32_t* n_scenes) override {
+        *n = w_.n;
+        *n_dyn = w_.n_dyn;
+        *n_joints = w_.n_joints;
+        *n_scenes = w_.n_scenes;
+        return DIO_OK;
+    }
+
+   private:
+    int snap_copy(bool save) {
+        char* p = static_cast<char*>(snap_);
+        const size_t nb = (size_t)std::max(1u, cap_.max_bodies), nr = (size_t)std::max(1u, cap_.max_contacts);
+        auto cp = [&](void* dev, size_t bytes) -> cudaError_t {
+            cudaError_t e = save ? cudaMemcpyAsync(p, dev, bytes, cudaMemcpyDeviceToDevice, stream_)
+                                 : cudaMemcpyAsync(dev, p, bytes, cudaMemcpyDeviceToDevice, stream_);
+            p += (bytes + 255) & ~size_t(255);
+            return e;
+        };
+        const size_t a4 = nb * sizeof(A4<P>);
+        DIO_CK(cp(w_.pos[0], a4));
+        DIO_CK(cp(w_.rot[0], a4));
+        DIO_CK(cp(w_.vel, a4));
+        DIO_CK(cp(w_.ang, a4));
+        DIO_CK(cp(w_.prev_vel, a4));
+        for (int b = 0; b < 2; ++b) {
+            DIO_CK(cp(rs_[b], nr * sizeof(RowStatic<R>)));
+            DIO_CK(cp(rd_[b], nr * sizeof(RowDual<P, R>)));
+            DIO_CK(cp(ab_[b], nr * sizeof(uint2)));
+        }
+        DIO_CK(cp(ctr_, sizeof(Counters)));
+        DIO_CK(cudaStreamSynchronize(stream_));
+        return DIO_OK;
+    }
+    void* snap_ = nullptr;
+    size_t snap_bytes_ = 0;
+    int snap_cur_ = 0;
+    uint64_t snap_steps_ = 0;
+    bool snap_valid_ = false;
+
+   public:
     int reset_timers() override {
         collect_spans();
         primal_ms_ = dual_ms_ = 0.0;
@@ -1250,6 +1326,7 @@ class Engine final : public EngineBase {
     // Coloured Gauss-Seidel step: same detection and rows, then a colouring
     // and per-colour primal sweeps in place (host-driven colour loop).
     int step_once_colored(const DioAvbdOptions& opt) {
+        plan_rebuild();
         uint32_t n = w_.n;
         PrepParams<R> pp = opts_prep(opt);
         set_rows(cur_);
@@ -1332,7 +1409,15 @@ class Engine final : public EngineBase {
         return DIO_OK;
     }
 
+    // decide whether this step rebuilds the LBVH topology or refits it
+    void plan_rebuild() {
+        uint32_t period = cfg_.bvh_rebuild_period ? cfg_.bvh_rebuild_period : 4;
+        rebuild_now_ = !lbvh_valid_ || period <= 1 || (steps_ % period) == 0;
+        lbvh_valid_ = true;
+    }
+
     int step_once_dev(const DioAvbdOptions& opt) {
+        plan_rebuild();
         DIO_TRY(step_body_dev(opt));
         cur_ = 1 - cur_;
         set_rows(cur_);
@@ -1369,7 +1454,9 @@ class Engine final : public EngineBase {
         std::vector<std::pair<cudaGraphNode_t, cudaGraphNode_t>> span_nodes;
         std::vector<int> span_kinds;
     };
-    GraphSlot graphs_[2];
+    GraphSlot graphs_[4];  // (row-buffer parity, LBVH rebuild or refit)
+    bool rebuild_now_ = true;
+    bool lbvh_valid_ = false;
 
     void drop_graphs() {
         for (auto& g : graphs_) {
@@ -1435,7 +1522,8 @@ class Engine final : public EngineBase {
     }
 
     int step_graph(const DioAvbdOptions& opt) {
-        GraphSlot& g = graphs_[cur_];
+        plan_rebuild();
+        GraphSlot& g = graphs_[cur_ * 2 + (rebuild_now_ ? 1 : 0)];
         if (!g.exec || std::memcmp(&g.opt, &opt, sizeof opt) != 0) DIO_TRY(capture(g, opt));
         for (size_t k = 0; k < g.span_nodes.size(); ++k) {
             if (!g.span_nodes[k].first || !g.span_nodes[k].second) continue;

@@ -134,10 +134,38 @@ __global__ void __launch_bounds__(256) k_init(DevWorld<P, R> w, uint32_t lo, uin
         init_body(w, i, o);
 }
 
-// One contact row seen from body i (avbd/src/lib.rs:321-418).
+// Where the primal reads another body's snapshot / step-start pose: global
+// memory, or a shared-memory tile of consecutive bodies with a global
+// fallback.  Both return the same values.
 template <class P, class R>
-__device__ __forceinline__ void primal_row(const DevWorld<P, R>& w, uint32_t r, uint32_t oth, int rd, Q4<R> sqr,
-                                           V3<R> dqsl, V3<R> dqsa, R k_alpha, Block6<R>& B) {
+struct GlobalFetch {
+    const DevWorld<P, R>& w;
+    int rd;
+    __device__ __forceinline__ A4<P> pos(uint32_t j) const { return w.pos[rd][j]; }
+    __device__ __forceinline__ A4<P> rot(uint32_t j) const { return w.rot[rd][j]; }
+    __device__ __forceinline__ A4<P> ipos(uint32_t j) const { return w.init_pos[j]; }
+    __device__ __forceinline__ A4<P> irot(uint32_t j) const { return w.init_rot[j]; }
+};
+
+template <class P, class R, int T>
+struct TileFetch {
+    const DevWorld<P, R>& w;
+    int rd;
+    uint32_t lo;
+    const A4<P>* sp;
+    const A4<P>* sq;
+    const A4<P>* si;
+    const A4<P>* sr;
+    __device__ __forceinline__ A4<P> pos(uint32_t j) const { return j - lo < (uint32_t)T ? sp[j - lo] : w.pos[rd][j]; }
+    __device__ __forceinline__ A4<P> rot(uint32_t j) const { return j - lo < (uint32_t)T ? sq[j - lo] : w.rot[rd][j]; }
+    __device__ __forceinline__ A4<P> ipos(uint32_t j) const { return j - lo < (uint32_t)T ? si[j - lo] : w.init_pos[j]; }
+    __device__ __forceinline__ A4<P> irot(uint32_t j) const { return j - lo < (uint32_t)T ? sr[j - lo] : w.init_rot[j]; }
+};
+
+// One contact row seen from body i (avbd/src/lib.rs:321-418).
+template <class P, class R, class F>
+__device__ __forceinline__ void primal_row_f(const DevWorld<P, R>& w, uint32_t r, uint32_t oth, const F& fetch,
+                                             Q4<R> sqr, V3<R> dqsl, V3<R> dqsa, R k_alpha, Block6<R>& B) {
     const RowStatic<R> rs = w.rs[r];
     const RowDual<P, R> du = w.rd[r];
     const bool container = oth == kContainer;
@@ -150,10 +178,10 @@ __device__ __forceinline__ void primal_row(const DevWorld<P, R>& w, uint32_t r, 
     V3<R> rw = rotate(sqr, is_a ? xyz(rs.ra) : xyz(rs.rb));
     V3<R> dol{R(0), R(0), R(0)}, doa{R(0), R(0), R(0)}, rot_other{R(0), R(0), R(0)};
     if (!container) {
-        A4<P> op = w.pos[rd][other];
-        A4<P> oq = w.rot[rd][other];
-        dol = cast3<R>(sub(xyz(op), xyz(w.init_pos[other])));
-        doa = cast3<R>(ang_diff(quat(oq), quat(w.init_rot[other])));
+        A4<P> op = fetch.pos(other);
+        A4<P> oq = fetch.rot(other);
+        dol = cast3<R>(sub(xyz(op), xyz(fetch.ipos(other))));
+        doa = cast3<R>(ang_diff(quat(oq), quat(fetch.irot(other))));
         rot_other = rotate(castq<R>(quat(oq)), is_a ? xyz(rs.rb) : xyz(rs.ra));
     }
     V3<R> j0 = cross(rw, r0), j1 = cross(rw, r1), j2 = cross(rw, r2);
@@ -175,6 +203,12 @@ __device__ __forceinline__ void primal_row(const DevWorld<P, R>& w, uint32_t r, 
     stamp(B, r0, j0, du.penalty.x, R(f0));
     stamp(B, r1, j1, du.penalty.y, R(f1));
     stamp(B, r2, j2, du.penalty.z, R(f2));
+}
+
+template <class P, class R>
+__device__ __forceinline__ void primal_row(const DevWorld<P, R>& w, uint32_t r, uint32_t oth, int rd, Q4<R> sqr,
+                                           V3<R> dqsl, V3<R> dqsa, R k_alpha, Block6<R>& B) {
+    primal_row_f(w, r, oth, GlobalFetch<P, R>{w, rd}, sqr, dqsl, dqsa, k_alpha, B);
 }
 
 // One joint seen from body i (avbd/src/lib.rs:425-537).
@@ -217,9 +251,9 @@ __device__ __forceinline__ void primal_joint(const DevWorld<P, R>& w, const DioC
 
 // The same joint row from a JView: p_a - p_b is formed exactly as the
 // reference forms it (joint a's anchor point minus joint b's).
-template <class P, class R>
-__device__ __forceinline__ void primal_jview(const DevWorld<P, R>& w, const JView& jv, int rd, V3<P> sp, Q4<P> sq,
-                                             Q4<R> sqr, Block6<R>& B) {
+template <class P, class R, class F>
+__device__ __forceinline__ void primal_jview_f(const JView& jv, const F& fetch, V3<P> sp, Q4<P> sq, Q4<R> sqr,
+                                               Block6<R>& B) {
     const bool is_a = !(jv.kind & kIsB);
     const uint32_t kind = jv.kind & ~kIsB;
     const V3<R> anc_s{R(jv.self_anchor.x), R(jv.self_anchor.y), R(jv.self_anchor.z)};
@@ -233,7 +267,7 @@ __device__ __forceinline__ void primal_jview(const DevWorld<P, R>& w, const JVie
         p_self = add(sp, rotate(sq, cast3<P>(anc_s)));
         r_self = rotate(sqr, anc_s);
     }
-    const V3<P> p_other = add(xyz(w.pos[rd][jv.other]), rotate(quat(w.rot[rd][jv.other]), cast3<P>(anc_o)));
+    const V3<P> p_other = add(xyz(fetch.pos(jv.other)), rotate(quat(fetch.rot(jv.other)), cast3<P>(anc_o)));
     const V3<R> delta = cast3<R>(is_a ? sub(p_self, p_other) : sub(p_other, p_self));
     const R sign = is_a ? R(1) : R(-1);
     const R stiff = R(jv.other_anchor.w);
@@ -257,14 +291,14 @@ __device__ __forceinline__ void primal_jview(const DevWorld<P, R>& w, const JVie
     }
 }
 
-// avbd_primal for one body: reads buffer rd, writes buffer wr.
-template <class P, class R>
-__device__ __forceinline__ void primal_body(const DevWorld<P, R>& w, uint32_t i, int rd, int wr,
-                                            const SolveParams<R>& o) {
+// avbd_primal for one body: reads buffer rd (through `fetch`), writes wr.
+template <class P, class R, class F>
+__device__ __forceinline__ void primal_body_f(const DevWorld<P, R>& w, uint32_t i, int wr, const SolveParams<R>& o,
+                                              const F& fetch) {
     const A4<R> inv = w.inv[i];
     if (inv.w == R(0)) return;
-    const V3<P> sp = xyz(w.pos[rd][i]);
-    const Q4<P> sq = quat(w.rot[rd][i]);
+    const V3<P> sp = xyz(fetch.pos(i));
+    const Q4<P> sq = quat(fetch.rot(i));
     const Q4<R> sqr = castq<R>(sq);
     R mdt2;
     V3<R> idt2;
@@ -296,22 +330,47 @@ __device__ __forceinline__ void primal_body(const DevWorld<P, R>& w, uint32_t i,
     B.g[3] = ra.x;
     B.g[4] = ra.y;
     B.g[5] = ra.z;
-    const V3<R> dqsl = cast3<R>(sub(sp, xyz(w.init_pos[i])));
-    const V3<R> dqsa = cast3<R>(ang_diff(sq, quat(w.init_rot[i])));
+    const V3<R> dqsl = cast3<R>(sub(sp, xyz(fetch.ipos(i))));
+    const V3<R> dqsa = cast3<R>(ang_diff(sq, quat(fetch.irot(i))));
     const R k_alpha = R(1) - o.alpha;
     const uint32_t j0 = w.row_off[i], j1 = w.row_off[i + 1];
-    for (uint32_t j = j0; j < j1; ++j) primal_row(w, w.row_idx[j], w.row_oth[j], rd, sqr, dqsl, dqsa, k_alpha, B);
+    for (uint32_t j = j0; j < j1; ++j) primal_row_f(w, w.row_idx[j], w.row_oth[j], fetch, sqr, dqsl, dqsa, k_alpha, B);
     if (w.n_joints) {
         const uint32_t k0 = w.joint_off[i], k1 = w.joint_off[i + 1];
         for (uint32_t k = k0; k < k1; ++k) {
             const JView jv = w.jview[k];
-            primal_jview(w, jv, rd, sp, sq, sqr, B);
+            primal_jview_f<P, R>(jv, fetch, sp, sq, sqr, B);
         }
     }
     R dx[6];
     solve6(B, dx);
     w.pos[wr][i] = pack(add(sp, cast3<P>(V3<R>{dx[0], dx[1], dx[2]})));
     w.rot[wr][i] = packq(quat_step(sq, cast3<P>(V3<R>{dx[3], dx[4], dx[5]})));
+}
+
+template <class P, class R>
+__device__ __forceinline__ void primal_body(const DevWorld<P, R>& w, uint32_t i, int rd, int wr,
+                                            const SolveParams<R>& o) {
+    primal_body_f(w, i, wr, o, GlobalFetch<P, R>{w, rd});
+}
+
+// Tile variant: the CTA's T consecutive bodies stage their snapshot and
+// step-start poses in shared memory; neighbours inside the tile (chain links,
+// nearby boxes) are read from there.  Jacobi only (buffer rd is read-only
+// during the launch).
+template <class P, class R, int T, int MINB>
+__global__ void __launch_bounds__(T, MINB) k_primal_tile(DevWorld<P, R> w, int rd, int wr, SolveParams<R> o) {
+    __shared__ A4<P> s_pos[T], s_rot[T], s_ipos[T], s_irot[T];
+    const uint32_t lo = blockIdx.x * T;
+    const uint32_t i = lo + threadIdx.x;
+    if (i < w.n) {
+        s_pos[threadIdx.x] = w.pos[rd][i];
+        s_rot[threadIdx.x] = w.rot[rd][i];
+        s_ipos[threadIdx.x] = w.init_pos[i];
+        s_irot[threadIdx.x] = w.init_rot[i];
+    }
+    __syncthreads();
+    if (i < w.n) primal_body_f(w, i, wr, o, TileFetch<P, R, T>{w, rd, lo, s_pos, s_rot, s_ipos, s_irot});
 }
 
 // One thread per dynamic body (static bodies are never solved,
@@ -324,9 +383,11 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_primal(DevWorld<P, R> w, int rd
         primal_body(w, w.dyn_list[t], rd, wr, o);
 }
 
-// launch-shape variants of k_primal: {threads per CTA, min CTAs per SM}
-constexpr int kPrimalVariants = 6;
-constexpr int kPrimalShape[kPrimalVariants][2] = {{128, 4}, {128, 5}, {128, 6}, {256, 2}, {256, 3}, {64, 10}};
+// launch-shape variants: 0-5 k_primal over the dynamic-body list with
+// {threads per CTA, min CTAs per SM}; 6-9 k_primal_tile over body tiles
+constexpr int kPrimalVariants = 10;
+constexpr int kPrimalShape[kPrimalVariants][2] = {{128, 4}, {128, 5}, {128, 6}, {256, 2}, {256, 3},
+                                                  {64, 10}, {128, 5}, {128, 6}, {256, 3}, {64, 10}};
 
 template <class P, class R>
 inline void launch_primal(int variant, int blocks_per_sm_hint, int sms, const DevWorld<P, R>& w, int rd, int wr,
@@ -349,6 +410,18 @@ inline void launch_primal(int variant, int blocks_per_sm_hint, int sms, const De
             break;
         case 5:
             k_primal<P, R, 64, 10><<<grid(64), 64, 0, s>>>(w, rd, wr, o);
+            break;
+        case 6:
+            k_primal_tile<P, R, 128, 5><<<grid_for(w.n, 128), 128, 0, s>>>(w, rd, wr, o);
+            break;
+        case 7:
+            k_primal_tile<P, R, 128, 6><<<grid_for(w.n, 128), 128, 0, s>>>(w, rd, wr, o);
+            break;
+        case 8:
+            k_primal_tile<P, R, 256, 3><<<grid_for(w.n, 256), 256, 0, s>>>(w, rd, wr, o);
+            break;
+        case 9:
+            k_primal_tile<P, R, 64, 10><<<grid_for(w.n, 64), 64, 0, s>>>(w, rd, wr, o);
             break;
         default:
             k_primal<P, R, 128, 5><<<grid(128), 128, 0, s>>>(w, rd, wr, o);

@@ -216,7 +216,9 @@ typedef struct DioConfig {
     uint32_t batched_solver;    /* 1: one CTA-per-scene persistent solve  */
     uint32_t profile;           /* time primal / dual launches with events */
     uint32_t broad_phase;       /* 0: LBVH (default), 1: dense sweep        */
-    uint32_t reserved[3];
+    uint32_t bvh_rebuild_period; /* LBVH topology rebuilt every N steps and
+                                    refitted in between (0: every 4)     */
+    uint32_t reserved[2];
 } DioConfig;
 
 /* World description for the fused device-resident step (extension of the
@@ -379,6 +381,15 @@ int dio_world_colors(DioCtx* ctx, uint32_t* out, uint32_t cap, uint32_t* n);
 int dio_world_stats(DioCtx* ctx, DioStepStats* out);
 /* Reset the kernel timers and launch counter of the world (extension). */
 int dio_world_reset_timers(DioCtx* ctx);
+/* Autotuner (extension): times the primal launch-shape variants and the
+ * LBVH rebuild period on the uploaded world (trial_steps timed steps per
+ * candidate, starting from a device snapshot that is restored afterwards,
+ * so the world's state is unchanged), applies the fastest configuration and
+ * returns it in `best`.  With `cache_path` set, a tuned configuration for
+ * the same device and world shape is reused from / appended to that text
+ * file.  Every candidate computes bit-identical results. */
+int dio_autotune(DioCtx* ctx, const DioAvbdOptions* options,
+                 uint32_t trial_steps, const char* cache_path, DioConfig* best);
 
 #ifdef __cplusplus
 }

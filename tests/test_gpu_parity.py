@@ -249,6 +249,32 @@ def test_profiled_world_times_every_primal_launch(use_graph):
     assert st["kernel_launches"] > 4 * 2 * iters
 
 
+def test_autotune_keeps_state_and_results(tmp_path):
+    """Every tuned variant computes the same bits, and the trials run from a
+    snapshot that is restored: stepping after tuning still matches the
+    oracle exactly; a second call reuses the cache file."""
+    sc = scenes.pack([scenes.box_demo(), scenes.constraints_demo(), scenes.pyramid(levels=4)])
+    ow = O.World(sc)
+    ow.step(sc.options, 3)
+    with _world(sc) as w:
+        w.step(sc.options, 3)
+        before = w.download()
+        cache = str(tmp_path / "tune.txt")
+        cfg = w.autotune(sc.options, trial_steps=2, cache_path=cache)
+        after = w.download()
+        assert np.array_equal(_bits(before[0]), _bits(after[0]))
+        assert np.array_equal(_bits(before[1]), _bits(after[1]))
+        assert 0 <= cfg["primal_variant"] < 10 and cfg["bvh_rebuild_period"] >= 1
+        cfg2 = w.autotune(sc.options, trial_steps=2, cache_path=cache)
+        assert (cfg2["primal_variant"], cfg2["bvh_rebuild_period"]) == (cfg["primal_variant"],
+                                                                        cfg["bvh_rebuild_period"])
+        w.step(sc.options, 10)
+        ow.step(sc.options, 10)
+        gb, gs = w.download()
+    rb, rs = ow.download()
+    assert np.array_equal(_bits(gb), _bits(rb)) and np.array_equal(_bits(gs), _bits(rs))
+
+
 def _independent(colors, rows, joints, dyn):
     for a, b in list(zip(rows["a"], rows["b"])) + list(zip(joints["a"], joints["b"])):
         if b == abi.CONTAINER or a == b or not (dyn[a] and dyn[b]):
