@@ -228,13 +228,13 @@ def main():
     ms = e0.elapsed_time(e1)
     st = w.stats()
     b32_after, _ = w.download()  # for the FP64 comparison below
-    t = torch.tensor([ms], device="cuda")
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_max = float(t.item())
+    from diomedes_gb300 import dist as dio_dist
+
+    # max time over ranks, body-steps summed over ranks (each rank owns its scenes)
+    ms_max, body_steps = dio_dist.frame(dist, ms, sc.n * args.steps, device="cuda")
     n_dyn = int((sc.state["inv_mass"] != 0).sum())
     total_bodies = sc.n * world
-    value = total_bodies * args.steps / (ms_max / 1e3)
+    value = body_steps / (ms_max / 1e3)
 
     # roofline of the primal kernel (event-timed on the launching stream)
     peak, peak_kind = measured_hbm_peak()

@@ -502,9 +502,16 @@ __device__ __forceinline__ void recover_body(const DevWorld<P, R>& w, uint32_t i
     P dt = P(o.dt);
     A4<P> v = w.vel[i];
     w.prev_vel[i] = v;
-    w.vel[i] = pack(divs(sub(xyz(p4), xyz(w.init_pos[i])), dt));
+    const V3<P> nv = divs(sub(xyz(p4), xyz(w.init_pos[i])), dt);
+    w.vel[i] = pack(nv);
     Q4<P> rel = qmul(quat(q4), conj(quat(w.init_rot[i])));
-    w.ang[i] = pack(divs(V3<P>{P(2) * rel.x, P(2) * rel.y, P(2) * rel.z}, dt));
+    const V3<P> na = divs(V3<P>{P(2) * rel.x, P(2) * rel.y, P(2) * rel.z}, dt);
+    w.ang[i] = pack(na);
+    // a non-finite pose or velocity is reported (DIO_ERR_NONFINITE), as the
+    // reference demos' constraint tracing reports it (demos/constraints/src/main.rs:24-60)
+    if (w.ctr && !(finite_(nv.x) && finite_(nv.y) && finite_(nv.z) && finite_(na.x) && finite_(na.y) &&
+                   finite_(na.z) && finite_(q4.w)))
+        atomicOr(&w.ctr->error_flags, kErrNonFinite);
 }
 
 template <class P, class R>

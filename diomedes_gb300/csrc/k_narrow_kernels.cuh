@@ -95,23 +95,97 @@ __global__ void __launch_bounds__(128) k_gjk(DevWorld<P, R> w) {
     }
 }
 
-// Stage 3: EPA, one warp per queued pair, polytope in shared memory.
+// ---- bulk (TMA) copies global -> shared with mbarrier completion ----
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded, warp-uniform wait: every lane polls until all lanes have seen the
+// phase complete, at most `tries` rounds; the result is the same in all lanes
+__device__ __forceinline__ bool mbar_wait_warp(uint64_t* bar, uint32_t parity, uint32_t tries) {
+    bool done = false;
+    for (uint32_t k = 0; k < tries; ++k) {
+        if (!done) done = mbar_try_wait(bar, parity);
+        if (__all_sync(0xFFFFFFFFu, done)) return true;
+    }
+    return __all_sync(0xFFFFFFFFu, done);
+}
+
+constexpr uint32_t kHullStage = 64;  // vertices per hull staged in shared memory
+
+// Stage 3: EPA, one warp per queued pair, polytope in shared memory.  Hull
+// vertex lists (both bodies, up to 64 vertices each) are staged into the
+// warp's shared memory with bulk TMA copies, so the support queries of the
+// expansion read shared memory.
 template <class P, class R>
 __global__ void __launch_bounds__(32 * epa_warps<R>()) k_epa(DevWorld<P, R> w) {
     constexpr int kEpaWarps = epa_warps<R>();
     __shared__ EpaSmem<R> smem[kEpaWarps];
+    __shared__ A4<R> hull_s[kEpaWarps][2 * kHullStage];
+    __shared__ uint64_t mbar[kEpaWarps];
     const uint32_t warp = threadIdx.x >> 5;
     const uint32_t lane = threadIdx.x & 31;
     EpaSmem<R>& S = smem[warp];
+    if (lane == 0) mbar_init(&mbar[warp], 1);
+    __syncwarp();
+    uint32_t parity = 0;
     uint32_t nw = w.ctr->epa_work;
     for (uint32_t q = blockIdx.x * kEpaWarps + warp; q < nw; q += gridDim.x * kEpaWarps) {
         uint32_t p = w.epa_list[q];
         DioPair pr = w.pairs[p];
         NB<R> a = load_nb(w, pr.a);
         NB<R> b = load_nb(w, pr.b);
+        const A4<R>* hull = w.hull;
+        const bool ha = a.shape.tag == DIO_SHAPE_HULL, hb = b.shape.tag == DIO_SHAPE_HULL;
+        const bool fits = (!ha || (a.shape.hc > 0 && a.shape.hc <= kHullStage)) &&
+                          (!hb || (b.shape.hc > 0 && b.shape.hc <= kHullStage));
+        if ((ha || hb) && fits && w.hull) {
+            if (lane == 0) {
+                // order the previous pair's shared-memory reads before the async writes
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                const uint32_t bytes = (ha ? a.shape.hc : 0u) * (uint32_t)sizeof(A4<R>) +
+                                       (hb ? b.shape.hc : 0u) * (uint32_t)sizeof(A4<R>);
+                mbar_expect_tx(&mbar[warp], bytes);
+                if (ha) bulk_g2s(&hull_s[warp][0], w.hull + a.shape.hf, a.shape.hc * sizeof(A4<R>), &mbar[warp]);
+                if (hb)
+                    bulk_g2s(&hull_s[warp][kHullStage], w.hull + b.shape.hf, b.shape.hc * sizeof(A4<R>),
+                             &mbar[warp]);
+            }
+            bool done = mbar_wait_warp(&mbar[warp], parity, 1u << 20);
+            if (!done) {
+                if (lane == 0) atomicOr(&w.ctr->error_flags, kErrTimeout);
+                done = mbar_wait_warp(&mbar[warp], parity, 1u << 20);  // let the copies land
+                if (!done) return;                                     // warp-uniform
+            }
+            parity ^= 1u;
+            hull = &hull_s[warp][0];
+            if (ha) a.shape.hf = 0;
+            if (hb) b.shape.hf = kHullStage;
+        }
         V3<R> n, pa, pb;
         R depth;
-        bool ok = epa_warp(S, a, b, w.simplex + (size_t)q * 8, w.hull, &w.ctr->error_flags, n, depth, pa, pb);
+        bool ok = epa_warp(S, a, b, w.simplex + (size_t)q * 8, hull, &w.ctr->error_flags, n, depth, pa, pb);
         if (ok && lane == 0) put_slot(&w.slots[(size_t)p * w.per_pair], pr.a, pr.b, n, depth, pa, pb);
         __syncwarp();
     }

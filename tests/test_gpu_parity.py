@@ -249,6 +249,35 @@ def test_profiled_world_times_every_primal_launch(use_graph):
     assert st["kernel_launches"] > 4 * 2 * iters
 
 
+def test_nonfinite_state_is_reported():
+    """A NaN injected on the host (as a caller's bad input would arrive) is
+    reported as DIO_ERR_NONFINITE after the step, not silently propagated."""
+    sc = scenes.constraints_demo()
+    with _world(sc) as w:
+        w.step(sc.options, 2)
+        b, s = w.download()
+        bad = s.copy()
+        bad["vel"][1, 0] = np.nan
+        w.set_state(None, bad)
+        with pytest.raises(abi.DioError) as e:
+            w.step(sc.options, 1)
+        assert e.value.status == abi.DIO_ERR_NONFINITE
+        w.set_state(b, s)  # recovers once the state is finite again
+        w.step(sc.options, 1)
+
+
+def test_hull_pairs_with_staged_vertices_match_oracle():
+    """EPA on hull pairs (vertices staged by bulk copies into shared memory)."""
+    sc = scenes.mixed_pile(n=1500, extent=7.0, seed=11)
+    pairs, _ = O.broad(sc.bodies, hull=sc.hull_vertices)
+    ref = O.narrow(sc.bodies, pairs, hull=sc.hull_vertices)
+    with compute.NarrowPhaseCompute(sc.n, len(pairs), max_hull_vertices=len(sc.hull_vertices)) as npc:
+        npc.set_hull_vertices(sc.hull_vertices)
+        got = npc.run(sc.bodies, pairs)
+    assert int(ref["valid"].sum()) > 100
+    assert np.array_equal(_bits(got), _bits(ref))
+
+
 def test_autotune_keeps_state_and_results(tmp_path):
     """Every tuned variant computes the same bits, and the trials run from a
     snapshot that is restored: stepping after tuning still matches the
