@@ -274,6 +274,29 @@ static __global__ void k_dyn_fill(const uint32_t* flags, const uint32_t* pos, ui
         if (flags[i]) list[pos[i]] = i;
 }
 
+// Work signature of a dynamic body for the primal's thread order: ball-socket
+// incidences (three rows each) first, then distance joints, then the shape.
+// Bodies with one signature run the same code path, so sorting the list by
+// it keeps warps convergent; the Jacobi primal does not depend on the order.
+template <class P, class R>
+__global__ void k_dyn_keys(DevWorld<P, R> w, const uint32_t* list, uint32_t nd, uint32_t* keys) {
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nd; t += gridDim.x * blockDim.x) {
+        const uint32_t i = list[t];
+        uint32_t nb = 0, nl = 0;
+        if (w.n_joints)
+            for (uint32_t k = w.joint_off[i]; k < w.joint_off[i + 1]; ++k) {
+                if ((w.jview[k].kind & ~kIsB) == DIO_CONSTRAINT_BALL_SOCKET)
+                    ++nb;
+                else
+                    ++nl;
+            }
+        nb = nb > 3u ? 3u : nb;
+        nl = nl > 3u ? 3u : nl;
+        const uint32_t tag = w.shape[i].tag > 7u ? 7u : w.shape[i].tag;
+        keys[t] = ((3u - nb) << 5) | ((3u - nl) << 3) | tag;
+    }
+}
+
 // one JView per (body, joint) incidence in the body's joint-CSR order
 static __global__ void k_build_jview(const DioConstraint* joints, const uint32_t* joff, const uint32_t* jidx,
                                      uint32_t n, JView* out) {
@@ -413,6 +436,7 @@ class Engine final : public EngineBase {
         DIO_TRY(alloc(&joint_idx_, 2ull * J));
         DIO_TRY(alloc(&jview_, 2ull * J));
         DIO_TRY(alloc(&dyn_list_, N));
+        DIO_TRY(alloc(&dyn_tmp_, N));
         DIO_TRY(alloc(&color_hist_, kMaxColors + 2));
         const size_t CNT = std::max<size_t>(std::max<size_t>(N, (size_t)PP * per_cap_), 2ull * M) + 2;
         DIO_TRY(alloc(&counts_, CNT));
@@ -613,6 +637,7 @@ class Engine final : public EngineBase {
         uint32_t ninc = offsets[n];
         if (ninc > 2ull * cap_.max_contacts) return cap_err("too many CSR indices");
         if (ninc && !indices) return inval("null indices");
+        w_.n_joints = 0;  // this call's joints are uploaded below
         DIO_TRY(upload_state(state, n));
         // poses
         char* st = reinterpret_cast<char*>(dstage_);
@@ -683,6 +708,7 @@ class Engine final : public EngineBase {
         if (n && (!d->bodies || !d->state)) return inval("null bodies/state");
         drop_graphs();
         lbvh_valid_ = false;
+        w_.n_joints = 0;  // the world's joints are uploaded below
         DIO_TRY(upload_bodies(d->bodies, n));
         if (d->positions_f64 || d->orientations_f64) {
             double* dp = reinterpret_cast<double*>(dstage_);
@@ -938,6 +964,18 @@ class Engine final : public EngineBase {
         if (w_.n_dyn != nd) drop_graphs();  // launch shapes depend on it
         w_.n_dyn = nd;
         w_.dyn_list = dyn_list_;
+        return order_dyn_list();
+    }
+    // stable sort of the dynamic-body list by work signature (k_dyn_keys);
+    // index order is kept inside a signature
+    int order_dyn_list() {
+        const uint32_t nd = w_.n_dyn;
+        if (nd < 2) return DIO_OK;
+        k_dyn_keys<P, R><<<grid_for(nd, 256), 256, 0, stream_>>>(w_, dyn_list_, nd, counts2_);
+        size_t tb = cub_bytes_;
+        DIO_CK(cub::DeviceRadixSort::SortPairs(cub_tmp_, tb, counts2_, offsets2_, dyn_list_, dyn_tmp_, (int)nd, 0, 8,
+                                               stream_));
+        DIO_CK(cudaMemcpyAsync(dyn_list_, dyn_tmp_, (size_t)nd * 4, cudaMemcpyDeviceToDevice, stream_));
         return DIO_OK;
     }
     int single_scene(uint32_t n, const DioContainer* c) {
@@ -966,7 +1004,7 @@ class Engine final : public EngineBase {
         w_.n_joints = nj;
         if (!nj) {
             DIO_CK(cudaMemsetAsync(joint_off_, 0, ((size_t)n + 1) * 4, stream_));
-            return DIO_OK;
+            return order_dyn_list();
         }
         DIO_CK(cudaMemcpyAsync(joints_, cons, (size_t)nj * sizeof(DioConstraint), cudaMemcpyHostToDevice, stream_));
         uint32_t total = 2 * nj;
@@ -981,7 +1019,7 @@ class Engine final : public EngineBase {
         DIO_CK(cudaMemcpyAsync(joint_idx_, inc_row_s_, (size_t)total * 4, cudaMemcpyDeviceToDevice, stream_));
         k_build_jview<<<grid_for(n, 128), 128, 0, stream_>>>(joints_, joint_off_, joint_idx_, n, jview_);
         w_.jview = jview_;
-        return DIO_OK;
+        return order_dyn_list();
     }
     int sort_keys(const uint2* ab, uint32_t m, unsigned long long* keys_out, uint32_t* ids_out) {
         if (!m) return DIO_OK;
@@ -1590,6 +1628,7 @@ class Engine final : public EngineBase {
     uint32_t *joint_off_ = nullptr, *joint_idx_ = nullptr;
     JView* jview_ = nullptr;
     uint32_t* dyn_list_ = nullptr;
+    uint32_t* dyn_tmp_ = nullptr;
     uint32_t* color_hist_ = nullptr;
     uint32_t ncolors_ = 0;
     uint32_t color_off_h_[kMaxColors + 1] = {};

@@ -40,6 +40,27 @@ __device__ __forceinline__ void stamp(Block6<R>& B, V3<R> jl, V3<R> ja, R k, R f
     for (int i = 0; i < 6; ++i) B.g[i] = B.g[i] + J[i] * f;
 }
 
+// stamp() for a row whose Jacobian entries outside MASK are exact zeros
+// (a ball-socket axis row: J = (s e_k, r x s e_k)).  The H terms with a zero
+// factor are +-0 when J and k are finite, and adding +-0 leaves an H entry
+// unchanged because a round-to-nearest sum that starts at +0 (or at the
+// positive diagonal) is never -0; so skipping them is exact.  g takes all
+// six terms (its start values can be -0).  Callers check finiteness first.
+template <int MASK, class R>
+__device__ __forceinline__ void stamp_masked(Block6<R>& B, V3<R> jl, V3<R> ja, R k, R f) {
+    const R J[6] = {jl.x, jl.y, jl.z, ja.x, ja.y, ja.z};
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+        for (int j = 0; j <= i; ++j)
+            if (((MASK >> i) & 1) && ((MASK >> j) & 1)) B.h[tri(i, j)] = B.h[tri(i, j)] + J[i] * J[j] * k;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) B.g[i] = B.g[i] + J[i] * f;
+}
+constexpr int kMaskAxisX = (1 << 0) | (1 << 4) | (1 << 5);  // J = (s, 0, 0, 0, s r.z, -s r.y)
+constexpr int kMaskAxisY = (1 << 1) | (1 << 3) | (1 << 5);  // J = (0, s, 0, -s r.z, 0, s r.x)
+constexpr int kMaskAxisZ = (1 << 2) | (1 << 3) | (1 << 4);  // J = (0, 0, s, s r.y, -s r.x, 0)
+
 // solve6, avbd/src/lib.rs:107-180 (unpivoted LDL^T); solves H x = -g.
 template <class R>
 __device__ __forceinline__ void solve6(const Block6<R>& B, R x[6]) {
@@ -275,9 +296,15 @@ __device__ __forceinline__ void primal_jview_f(const JView& jv, const F& fetch, 
         V3<R> jx = scale(V3<R>{R(1), R(0), R(0)}, sign);
         V3<R> jy = scale(V3<R>{R(0), R(1), R(0)}, sign);
         V3<R> jz = scale(V3<R>{R(0), R(0), R(1)}, sign);
-        stamp(B, jx, cross(r_self, jx), stiff, delta.x * stiff);
-        stamp(B, jy, cross(r_self, jy), stiff, delta.y * stiff);
-        stamp(B, jz, cross(r_self, jz), stiff, delta.z * stiff);
+        if (finite_(stiff * (dabs(r_self.x) + dabs(r_self.y) + dabs(r_self.z)))) {
+            stamp_masked<kMaskAxisX>(B, jx, cross(r_self, jx), stiff, delta.x * stiff);
+            stamp_masked<kMaskAxisY>(B, jy, cross(r_self, jy), stiff, delta.y * stiff);
+            stamp_masked<kMaskAxisZ>(B, jz, cross(r_self, jz), stiff, delta.z * stiff);
+        } else {
+            stamp(B, jx, cross(r_self, jx), stiff, delta.x * stiff);
+            stamp(B, jy, cross(r_self, jy), stiff, delta.y * stiff);
+            stamp(B, jz, cross(r_self, jz), stiff, delta.z * stiff);
+        }
     } else {
         R len = length(delta);
         R target = R(jv.self_anchor.w);
