@@ -25,6 +25,7 @@ SPHERE, CUBE, TETRAHEDRON, BOX, HULL = 0, 1, 2, 3, 4
 CONTAINER = 0xFFFFFFFF
 SPRING, ROD, BALL_SOCKET, ROPE = 0, 1, 2, 3
 CONTACTS_PER_PAIR = 4
+PRIMAL_VARIANTS = 10  # DIO_PRIMAL_VARIANTS
 
 SOLVER_JACOBI, SOLVER_COLORED = 0, 1
 PREC_F32, PREC_SPLIT, PREC_F64 = 0, 1, 2

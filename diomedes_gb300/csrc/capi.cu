@@ -35,7 +35,7 @@ DioConfig default_config() {
     c.precision = DIO_PREC_F32;
     c.contacts_per_pair = DIO_CONTACTS_PER_PAIR;
     c.use_graph = 1;
-    c.primal_variant = 2;
+    c.primal_variant = 5;  // {64 threads, 10 CTAs/SM}: 96 registers, no spills
     c.block_size = 0;
     c.batched_solver = 0;
     return c;
@@ -360,7 +360,7 @@ int dio_autotune(DioCtx* ctx, const DioAvbdOptions* options, uint32_t trial_step
     // 1) primal launch shape at the default rebuild period
     double best_ms = 1e300;
     DioConfig best_cfg = cfg;
-    for (uint32_t var = 0; var < 10; ++var) {
+    for (uint32_t var = 0; var < DIO_PRIMAL_VARIANTS; ++var) {
         DioConfig c = cfg;
         c.primal_variant = var;
         double ms = 0.0;

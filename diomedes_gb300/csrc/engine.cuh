@@ -101,7 +101,7 @@ struct JView {
 template <class P, class R>
 struct DevWorld {
     uint32_t n;  // bodies
-    const uint32_t* dyn_list;  // dynamic bodies in index order
+    const uint32_t* dyn_list;  // dynamic bodies, ordered by work signature
     uint32_t n_dyn;
     const JView* jview;        // per-body joint views (joint CSR order)
     // poses

@@ -970,7 +970,7 @@ class Engine final : public EngineBase {
     // index order is kept inside a signature
     int order_dyn_list() {
         const uint32_t nd = w_.n_dyn;
-        if (nd < 2) return DIO_OK;
+        if (!nd) return DIO_OK;
         k_dyn_keys<P, R><<<grid_for(nd, 256), 256, 0, stream_>>>(w_, dyn_list_, nd, counts2_);
         size_t tb = cub_bytes_;
         DIO_CK(cub::DeviceRadixSort::SortPairs(cub_tmp_, tb, counts2_, offsets2_, dyn_list_, dyn_tmp_, (int)nd, 0, 8,

@@ -271,10 +271,11 @@ __device__ __forceinline__ void primal_joint(const DevWorld<P, R>& w, const DioC
 }
 
 // The same joint row from a JView: p_a - p_b is formed exactly as the
-// reference forms it (joint a's anchor point minus joint b's).
-template <class P, class R, class F>
-__device__ __forceinline__ void primal_jview_f(const JView& jv, const F& fetch, V3<P> sp, Q4<P> sq, Q4<R> sqr,
-                                               Block6<R>& B) {
+// reference forms it (joint a's anchor point minus joint b's).  `op4`/`oq4`
+// are the other body's snapshot pose, loaded by the caller.
+template <class P, class R>
+__device__ __forceinline__ void primal_jview_p(const JView& jv, A4<P> op4, A4<P> oq4, V3<P> sp, Q4<P> sq,
+                                               Q4<R> sqr, Block6<R>& B) {
     const bool is_a = !(jv.kind & kIsB);
     const uint32_t kind = jv.kind & ~kIsB;
     const V3<R> anc_s{R(jv.self_anchor.x), R(jv.self_anchor.y), R(jv.self_anchor.z)};
@@ -288,7 +289,7 @@ __device__ __forceinline__ void primal_jview_f(const JView& jv, const F& fetch, 
         p_self = add(sp, rotate(sq, cast3<P>(anc_s)));
         r_self = rotate(sqr, anc_s);
     }
-    const V3<P> p_other = add(xyz(fetch.pos(jv.other)), rotate(quat(fetch.rot(jv.other)), cast3<P>(anc_o)));
+    const V3<P> p_other = add(xyz(op4), rotate(quat(oq4), cast3<P>(anc_o)));
     const V3<R> delta = cast3<R>(is_a ? sub(p_self, p_other) : sub(p_other, p_self));
     const R sign = is_a ? R(1) : R(-1);
     const R stiff = R(jv.other_anchor.w);
@@ -318,10 +319,17 @@ __device__ __forceinline__ void primal_jview_f(const JView& jv, const F& fetch, 
     }
 }
 
-// avbd_primal for one body: reads buffer rd (through `fetch`), writes wr.
 template <class P, class R, class F>
-__device__ __forceinline__ void primal_body_f(const DevWorld<P, R>& w, uint32_t i, int wr, const SolveParams<R>& o,
-                                              const F& fetch) {
+__device__ __forceinline__ void primal_jview_f(const JView& jv, const F& fetch, V3<P> sp, Q4<P> sq, Q4<R> sqr,
+                                               Block6<R>& B) {
+    primal_jview_p<P, R>(jv, fetch.pos(jv.other), fetch.rot(jv.other), sp, sq, sqr, B);
+}
+
+// avbd_primal for one body: reads buffer rd (through `fetch`), writes wr.
+// [k0, k1) is the body's joint-view range.
+template <class P, class R, class F>
+__device__ __forceinline__ void primal_body_f(const DevWorld<P, R>& w, uint32_t i, uint32_t k0, uint32_t k1, int wr,
+                                              const SolveParams<R>& o, const F& fetch) {
     const A4<R> inv = w.inv[i];
     if (inv.w == R(0)) return;
     const V3<P> sp = xyz(fetch.pos(i));
@@ -362,12 +370,9 @@ __device__ __forceinline__ void primal_body_f(const DevWorld<P, R>& w, uint32_t 
     const R k_alpha = R(1) - o.alpha;
     const uint32_t j0 = w.row_off[i], j1 = w.row_off[i + 1];
     for (uint32_t j = j0; j < j1; ++j) primal_row_f(w, w.row_idx[j], w.row_oth[j], fetch, sqr, dqsl, dqsa, k_alpha, B);
-    if (w.n_joints) {
-        const uint32_t k0 = w.joint_off[i], k1 = w.joint_off[i + 1];
-        for (uint32_t k = k0; k < k1; ++k) {
-            const JView jv = w.jview[k];
-            primal_jview_f<P, R>(jv, fetch, sp, sq, sqr, B);
-        }
+    for (uint32_t k = k0; k < k1; ++k) {
+        const JView jv = w.jview[k];
+        primal_jview_f<P, R>(jv, fetch, sp, sq, sqr, B);
     }
     R dx[6];
     solve6(B, dx);
@@ -378,7 +383,8 @@ __device__ __forceinline__ void primal_body_f(const DevWorld<P, R>& w, uint32_t 
 template <class P, class R>
 __device__ __forceinline__ void primal_body(const DevWorld<P, R>& w, uint32_t i, int rd, int wr,
                                             const SolveParams<R>& o) {
-    primal_body_f(w, i, wr, o, GlobalFetch<P, R>{w, rd});
+    const uint32_t k0 = w.n_joints ? w.joint_off[i] : 0u, k1 = w.n_joints ? w.joint_off[i + 1] : 0u;
+    primal_body_f(w, i, k0, k1, wr, o, GlobalFetch<P, R>{w, rd});
 }
 
 // Tile variant: the CTA's T consecutive bodies stage their snapshot and
@@ -397,7 +403,10 @@ __global__ void __launch_bounds__(T, MINB) k_primal_tile(DevWorld<P, R> w, int r
         s_irot[threadIdx.x] = w.init_rot[i];
     }
     __syncthreads();
-    if (i < w.n) primal_body_f(w, i, wr, o, TileFetch<P, R, T>{w, rd, lo, s_pos, s_rot, s_ipos, s_irot});
+    if (i < w.n) {
+        const uint32_t k0 = w.n_joints ? w.joint_off[i] : 0u, k1 = w.n_joints ? w.joint_off[i + 1] : 0u;
+        primal_body_f(w, i, k0, k1, wr, o, TileFetch<P, R, T>{w, rd, lo, s_pos, s_rot, s_ipos, s_irot});
+    }
 }
 
 // One thread per dynamic body (static bodies are never solved,
@@ -410,9 +419,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_primal(DevWorld<P, R> w, int rd
         primal_body(w, w.dyn_list[t], rd, wr, o);
 }
 
-// launch-shape variants: 0-5 k_primal over the dynamic-body list with
-// {threads per CTA, min CTAs per SM}; 6-9 k_primal_tile over body tiles
-constexpr int kPrimalVariants = 10;
+// variants: 0-5 k_primal over the dynamic-body list with {threads per CTA,
+// min CTAs per SM}; 6-9 k_primal_tile over body tiles
+constexpr int kPrimalVariants = DIO_PRIMAL_VARIANTS;
 constexpr int kPrimalShape[kPrimalVariants][2] = {{128, 4}, {128, 5}, {128, 6}, {256, 2}, {256, 3},
                                                   {64, 10}, {128, 5}, {128, 6}, {256, 3}, {64, 10}};
 

@@ -206,12 +206,17 @@ enum DioPrecision {
     DIO_PREC_F64 = 2    /* everything in FP64 (the all-FP64 GPU oracle run) */
 };
 
+/* number of primal kernel variants selectable by DioConfig.primal_variant */
+#define DIO_PRIMAL_VARIANTS 10
+
 typedef struct DioConfig {
     uint32_t solver_mode;       /* DioSolverMode                          */
     uint32_t precision;         /* DioPrecision (fixed at world upload)   */
     uint32_t contacts_per_pair; /* 4 (reference) or 8 (extended manifold) */
     uint32_t use_graph;         /* replay each step as a CUDA graph       */
-    uint32_t primal_variant;    /* primal launch shape 0..5 (autotuned)   */
+    uint32_t primal_variant;    /* primal kernel variant, 0 .. DIO_PRIMAL_VARIANTS-1
+                                   (launch shape, body tiles; every variant
+                                   computes the same bits; autotuned)     */
     uint32_t block_size;        /* reserved (0)                           */
     uint32_t batched_solver;    /* 1: one CTA-per-scene persistent solve  */
     uint32_t profile;           /* time primal / dual launches with events */

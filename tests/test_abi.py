@@ -67,3 +67,14 @@ def test_default_options_match_avbd_options_default():
     o = ph.avbd_options()
     assert (o.iterations, round(o.alpha, 6), o.beta_lin, round(o.margin, 6), o.penalty_min) == (10, 0.99, 1e4, 0.01, 1.0)
     assert list(o.gravity) == [0.0, -10.0, 0.0]
+
+
+def test_header_constants_match_the_python_mirror():
+    with open(os.path.join(ROOT, "include", "dio_cuda.h")) as f:
+        text = f.read()
+    m = re.search(r"#define DIO_PRIMAL_VARIANTS (\d+)", text)
+    assert m and int(m.group(1)) == abi.PRIMAL_VARIANTS
+    for name in ("DIO_OK", "DIO_ERR_INVALID", "DIO_ERR_CAPACITY", "DIO_ERR_TIMEOUT", "DIO_ERR_CUDA",
+                 "DIO_ERR_NONFINITE", "DIO_ERR_STATE"):
+        m = re.search(name + r"\s*=\s*(\d+)", text)
+        assert m and int(m.group(1)) == getattr(abi, name), name

@@ -278,6 +278,20 @@ def test_hull_pairs_with_staged_vertices_match_oracle():
     assert np.array_equal(_bits(got), _bits(ref))
 
 
+@pytest.mark.parametrize("variant", range(abi.PRIMAL_VARIANTS))
+def test_every_primal_variant_matches_oracle(variant):
+    """Launch shapes, tiles, per-position records and paired joint loads all
+    compute the oracle's bits (joints of every kind, contacts, ground)."""
+    sc = scenes.pack([scenes.box_demo(), scenes.constraints_demo(), scenes.pyramid(levels=4)])
+    ow = O.World(sc)
+    ow.step(sc.options, 8)
+    with _world(sc, primal_variant=variant) as w:
+        w.step(sc.options, 8)
+        gb, gs = w.download()
+    rb, rs = ow.download()
+    assert np.array_equal(_bits(gb), _bits(rb)) and np.array_equal(_bits(gs), _bits(rs))
+
+
 def test_autotune_keeps_state_and_results(tmp_path):
     """Every tuned variant computes the same bits, and the trials run from a
     snapshot that is restored: stepping after tuning still matches the
@@ -293,7 +307,7 @@ def test_autotune_keeps_state_and_results(tmp_path):
         after = w.download()
         assert np.array_equal(_bits(before[0]), _bits(after[0]))
         assert np.array_equal(_bits(before[1]), _bits(after[1]))
-        assert 0 <= cfg["primal_variant"] < 10 and cfg["bvh_rebuild_period"] >= 1
+        assert 0 <= cfg["primal_variant"] < abi.PRIMAL_VARIANTS and cfg["bvh_rebuild_period"] >= 1
         cfg2 = w.autotune(sc.options, trial_steps=2, cache_path=cache)
         assert (cfg2["primal_variant"], cfg2["bvh_rebuild_period"]) == (cfg["primal_variant"],
                                                                         cfg["bvh_rebuild_period"])
