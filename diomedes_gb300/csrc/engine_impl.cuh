@@ -444,6 +444,7 @@ class Engine final : public EngineBase {
         DIO_TRY(alloc(&counts2_, (size_t)N + 2));
         DIO_TRY(alloc(&offsets2_, (size_t)N + 2));
         DIO_TRY(alloc(&scenes_, S));
+        DIO_TRY(alloc(&chunks_, S));
         DIO_TRY(alloc(&hull_, H));
         DIO_TRY(alloc(&ctr_, 1));
         DIO_CK(cudaMallocHost(&hctr_, sizeof(Counters)));
@@ -483,6 +484,45 @@ class Engine final : public EngineBase {
         int dev = 0;
         DIO_CK(cudaGetDevice(&dev));
         DIO_CK(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev));
+        const int tree_bytes = (int)scene_tree_bytes<R>(scene_tree_cap<R>());
+        DIO_CK(cudaFuncSetAttribute(k_scene_tree<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, tree_bytes));
+        DIO_CK(cudaFuncSetAttribute(k_scene_tree<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tree_bytes));
+        return DIO_OK;
+    }
+    // largest scene, and the chunks of consecutive scenes (each of at most
+    // scene_tree_cap bodies, packed up to that many) for k_scene_tree
+    int note_scene_sizes() {
+        const uint32_t cap = scene_tree_cap<R>();
+        scene_max_ = 0;
+        chunk_max_ = 0;
+        chunks_host_.clear();
+        uint32_t open_bodies = 0;
+        bool open = false;
+        auto close = [&](uint32_t end) {
+            if (!open) return;
+            chunks_host_.back().y = end;
+            chunk_max_ = std::max(chunk_max_, open_bodies);
+            open = false;
+        };
+        for (uint32_t s = 0; s < (uint32_t)scenes_host_.size(); ++s) {
+            const uint32_t sz = scenes_host_[s].body_hi - scenes_host_[s].body_lo;
+            scene_max_ = std::max(scene_max_, sz);
+            if (sz > cap) {
+                close(s);
+                continue;
+            }
+            if (open && open_bodies + sz > cap) close(s);
+            if (!open) {
+                chunks_host_.push_back(make_uint2(s, s));
+                open_bodies = 0;
+                open = true;
+            }
+            open_bodies += sz;
+        }
+        close((uint32_t)scenes_host_.size());
+        if (!chunks_host_.empty())
+            DIO_CK(cudaMemcpyAsync(chunks_, chunks_host_.data(), chunks_host_.size() * sizeof(uint2),
+                                   cudaMemcpyHostToDevice, stream_));
         return DIO_OK;
     }
 
@@ -742,6 +782,7 @@ class Engine final : public EngineBase {
             }
         }
         scenes_host_ = sc;
+        DIO_TRY(note_scene_sizes());
         DIO_CK(cudaMemcpyAsync(scenes_, sc.data(), ns * sizeof(SceneDesc), cudaMemcpyHostToDevice, stream_));
         DIO_CK(cudaMemcpyAsync(origin_, org.data(), ns * sizeof(A4<P>), cudaMemcpyHostToDevice, stream_));
         w_.origin = cfg_.precision == DIO_PREC_SPLIT ? origin_ : nullptr;
@@ -997,6 +1038,7 @@ class Engine final : public EngineBase {
         w_.n = n;
         // the API path is single-scene FP32; keep host scene table in sync
         scenes_host_.assign(1, x);
+        DIO_TRY(note_scene_sizes());
         DIO_CK(cudaStreamSynchronize(stream_));
         return DIO_OK;
     }
@@ -1090,27 +1132,58 @@ class Engine final : public EngineBase {
     // Refit the current tree to this step's AABBs and traverse it.  Any
     // valid tree over the scene's leaves yields the exact overlap set, so
     // the topology is rebuilt only every bvh_rebuild_period steps.
+    // Scenes of at most scene_tree_cap bodies are refitted and traversed by
+    // k_scene_tree (one CTA per chunk of scenes, trees in shared memory),
+    // larger ones by the global k_refit / k_traverse.
     int run_lbvh_refit(uint32_t n, int g) {
-        DIO_CK(cudaMemsetAsync(lb_visits_, 0, (size_t)n * 4, stream_));
-        k_refit<R><<<g, 256, 0, stream_>>>(w_.aabb_min, w_.aabb_max, lb_leaf_, scenes_, w_.scene, n, lb_children_,
-                                           lb_parent_, lb_leaf_min_, lb_leaf_max_, lb_node_min_, lb_node_max_,
-                                           lb_visits_);
+        const uint32_t cap = scene_tree_cap<R>();
+        const uint32_t nchunks = (uint32_t)chunks_host_.size();
+        const uint32_t tcap = std::max(2u, chunk_max_);
+        const size_t tbytes = scene_tree_bytes<R>(tcap);
+        const bool global_path = scene_max_ > cap;
+        const uint32_t tcap_skip = cap;
+        auto scene_tree = [&](bool write) {
+            if (!nchunks) return;
+            if (write)
+                k_scene_tree<R, true><<<nchunks, kSceneTreeThreads, tbytes, stream_>>>(
+                    w_.aabb_min, w_.aabb_max, lb_leaf_, scenes_, w_.scene, chunks_, n, tcap, lb_children_,
+                    lb_parent_, lb_leaf_min_, lb_leaf_max_, lb_node_min_, lb_node_max_, counts_, offsets_, lb_pb_,
+                    w_.max_pairs, &ctr_->error_flags);
+            else
+                k_scene_tree<R, false><<<nchunks, kSceneTreeThreads, tbytes, stream_>>>(
+                    w_.aabb_min, w_.aabb_max, lb_leaf_, scenes_, w_.scene, chunks_, n, tcap, lb_children_,
+                    lb_parent_, lb_leaf_min_, lb_leaf_max_, lb_node_min_, lb_node_max_, counts_, offsets_, lb_pb_,
+                    w_.max_pairs, &ctr_->error_flags);
+            ++launches_;
+        };
         int gt = grid_for(n, 128);
-        k_traverse<R><<<gt, 128, 0, stream_>>>(lb_leaf_, scenes_, w_.scene, n, lb_children_, lb_leaf_min_,
-                                               lb_leaf_max_, lb_node_min_, lb_node_max_, counts_, offsets_, lb_pb_,
-                                               w_.max_pairs, false, &ctr_->error_flags);
+        scene_tree(false);
+        if (global_path) {
+            DIO_CK(cudaMemsetAsync(lb_visits_, 0, (size_t)n * 4, stream_));
+            k_refit<R><<<g, 256, 0, stream_>>>(w_.aabb_min, w_.aabb_max, lb_leaf_, scenes_, w_.scene, n,
+                                               lb_children_, lb_parent_, lb_leaf_min_, lb_leaf_max_, lb_node_min_,
+                                               lb_node_max_, lb_visits_, tcap_skip);
+            k_traverse<R><<<gt, 128, 0, stream_>>>(lb_leaf_, scenes_, w_.scene, n, lb_children_, lb_leaf_min_,
+                                                   lb_leaf_max_, lb_node_min_, lb_node_max_, counts_, offsets_,
+                                                   lb_pb_, w_.max_pairs, false, &ctr_->error_flags, tcap_skip);
+            launches_ += 2;
+        }
         DIO_CK(cudaMemsetAsync(counts_ + n, 0, 4, stream_));
         size_t tb = cub_bytes_;
         DIO_CK(cub::DeviceScan::ExclusiveSum(cub_tmp_, tb, counts_, offsets_, (int)n + 1, stream_));
-        k_traverse<R><<<gt, 128, 0, stream_>>>(lb_leaf_, scenes_, w_.scene, n, lb_children_, lb_leaf_min_,
-                                               lb_leaf_max_, lb_node_min_, lb_node_max_, counts_, offsets_, lb_pb_,
-                                               w_.max_pairs, true, &ctr_->error_flags);
+        scene_tree(true);
+        if (global_path) {
+            k_traverse<R><<<gt, 128, 0, stream_>>>(lb_leaf_, scenes_, w_.scene, n, lb_children_, lb_leaf_min_,
+                                                   lb_leaf_max_, lb_node_min_, lb_node_max_, counts_, offsets_,
+                                                   lb_pb_, w_.max_pairs, true, &ctr_->error_flags, tcap_skip);
+            ++launches_;
+        }
         k_pairs_total<<<1, 1, 0, stream_>>>(ctr_, offsets_ + n, w_.max_pairs);
         DIO_CK(cudaMemsetAsync(lb_long_count_, 0, 4, stream_));
         k_sort_segments<<<g, 256, 0, stream_>>>(offsets_, n, w_.max_pairs, lb_pb_, lb_long_, lb_long_count_);
         k_sort_long<<<sms_, 512, 0, stream_>>>(offsets_, lb_pb_, lb_long_, lb_long_count_, &ctr_->error_flags);
         k_pairs_from_segments<<<g, 256, 0, stream_>>>(offsets_, n, lb_pb_, w_.pairs, w_.max_pairs);
-        launches_ += 8;
+        launches_ += 5;
         return DIO_OK;
     }
 
@@ -1635,6 +1708,10 @@ class Engine final : public EngineBase {
     uint32_t *counts_ = nullptr, *offsets_ = nullptr, *counts2_ = nullptr, *offsets2_ = nullptr;
     SceneDesc* scenes_ = nullptr;
     std::vector<SceneDesc> scenes_host_;
+    uint32_t scene_max_ = 0;  // bodies in the largest scene
+    uint32_t chunk_max_ = 0;  // bodies in the largest scene chunk
+    std::vector<uint2> chunks_host_;
+    uint2* chunks_ = nullptr;
     A4<P>* origin_ = nullptr;
     A4<R>* hull_ = nullptr;
     Counters* ctr_ = nullptr;

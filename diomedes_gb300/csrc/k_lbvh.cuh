@@ -168,12 +168,14 @@ static __global__ void k_karras(const uint32_t* keys, const SceneDesc* scenes, c
 template <class R>
 __global__ void k_refit(const A4<R>* mn, const A4<R>* mx, const uint32_t* leaf_body, const SceneDesc* scenes,
                         const uint32_t* scene_of_pos, uint32_t n, const uint2* children, const uint32_t* parent,
-                        A4<R>* leaf_min, A4<R>* leaf_max, A4<R>* node_min, A4<R>* node_max, uint32_t* visits) {
+                        A4<R>* leaf_min, A4<R>* leaf_max, A4<R>* node_min, A4<R>* node_max, uint32_t* visits,
+                        uint32_t skip_max) {
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        const SceneDesc sc = scenes[scene_of_pos[p]];
+        if (sc.body_hi - sc.body_lo <= skip_max) continue;  // k_scene_tree's scene
         uint32_t b = leaf_body[p];
         leaf_min[p] = mn[b];
         leaf_max[p] = mx[b];
-        const SceneDesc sc = scenes[scene_of_pos[p]];
         if (sc.body_hi - sc.body_lo < 2) continue;
         __threadfence();
         uint32_t node = parent[n + p];
@@ -207,10 +209,11 @@ __global__ void __launch_bounds__(128) k_traverse(const uint32_t* leaf_body, con
                                                   const A4<R>* leaf_min, const A4<R>* leaf_max,
                                                   const A4<R>* node_min, const A4<R>* node_max, uint32_t* counts,
                                                   const uint32_t* offsets, uint32_t* pb, uint32_t cap, bool write_out,
-                                                  uint32_t* err) {
+                                                  uint32_t* err, uint32_t skip_max) {
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
-        const uint32_t i = leaf_body[p];
         const SceneDesc sc = scenes[scene_of_pos[p]];
+        if (sc.body_hi - sc.body_lo <= skip_max) continue;  // k_scene_tree's scene
+        const uint32_t i = leaf_body[p];
         uint32_t found = 0;
         uint32_t out = write_out ? offsets[i] : 0;
         if (sc.body_hi - sc.body_lo >= 2) {
@@ -258,6 +261,167 @@ __global__ void __launch_bounds__(128) k_traverse(const uint32_t* leaf_body, con
             }
         }
         if (!write_out) counts[i] = found;
+    }
+}
+
+// ---- one CTA per chunk of scenes, trees in shared memory ----
+// Consecutive scenes of at most scene_tree_cap<R>() bodies are packed into
+// chunks of at most that many bodies; one CTA stages its chunk's trees (leaf
+// and node boxes, children, parents) in shared memory, refits them with
+// shared-memory atomics and traverses them without touching global memory.
+// The count pass refits and counts; the write pass reloads the refitted boxes
+// and emits partners at the scanned offsets.  Partner sets are those of the
+// global kernels above (same trees, same test); their order does not matter
+// because each body's list is sorted afterwards.
+template <class R>
+__host__ __device__ constexpr uint32_t scene_tree_cap() { return sizeof(R) == 4 ? 2048u : 1024u; }
+template <class R>
+__host__ __device__ constexpr size_t scene_tree_bytes(uint32_t cap) {
+    // leaf min/max, node min/max, children, leaf parent, node parent, visit
+    // flag, leaf body, leaf's scene root
+    return (size_t)cap * (4 * sizeof(A4<R>) + sizeof(uint2) + 5 * sizeof(uint32_t));
+}
+constexpr int kSceneTreeThreads = 1024;
+constexpr uint32_t kNoRoot = 0xFFFFFFFFu;
+
+template <class R, bool WRITE>
+__global__ void __launch_bounds__(kSceneTreeThreads)
+    k_scene_tree(const A4<R>* aabb_min, const A4<R>* aabb_max, const uint32_t* leaf_body, const SceneDesc* scenes,
+                 const uint32_t* scene_of_pos, const uint2* chunks, uint32_t n, uint32_t cap_bodies,
+                 const uint2* children, const uint32_t* parent, A4<R>* g_leaf_min, A4<R>* g_leaf_max,
+                 A4<R>* g_node_min, A4<R>* g_node_max, uint32_t* counts, const uint32_t* offsets, uint32_t* pb,
+                 uint32_t cap, uint32_t* err) {
+    extern __shared__ __align__(16) unsigned char tree_smem[];
+    const uint2 chunk = chunks[blockIdx.x];  // scenes [x, y)
+    const uint32_t lo = scenes[chunk.x].body_lo;
+    const uint32_t nb = scenes[chunk.y - 1].body_hi - lo;
+    if (nb > cap_bodies) {  // the host packs chunks within the cap
+        if (threadIdx.x == 0) atomicOr(err, kErrIndexOverflow);
+        return;
+    }
+    A4<R>* lmn = reinterpret_cast<A4<R>*>(tree_smem);
+    A4<R>* lmx = lmn + cap_bodies;
+    A4<R>* nmn = lmx + cap_bodies;
+    A4<R>* nmx = nmn + cap_bodies;
+    uint2* ch = reinterpret_cast<uint2*>(nmx + cap_bodies);
+    uint32_t* lpar = reinterpret_cast<uint32_t*>(ch + cap_bodies);
+    uint32_t* npar = lpar + cap_bodies;
+    uint32_t* vis = npar + cap_bodies;
+    uint32_t* lbody = vis + cap_bodies;
+    uint32_t* lroot = lbody + cap_bodies;
+    const uint32_t tid = threadIdx.x, nt = blockDim.x;
+    // slot p is leaf p of its scene and, except for a scene's last slot,
+    // internal node (p - scene start) of that scene
+    for (uint32_t p = tid; p < nb; p += nt) {
+        const SceneDesc sc = scenes[scene_of_pos[lo + p]];
+        const uint32_t root = sc.body_lo - lo, ns = sc.body_hi - sc.body_lo;
+        const uint32_t b = leaf_body[lo + p];
+        lbody[p] = b;
+        lroot[p] = ns >= 2 ? root : kNoRoot;
+        if (WRITE) {
+            lmn[p] = g_leaf_min[lo + p];
+            lmx[p] = g_leaf_max[lo + p];
+        } else {
+            const A4<R> a = aabb_min[b], c = aabb_max[b];
+            lmn[p] = a;
+            lmx[p] = c;
+            g_leaf_min[lo + p] = a;
+            g_leaf_max[lo + p] = c;
+            lpar[p] = ns >= 2 ? parent[n + lo + p] - lo : 0u;
+        }
+        if (lo + p + 1 < sc.body_hi) {  // internal node
+            const uint2 c = children[lo + p];
+            ch[p] = make_uint2((c.x & kLeafFlag) ? (((c.x & ~kLeafFlag) - lo) | kLeafFlag) : c.x - lo,
+                               (c.y & kLeafFlag) ? (((c.y & ~kLeafFlag) - lo) | kLeafFlag) : c.y - lo);
+            if (WRITE) {
+                nmn[p] = g_node_min[lo + p];
+                nmx[p] = g_node_max[lo + p];
+            } else {
+                npar[p] = p == root ? p : parent[lo + p] - lo;
+                vis[p] = 0u;
+            }
+        }
+    }
+    __syncthreads();
+    if (!WRITE) {
+        // bottom-up unions: the second arrival at a node computes it
+        for (uint32_t p = tid; p < nb; p += nt) {
+            const uint32_t root = lroot[p];
+            if (root == kNoRoot) continue;
+            uint32_t node = lpar[p];
+            for (uint32_t depth = 0; depth < nb; ++depth) {  // a path has < nb nodes
+                __threadfence_block();
+                if (atomicAdd(&vis[node], 1u) == 0) break;
+                __threadfence_block();
+                const uint2 c = ch[node];
+                const uint32_t li = c.x & ~kLeafFlag, ri = c.y & ~kLeafFlag;
+                const A4<R> a0 = (c.x & kLeafFlag) ? lmn[li] : nmn[li], a1 = (c.x & kLeafFlag) ? lmx[li] : nmx[li];
+                const A4<R> b0 = (c.y & kLeafFlag) ? lmn[ri] : nmn[ri], b1 = (c.y & kLeafFlag) ? lmx[ri] : nmx[ri];
+                nmn[node] = A4<R>{fmin_(a0.x, b0.x), fmin_(a0.y, b0.y), fmin_(a0.z, b0.z), R(0)};
+                nmx[node] = A4<R>{fmax_(a1.x, b1.x), fmax_(a1.y, b1.y), fmax_(a1.z, b1.z), R(0)};
+                if (node == root) break;
+                node = npar[node];
+            }
+        }
+        __syncthreads();
+        for (uint32_t p = tid; p < nb; p += nt)
+            if (lroot[p] != kNoRoot && lo + p + 1 < scenes[scene_of_pos[lo + p]].body_hi) {
+                g_node_min[lo + p] = nmn[p];
+                g_node_max[lo + p] = nmx[p];
+            }
+    }
+    for (uint32_t p = tid; p < nb; p += nt) {
+        const uint32_t i = lbody[p];
+        const uint32_t root = lroot[p];
+        if (root == kNoRoot) {
+            if (!WRITE) counts[i] = 0u;
+            continue;
+        }
+        const A4<R> qmn = lmn[p], qmx = lmx[p];
+        uint32_t found = 0;
+        uint32_t out = WRITE ? offsets[i] : 0u;
+        uint32_t stack[kStack];
+        int sp = 0;
+        uint32_t node = root;
+        while (true) {
+            const uint2 c = ch[node];
+            const uint32_t cc[2] = {c.x, c.y};
+            uint32_t next[2];
+            uint32_t push = 0;
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const uint32_t x = cc[k];
+                const uint32_t idx = x & ~kLeafFlag;
+                if (x & kLeafFlag) {
+                    if (overlap(qmn, qmx, lmn[idx], lmx[idx])) {
+                        const uint32_t j = lbody[idx];
+                        if (j > i) {
+                            if (WRITE) {
+                                if (out < cap) pb[out] = j;
+                                ++out;
+                            } else {
+                                ++found;
+                            }
+                        }
+                    }
+                } else if (overlap(qmn, qmx, nmn[idx], nmx[idx])) {
+                    next[push++] = idx;
+                }
+            }
+            if (push == 0) {
+                if (sp == 0) break;
+                node = stack[--sp];
+            } else {
+                node = next[0];
+                if (push == 2) {
+                    if (sp < kStack)
+                        stack[sp++] = next[1];
+                    else
+                        atomicOr(err, kErrIndexOverflow);
+                }
+            }
+        }
+        if (!WRITE) counts[i] = found;
     }
 }
 

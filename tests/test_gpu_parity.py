@@ -235,6 +235,28 @@ def test_lbvh_and_dense_pair_sets_at_scale(broad_phase):
         assert np.array_equal(got, ref), sc.name
 
 
+def test_world_with_large_and_small_scenes_matches_oracle():
+    """Scenes up to the shared-memory tree size are refitted and traversed by
+    one CTA each, larger ones by the global kernels; a world holding both
+    (2304-body cube field between small scenes, LBVH rebuilt every 2 steps)
+    still steps to the oracle's bits."""
+    parts = [scenes.pyramid(levels=3), scenes.cube_field(nx=16, nz=16, ny=9), scenes.box_demo()]
+    for p in parts:
+        p.options = parts[0].options
+    packed = scenes.pack(parts)
+    ow = O.World(packed)
+    ow.step(packed.options, 6)
+    with _world(packed, bvh_rebuild_period=2) as w:
+        w.step(packed.options, 6)
+        gb, gs = w.download()
+        gc = w.contacts()
+        st = w.stats()
+    rb, rs = ow.download()
+    assert st["error_flags"] == 0 and st["pairs"] > 1000
+    assert np.array_equal(_bits(gb), _bits(rb)) and np.array_equal(_bits(gs), _bits(rs))
+    assert np.array_equal(_bits(gc), _bits(ow.contacts()))
+
+
 @pytest.mark.parametrize("use_graph", [0, 1])
 def test_profiled_world_times_every_primal_launch(use_graph):
     sc = scenes.box_demo()

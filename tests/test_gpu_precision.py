@@ -26,8 +26,9 @@ def _world(sc, **cfg):
 
 @pytest.mark.parametrize("precision", [abi.PREC_SPLIT, abi.PREC_F64])
 def test_precision_world_matches_same_precision_oracle(precision):
+    # the 1080-body field is above the FP64 shared-memory tree size (1024)
     for sc in [scenes.pyramid(levels=4), scenes.box_demo(), scenes.constraints_demo(),
-               scenes.mixed_pile(n=400, extent=5.0)]:
+               scenes.mixed_pile(n=400, extent=5.0), scenes.cube_field(nx=12, nz=10, ny=9)]:
         ow = O.World(sc, precision=precision)
         ow.step(sc.options, 20)
         rp, rq = ow.download_f64()
