@@ -445,6 +445,11 @@ class Engine final : public EngineBase {
         DIO_TRY(alloc(&offsets2_, (size_t)N + 2));
         DIO_TRY(alloc(&scenes_, S));
         DIO_TRY(alloc(&chunks_, S));
+        DIO_TRY(alloc(&chunk_n_, S));
+        DIO_TRY(alloc(&chunk_ovf_, S));
+        // pair scratch of the shared-memory trees: scratch_k_ slots per body
+        scratch_k_ = (uint32_t)std::min<uint64_t>(8, std::max<uint64_t>(2, 2 * ((uint64_t)PP + N - 1) / N));
+        DIO_TRY(alloc(&tree_scratch_, (size_t)N * scratch_k_));
         DIO_TRY(alloc(&hull_, H));
         DIO_TRY(alloc(&ctr_, 1));
         DIO_CK(cudaMallocHost(&hctr_, sizeof(Counters)));
@@ -1142,18 +1147,32 @@ class Engine final : public EngineBase {
         const size_t tbytes = scene_tree_bytes<R>(tcap);
         const bool global_path = scene_max_ > cap;
         const uint32_t tcap_skip = cap;
+        TreeArgs ta;
+        ta.leaf_body = lb_leaf_;
+        ta.scenes = scenes_;
+        ta.scene_of_pos = w_.scene;
+        ta.chunks = chunks_;
+        ta.n = n;
+        ta.cap_bodies = tcap;
+        ta.children = lb_children_;
+        ta.parent = lb_parent_;
+        ta.counts = counts_;
+        ta.offsets = offsets_;
+        ta.pb = lb_pb_;
+        ta.cap = w_.max_pairs;
+        ta.scratch = tree_scratch_;
+        ta.scratch_k = scratch_k_;
+        ta.chunk_n = chunk_n_;
+        ta.chunk_ovf = chunk_ovf_;
+        ta.err = &ctr_->error_flags;
         auto scene_tree = [&](bool write) {
             if (!nchunks) return;
             if (write)
                 k_scene_tree<R, true><<<nchunks, kSceneTreeThreads, tbytes, stream_>>>(
-                    w_.aabb_min, w_.aabb_max, lb_leaf_, scenes_, w_.scene, chunks_, n, tcap, lb_children_,
-                    lb_parent_, lb_leaf_min_, lb_leaf_max_, lb_node_min_, lb_node_max_, counts_, offsets_, lb_pb_,
-                    w_.max_pairs, &ctr_->error_flags);
+                    w_.aabb_min, w_.aabb_max, lb_leaf_min_, lb_leaf_max_, lb_node_min_, lb_node_max_, ta);
             else
                 k_scene_tree<R, false><<<nchunks, kSceneTreeThreads, tbytes, stream_>>>(
-                    w_.aabb_min, w_.aabb_max, lb_leaf_, scenes_, w_.scene, chunks_, n, tcap, lb_children_,
-                    lb_parent_, lb_leaf_min_, lb_leaf_max_, lb_node_min_, lb_node_max_, counts_, offsets_, lb_pb_,
-                    w_.max_pairs, &ctr_->error_flags);
+                    w_.aabb_min, w_.aabb_max, lb_leaf_min_, lb_leaf_max_, lb_node_min_, lb_node_max_, ta);
             ++launches_;
         };
         int gt = grid_for(n, 128);
@@ -1712,6 +1731,10 @@ class Engine final : public EngineBase {
     uint32_t chunk_max_ = 0;  // bodies in the largest scene chunk
     std::vector<uint2> chunks_host_;
     uint2* chunks_ = nullptr;
+    uint32_t* chunk_n_ = nullptr;
+    uint32_t* chunk_ovf_ = nullptr;
+    uint2* tree_scratch_ = nullptr;
+    uint32_t scratch_k_ = 2;
     A4<P>* origin_ = nullptr;
     A4<R>* hull_ = nullptr;
     Counters* ctr_ = nullptr;

@@ -266,56 +266,99 @@ __global__ void __launch_bounds__(128) k_traverse(const uint32_t* leaf_body, con
 
 // ---- one CTA per chunk of scenes, trees in shared memory ----
 // Consecutive scenes of at most scene_tree_cap<R>() bodies are packed into
-// chunks of at most that many bodies; one CTA stages its chunk's trees (leaf
-// and node boxes, children, parents) in shared memory, refits them with
-// shared-memory atomics and traverses them without touching global memory.
-// The count pass refits and counts; the write pass reloads the refitted boxes
-// and emits partners at the scanned offsets.  Partner sets are those of the
-// global kernels above (same trees, same test); their order does not matter
-// because each body's list is sorted afterwards.
+// chunks of at most that many bodies (a chunk's bodies and sorted positions
+// are both the index range [lo, hi)).  One CTA stages its chunk's trees (leaf
+// and node boxes, children, parents) in shared memory.
+//   count pass  refit with shared-memory atomics (also each node's highest
+//               leaf position), then traverse: the leaf at position p visits
+//               only subtrees holding positions > p, so each overlapping pair
+//               is found once, by its lower position; it is counted for body
+//               a = min(i, j) and appended as (a, b) to the chunk's scratch
+//               region (scratch_k slots per body of the chunk)
+//   write pass  places the scratch pairs at the scanned per-body offsets; a
+//               chunk whose scratch overflowed is traversed again and written
+//               directly (body i's partners j > i)
+// Per-body partner sets equal those of the global kernels (same trees, same
+// test); the order inside a body's segment does not matter because each
+// segment is sorted afterwards.
 template <class R>
 __host__ __device__ constexpr uint32_t scene_tree_cap() { return sizeof(R) == 4 ? 2048u : 1024u; }
 template <class R>
 __host__ __device__ constexpr size_t scene_tree_bytes(uint32_t cap) {
     // leaf min/max, node min/max, children, leaf parent, node parent, visit
-    // flag, leaf body, leaf's scene root
-    return (size_t)cap * (4 * sizeof(A4<R>) + sizeof(uint2) + 5 * sizeof(uint32_t));
+    // flag (then per-body count), leaf body, leaf's scene root, node's
+    // highest leaf position
+    return (size_t)cap * (4 * sizeof(A4<R>) + sizeof(uint2) + 6 * sizeof(uint32_t)) + 16;
 }
 constexpr int kSceneTreeThreads = 1024;
 constexpr uint32_t kNoRoot = 0xFFFFFFFFu;
 
+struct TreeArgs {
+    const uint32_t* leaf_body;
+    const SceneDesc* scenes;
+    const uint32_t* scene_of_pos;
+    const uint2* chunks;
+    uint32_t n;
+    uint32_t cap_bodies;
+    const uint2* children;
+    const uint32_t* parent;
+    uint32_t* counts;
+    const uint32_t* offsets;
+    uint32_t* pb;
+    uint32_t cap;
+    uint2* scratch;
+    uint32_t scratch_k;
+    uint32_t* chunk_n;
+    uint32_t* chunk_ovf;
+    uint32_t* err;
+};
+
 template <class R, bool WRITE>
 __global__ void __launch_bounds__(kSceneTreeThreads)
-    k_scene_tree(const A4<R>* aabb_min, const A4<R>* aabb_max, const uint32_t* leaf_body, const SceneDesc* scenes,
-                 const uint32_t* scene_of_pos, const uint2* chunks, uint32_t n, uint32_t cap_bodies,
-                 const uint2* children, const uint32_t* parent, A4<R>* g_leaf_min, A4<R>* g_leaf_max,
-                 A4<R>* g_node_min, A4<R>* g_node_max, uint32_t* counts, const uint32_t* offsets, uint32_t* pb,
-                 uint32_t cap, uint32_t* err) {
+    k_scene_tree(const A4<R>* aabb_min, const A4<R>* aabb_max, A4<R>* g_leaf_min, A4<R>* g_leaf_max,
+                 A4<R>* g_node_min, A4<R>* g_node_max, TreeArgs t) {
     extern __shared__ __align__(16) unsigned char tree_smem[];
-    const uint2 chunk = chunks[blockIdx.x];  // scenes [x, y)
-    const uint32_t lo = scenes[chunk.x].body_lo;
-    const uint32_t nb = scenes[chunk.y - 1].body_hi - lo;
-    if (nb > cap_bodies) {  // the host packs chunks within the cap
-        if (threadIdx.x == 0) atomicOr(err, kErrIndexOverflow);
+    const uint32_t cidx = blockIdx.x;
+    const uint2 chunk = t.chunks[cidx];  // scenes [x, y)
+    const uint32_t lo = t.scenes[chunk.x].body_lo;
+    const uint32_t nb = t.scenes[chunk.y - 1].body_hi - lo;
+    const uint32_t cb = t.cap_bodies;
+    if (nb > cb) {  // the host packs chunks within the cap
+        if (threadIdx.x == 0) atomicOr(t.err, kErrIndexOverflow);
         return;
     }
-    A4<R>* lmn = reinterpret_cast<A4<R>*>(tree_smem);
-    A4<R>* lmx = lmn + cap_bodies;
-    A4<R>* nmn = lmx + cap_bodies;
-    A4<R>* nmx = nmn + cap_bodies;
-    uint2* ch = reinterpret_cast<uint2*>(nmx + cap_bodies);
-    uint32_t* lpar = reinterpret_cast<uint32_t*>(ch + cap_bodies);
-    uint32_t* npar = lpar + cap_bodies;
-    uint32_t* vis = npar + cap_bodies;
-    uint32_t* lbody = vis + cap_bodies;
-    uint32_t* lroot = lbody + cap_bodies;
     const uint32_t tid = threadIdx.x, nt = blockDim.x;
+    uint32_t* s_cursor = reinterpret_cast<uint32_t*>(tree_smem);
+    A4<R>* lmn = reinterpret_cast<A4<R>*>(tree_smem + 16);
+    A4<R>* lmx = lmn + cb;
+    A4<R>* nmn = lmx + cb;
+    A4<R>* nmx = nmn + cb;
+    uint2* ch = reinterpret_cast<uint2*>(nmx + cb);
+    uint32_t* lpar = reinterpret_cast<uint32_t*>(ch + cb);
+    uint32_t* npar = lpar + cb;
+    uint32_t* vis = npar + cb;  // visit flags, then per-body pair counts
+    uint32_t* lbody = vis + cb;
+    uint32_t* lroot = lbody + cb;
+    uint32_t* nhi = lroot + cb;
+    if (WRITE && !t.chunk_ovf[cidx]) {
+        // place the scratch pairs: body a's segment starts at offsets[a]
+        for (uint32_t p = tid; p < nb; p += nt) vis[p] = 0u;
+        __syncthreads();
+        const uint32_t np = t.chunk_n[cidx];
+        const uint2* src = t.scratch + (size_t)lo * t.scratch_k;
+        for (uint32_t k = tid; k < np; k += nt) {
+            const uint2 ab = src[k];
+            const uint32_t pos = t.offsets[ab.x] + atomicAdd(&vis[ab.x - lo], 1u);
+            if (pos < t.cap) t.pb[pos] = ab.y;
+        }
+        return;
+    }
     // slot p is leaf p of its scene and, except for a scene's last slot,
     // internal node (p - scene start) of that scene
     for (uint32_t p = tid; p < nb; p += nt) {
-        const SceneDesc sc = scenes[scene_of_pos[lo + p]];
+        const SceneDesc sc = t.scenes[t.scene_of_pos[lo + p]];
         const uint32_t root = sc.body_lo - lo, ns = sc.body_hi - sc.body_lo;
-        const uint32_t b = leaf_body[lo + p];
+        const uint32_t b = t.leaf_body[lo + p];
         lbody[p] = b;
         lroot[p] = ns >= 2 ? root : kNoRoot;
         if (WRITE) {
@@ -327,24 +370,26 @@ __global__ void __launch_bounds__(kSceneTreeThreads)
             lmx[p] = c;
             g_leaf_min[lo + p] = a;
             g_leaf_max[lo + p] = c;
-            lpar[p] = ns >= 2 ? parent[n + lo + p] - lo : 0u;
+            lpar[p] = ns >= 2 ? t.parent[t.n + lo + p] - lo : 0u;
         }
         if (lo + p + 1 < sc.body_hi) {  // internal node
-            const uint2 c = children[lo + p];
+            const uint2 c = t.children[lo + p];
             ch[p] = make_uint2((c.x & kLeafFlag) ? (((c.x & ~kLeafFlag) - lo) | kLeafFlag) : c.x - lo,
                                (c.y & kLeafFlag) ? (((c.y & ~kLeafFlag) - lo) | kLeafFlag) : c.y - lo);
             if (WRITE) {
                 nmn[p] = g_node_min[lo + p];
                 nmx[p] = g_node_max[lo + p];
             } else {
-                npar[p] = p == root ? p : parent[lo + p] - lo;
+                npar[p] = p == root ? p : t.parent[lo + p] - lo;
                 vis[p] = 0u;
             }
         }
     }
+    if (!WRITE && tid == 0) *s_cursor = 0u;
     __syncthreads();
     if (!WRITE) {
-        // bottom-up unions: the second arrival at a node computes it
+        // bottom-up unions and highest leaf positions: the second arrival at
+        // a node computes it
         for (uint32_t p = tid; p < nb; p += nt) {
             const uint32_t root = lroot[p];
             if (root == kNoRoot) continue;
@@ -355,31 +400,34 @@ __global__ void __launch_bounds__(kSceneTreeThreads)
                 __threadfence_block();
                 const uint2 c = ch[node];
                 const uint32_t li = c.x & ~kLeafFlag, ri = c.y & ~kLeafFlag;
-                const A4<R> a0 = (c.x & kLeafFlag) ? lmn[li] : nmn[li], a1 = (c.x & kLeafFlag) ? lmx[li] : nmx[li];
-                const A4<R> b0 = (c.y & kLeafFlag) ? lmn[ri] : nmn[ri], b1 = (c.y & kLeafFlag) ? lmx[ri] : nmx[ri];
+                const bool ll = c.x & kLeafFlag, rl = c.y & kLeafFlag;
+                const A4<R> a0 = ll ? lmn[li] : nmn[li], a1 = ll ? lmx[li] : nmx[li];
+                const A4<R> b0 = rl ? lmn[ri] : nmn[ri], b1 = rl ? lmx[ri] : nmx[ri];
                 nmn[node] = A4<R>{fmin_(a0.x, b0.x), fmin_(a0.y, b0.y), fmin_(a0.z, b0.z), R(0)};
                 nmx[node] = A4<R>{fmax_(a1.x, b1.x), fmax_(a1.y, b1.y), fmax_(a1.z, b1.z), R(0)};
+                nhi[node] = max(ll ? li : nhi[li], rl ? ri : nhi[ri]);
                 if (node == root) break;
                 node = npar[node];
             }
         }
         __syncthreads();
-        for (uint32_t p = tid; p < nb; p += nt)
-            if (lroot[p] != kNoRoot && lo + p + 1 < scenes[scene_of_pos[lo + p]].body_hi) {
+        for (uint32_t p = tid; p < nb; p += nt) {
+            vis[p] = 0u;  // per-body pair counts from here on
+            if (lroot[p] != kNoRoot && lo + p + 1 < t.scenes[t.scene_of_pos[lo + p]].body_hi) {
                 g_node_min[lo + p] = nmn[p];
                 g_node_max[lo + p] = nmx[p];
             }
-    }
-    for (uint32_t p = tid; p < nb; p += nt) {
-        const uint32_t i = lbody[p];
-        const uint32_t root = lroot[p];
-        if (root == kNoRoot) {
-            if (!WRITE) counts[i] = 0u;
-            continue;
         }
+        __syncthreads();
+    }
+    const uint32_t region = nb * t.scratch_k;
+    uint2* dst = t.scratch + (size_t)lo * t.scratch_k;
+    for (uint32_t p = tid; p < nb; p += nt) {
+        const uint32_t root = lroot[p];
+        if (root == kNoRoot) continue;
+        const uint32_t i = lbody[p];
         const A4<R> qmn = lmn[p], qmx = lmx[p];
-        uint32_t found = 0;
-        uint32_t out = WRITE ? offsets[i] : 0u;
+        uint32_t out = WRITE ? t.offsets[i] : 0u;
         uint32_t stack[kStack];
         int sp = 0;
         uint32_t node = root;
@@ -393,18 +441,21 @@ __global__ void __launch_bounds__(kSceneTreeThreads)
                 const uint32_t x = cc[k];
                 const uint32_t idx = x & ~kLeafFlag;
                 if (x & kLeafFlag) {
-                    if (overlap(qmn, qmx, lmn[idx], lmx[idx])) {
+                    if ((WRITE || idx > p) && overlap(qmn, qmx, lmn[idx], lmx[idx])) {
                         const uint32_t j = lbody[idx];
-                        if (j > i) {
-                            if (WRITE) {
-                                if (out < cap) pb[out] = j;
+                        if (WRITE) {  // overflow fallback: body i's partners j > i
+                            if (j > i) {
+                                if (out < t.cap) t.pb[out] = j;
                                 ++out;
-                            } else {
-                                ++found;
                             }
+                        } else {
+                            const uint32_t a = min(i, j), b = max(i, j);
+                            atomicAdd(&vis[a - lo], 1u);
+                            const uint32_t slot = atomicAdd(s_cursor, 1u);
+                            if (slot < region) dst[slot] = make_uint2(a, b);
                         }
                     }
-                } else if (overlap(qmn, qmx, nmn[idx], nmx[idx])) {
+                } else if ((WRITE || nhi[idx] > p) && overlap(qmn, qmx, nmn[idx], nmx[idx])) {
                     next[push++] = idx;
                 }
             }
@@ -417,11 +468,19 @@ __global__ void __launch_bounds__(kSceneTreeThreads)
                     if (sp < kStack)
                         stack[sp++] = next[1];
                     else
-                        atomicOr(err, kErrIndexOverflow);
+                        atomicOr(t.err, kErrIndexOverflow);
                 }
             }
         }
-        if (!WRITE) counts[i] = found;
+    }
+    if (!WRITE) {
+        __syncthreads();
+        for (uint32_t p = tid; p < nb; p += nt) t.counts[lo + p] = vis[p];
+        if (tid == 0) {
+            const uint32_t total = *s_cursor;
+            t.chunk_n[cidx] = min(total, region);
+            t.chunk_ovf[cidx] = total > region ? 1u : 0u;
+        }
     }
 }
 
