@@ -20,6 +20,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <utility>
+
 #include "../../include/dio_cuda.h"
 #include "dio_math.cuh"
 
@@ -184,6 +186,33 @@ inline int grid_for(uint64_t n, int block, int max_blocks = 1 << 20) {
     if (g < 1) g = 1;
     if (g > (uint64_t)max_blocks) g = max_blocks;
     return (int)g;
+}
+
+// ---- programmatic dependent launch ----
+// A kernel launched with programmatic stream serialisation may start while
+// its predecessor drains; griddepcontrol.wait (first thing in the kernel)
+// blocks until the predecessor has completed and its writes are visible, and
+// launch_dependents lets the successor's CTAs be scheduled early.  Launched
+// without the attribute, both instructions have no effect.
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_k(bool pdl, void (*kern)(KArgs...), int grid, int block, size_t smem, cudaStream_t s,
+                            Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
 }
 
 // ---- launch entry points (explicitly instantiated per precision) ----

@@ -1277,15 +1277,18 @@ class Engine final : public EngineBase {
         if (m_dev) m = cap_.max_contacts;
         k_init<P, R><<<gb, 256, 0, stream_>>>(w_, 0, n, o);
         launches_ += 2;
+        // programmatic dependent launch between the solve's kernels, unless
+        // event timers sit between them
+        const bool pdl = !cfg_.profile;
         for (uint32_t k = 0; k < o.iterations; ++k) {
             int par = (int)(k % 2);
             cudaEvent_t e0 = span_begin();
-            launch_primal<P, R>((int)cfg_.primal_variant, 0, sms_, w_, par, 1 - par, o, stream_);
+            launch_primal<P, R>((int)cfg_.primal_variant, pdl, w_, par, 1 - par, o, stream_);
             span_end(e0, 0);
             ++launches_;
             if (m) {
                 cudaEvent_t e1 = span_begin();
-                k_dual<P, R><<<gm, 256, 0, stream_>>>(w_, 0, m, m_dev, 1 - par, o);
+                DIO_CK(launch_k(pdl, k_dual<P, R>, gm, 256, 0, stream_, w_, 0u, m, m_dev, 1 - par, o));
                 span_end(e1, 1);
                 ++launches_;
             }
@@ -1294,7 +1297,7 @@ class Engine final : public EngineBase {
         int rb = fp == 0 ? 1 : 0;
         uint32_t fp_read = (o.iterations == 0 ? 0u : o.iterations - 1u) % 2u;
         int final_buf = 1 - (int)fp_read;
-        k_recover<P, R><<<gb, 256, 0, stream_>>>(w_, 0, n, rb, final_buf, o);
+        DIO_CK(launch_k(pdl, k_recover<P, R>, gb, 256, 0, stream_, w_, 0u, n, rb, final_buf, o));
         DIO_CK(cudaGetLastError());
         return DIO_OK;
     }

@@ -365,11 +365,15 @@ __device__ __forceinline__ void primal_body_f(const DevWorld<P, R>& w, uint32_t 
     B.g[3] = ra.x;
     B.g[4] = ra.y;
     B.g[5] = ra.z;
-    const V3<R> dqsl = cast3<R>(sub(sp, xyz(fetch.ipos(i))));
-    const V3<R> dqsa = cast3<R>(ang_diff(sq, quat(fetch.irot(i))));
-    const R k_alpha = R(1) - o.alpha;
     const uint32_t j0 = w.row_off[i], j1 = w.row_off[i + 1];
-    for (uint32_t j = j0; j < j1; ++j) primal_row_f(w, w.row_idx[j], w.row_oth[j], fetch, sqr, dqsl, dqsa, k_alpha, B);
+    if (j0 < j1) {
+        // displacement since the step start: read only by contact rows
+        const V3<R> dqsl = cast3<R>(sub(sp, xyz(fetch.ipos(i))));
+        const V3<R> dqsa = cast3<R>(ang_diff(sq, quat(fetch.irot(i))));
+        const R k_alpha = R(1) - o.alpha;
+        for (uint32_t j = j0; j < j1; ++j)
+            primal_row_f(w, w.row_idx[j], w.row_oth[j], fetch, sqr, dqsl, dqsa, k_alpha, B);
+    }
     for (uint32_t k = k0; k < k1; ++k) {
         const JView jv = w.jview[k];
         primal_jview_f<P, R>(jv, fetch, sp, sq, sqr, B);
@@ -394,6 +398,7 @@ __device__ __forceinline__ void primal_body(const DevWorld<P, R>& w, uint32_t i,
 template <class P, class R, int T, int MINB>
 __global__ void __launch_bounds__(T, MINB) k_primal_tile(DevWorld<P, R> w, int rd, int wr, SolveParams<R> o) {
     __shared__ A4<P> s_pos[T], s_rot[T], s_ipos[T], s_irot[T];
+    pdl_enter();
     const uint32_t lo = blockIdx.x * T;
     const uint32_t i = lo + threadIdx.x;
     if (i < w.n) {
@@ -415,6 +420,7 @@ __global__ void __launch_bounds__(T, MINB) k_primal_tile(DevWorld<P, R> w, int r
 // variants are chosen per world by the autotuner.
 template <class P, class R, int BLOCK, int MINB>
 __global__ void __launch_bounds__(BLOCK, MINB) k_primal(DevWorld<P, R> w, int rd, int wr, SolveParams<R> o) {
+    pdl_enter();
     for (uint32_t t = blockIdx.x * BLOCK + threadIdx.x; t < w.n_dyn; t += gridDim.x * BLOCK)
         primal_body(w, w.dyn_list[t], rd, wr, o);
 }
@@ -426,44 +432,42 @@ constexpr int kPrimalShape[kPrimalVariants][2] = {{128, 4}, {128, 5}, {128, 6}, 
                                                   {64, 10}, {128, 5}, {128, 6}, {256, 3}, {64, 10}};
 
 template <class P, class R>
-inline void launch_primal(int variant, int blocks_per_sm_hint, int sms, const DevWorld<P, R>& w, int rd, int wr,
-                          const SolveParams<R>& o, cudaStream_t s) {
-    (void)blocks_per_sm_hint;
+inline void launch_primal(int variant, bool pdl, const DevWorld<P, R>& w, int rd, int wr, const SolveParams<R>& o,
+                          cudaStream_t s) {
     const uint32_t nd = w.n_dyn > 0 ? w.n_dyn : 1;
     auto grid = [&](int block) { return grid_for(nd, block); };
     switch (variant) {
         case 0:
-            k_primal<P, R, 128, 4><<<grid(128), 128, 0, s>>>(w, rd, wr, o);
+            launch_k(pdl, k_primal<P, R, 128, 4>, grid(128), 128, 0, s, w, rd, wr, o);
             break;
         case 2:
-            k_primal<P, R, 128, 6><<<grid(128), 128, 0, s>>>(w, rd, wr, o);
+            launch_k(pdl, k_primal<P, R, 128, 6>, grid(128), 128, 0, s, w, rd, wr, o);
             break;
         case 3:
-            k_primal<P, R, 256, 2><<<grid(256), 256, 0, s>>>(w, rd, wr, o);
+            launch_k(pdl, k_primal<P, R, 256, 2>, grid(256), 256, 0, s, w, rd, wr, o);
             break;
         case 4:
-            k_primal<P, R, 256, 3><<<grid(256), 256, 0, s>>>(w, rd, wr, o);
+            launch_k(pdl, k_primal<P, R, 256, 3>, grid(256), 256, 0, s, w, rd, wr, o);
             break;
         case 5:
-            k_primal<P, R, 64, 10><<<grid(64), 64, 0, s>>>(w, rd, wr, o);
+            launch_k(pdl, k_primal<P, R, 64, 10>, grid(64), 64, 0, s, w, rd, wr, o);
             break;
         case 6:
-            k_primal_tile<P, R, 128, 5><<<grid_for(w.n, 128), 128, 0, s>>>(w, rd, wr, o);
+            launch_k(pdl, k_primal_tile<P, R, 128, 5>, grid_for(w.n, 128), 128, 0, s, w, rd, wr, o);
             break;
         case 7:
-            k_primal_tile<P, R, 128, 6><<<grid_for(w.n, 128), 128, 0, s>>>(w, rd, wr, o);
+            launch_k(pdl, k_primal_tile<P, R, 128, 6>, grid_for(w.n, 128), 128, 0, s, w, rd, wr, o);
             break;
         case 8:
-            k_primal_tile<P, R, 256, 3><<<grid_for(w.n, 256), 256, 0, s>>>(w, rd, wr, o);
+            launch_k(pdl, k_primal_tile<P, R, 256, 3>, grid_for(w.n, 256), 256, 0, s, w, rd, wr, o);
             break;
         case 9:
-            k_primal_tile<P, R, 64, 10><<<grid_for(w.n, 64), 64, 0, s>>>(w, rd, wr, o);
+            launch_k(pdl, k_primal_tile<P, R, 64, 10>, grid_for(w.n, 64), 64, 0, s, w, rd, wr, o);
             break;
         default:
-            k_primal<P, R, 128, 5><<<grid(128), 128, 0, s>>>(w, rd, wr, o);
+            launch_k(pdl, k_primal<P, R, 128, 5>, grid(128), 128, 0, s, w, rd, wr, o);
             break;
     }
-    (void)sms;
 }
 
 // Coloured Gauss-Seidel sweep: bodies color_order[c0 .. c1) in place.
@@ -523,6 +527,7 @@ __device__ __forceinline__ void dual_row(const DevWorld<P, R>& w, uint32_t c, in
 template <class P, class R>
 __global__ void __launch_bounds__(256) k_dual(DevWorld<P, R> w, uint32_t lo, uint32_t hi, const uint32_t* dyn_hi,
                                               int rd, SolveParams<R> o) {
+    pdl_enter();
     uint32_t end = dyn_hi ? *dyn_hi : hi;
     for (uint32_t c = lo + blockIdx.x * blockDim.x + threadIdx.x; c < end; c += gridDim.x * blockDim.x)
         dual_row(w, c, rd, o);
@@ -553,6 +558,7 @@ __device__ __forceinline__ void recover_body(const DevWorld<P, R>& w, uint32_t i
 template <class P, class R>
 __global__ void __launch_bounds__(256) k_recover(DevWorld<P, R> w, uint32_t lo, uint32_t hi, int rb, int final_buf,
                                                  SolveParams<R> o) {
+    pdl_enter();
     for (uint32_t i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += gridDim.x * blockDim.x) {
         recover_body(w, i, rb, o);
         if (final_buf != 0) {
