@@ -131,9 +131,9 @@ __device__ __forceinline__ uint32_t container_rows(const DevWorld<P, R>& w, uint
     V3<R> vel = cast3<R>(xyz(w.vel[i]));
     const bool boxy = b.shape.tag == DIO_SHAPE_CUBE || b.shape.tag == DIO_SHAPE_BOX;
     // Quick reject: every support point lies within an L1 bounding radius of
-    // the body centre, so a body whose centre plus that radius plus this
-    // step's travel is (with rounding slack) inside all six walls has no
-    // row with depth > 0 -- the same empty set the full test produces.
+    // the body centre, so when the centre plus that radius plus this step's
+    // travel is (with rounding slack) inside a wall, that wall has no row
+    // with depth > 0 -- the same empty set the full test produces.
     R rbound = R(-1);
     if (boxy) {
         rbound = dabs(b.shape.c[0].x) + dabs(b.shape.c[0].y) + dabs(b.shape.c[0].z);
@@ -144,19 +144,10 @@ __device__ __forceinline__ uint32_t container_rows(const DevWorld<P, R>& w, uint
         for (int k = 0; k < 4; ++k)
             rbound = fmax_(rbound, dabs(b.shape.c[k].x) + dabs(b.shape.c[k].y) + dabs(b.shape.c[k].z));
     }
-    if (rbound >= R(0)) {
-        const R travel = length(vel) * o.dt;
-        bool inside = true;
-        for (int k = 0; k < 6 && inside; ++k) {
-            V3<R> axis = k < 2 ? V3<R>{R(1), R(0), R(0)} : (k < 4 ? V3<R>{R(0), R(1), R(0)} : V3<R>{R(0), R(0), R(1)});
-            V3<R> outward = rotate(crot, scale(axis, (k & 1) ? R(-1) : R(1)));
-            R plane = dot(center, outward) + half;
-            R d = dot(b.pos, outward);
-            R slack = R(1e-4) * (R(1) + dabs(plane) + dabs(d));
-            if (!(d + rbound + travel + slack < plane)) inside = false;
-        }
-        if (inside) return 0;
-    }
+    // The bound is applied per wall: a wall that no support point can reach
+    // this step yields no row, so it is skipped (the other walls, and every
+    // wall of a body without a bound, take the full test).
+    const R travel = rbound >= R(0) ? length(vel) * o.dt : R(0);
     uint32_t count = 0;
 #pragma unroll 1
     for (int k = 0; k < 6; ++k) {
@@ -164,6 +155,11 @@ __device__ __forceinline__ uint32_t container_rows(const DevWorld<P, R>& w, uint
         R sign = (k & 1) ? R(-1) : R(1);
         V3<R> outward = rotate(crot, scale(axis, sign));
         R plane = dot(center, outward) + half;
+        if (rbound >= R(0)) {
+            const R d = dot(b.pos, outward);
+            const R slack = R(1e-4) * (R(1) + dabs(plane) + dabs(d));
+            if (d + rbound + travel + slack < plane) continue;
+        }
         V3<R> pts[4];
         uint32_t np;
         if (boxy) {
