@@ -122,6 +122,7 @@ struct DevWorld {
     DioShape* shape;
     uint32_t* scene;
     A4<P>* origin;  // per-scene detection origin (split precision rebase)
+    const A4<R>* walls;  // per scene, 6 container walls: outward normal xyz, plane offset w
     const A4<R>* hull;  // hull vertex pool
     // broad phase
     A4<R>* aabb_min;

@@ -388,6 +388,8 @@ class Engine final : public EngineBase {
         DIO_TRY(alloc(&w_.shape, N));
         DIO_TRY(alloc(&w_.scene, N));
         DIO_TRY(alloc(&origin_, S));
+        DIO_TRY(alloc(&walls_, 6ull * S));
+        w_.walls = walls_;
         DIO_TRY(alloc(&w_.aabb_min, N));
         DIO_TRY(alloc(&w_.aabb_max, N));
         DIO_TRY(alloc(&w_.color, N));
@@ -791,6 +793,7 @@ class Engine final : public EngineBase {
         DIO_CK(cudaMemcpyAsync(scenes_, sc.data(), ns * sizeof(SceneDesc), cudaMemcpyHostToDevice, stream_));
         DIO_CK(cudaMemcpyAsync(origin_, org.data(), ns * sizeof(A4<P>), cudaMemcpyHostToDevice, stream_));
         w_.origin = cfg_.precision == DIO_PREC_SPLIT ? origin_ : nullptr;
+        k_scene_walls<P, R><<<grid_for(6ull * ns, 128), 128, 0, stream_>>>(w_, scenes_, ns, walls_);
         w_.n_scenes = ns;
         k_scene_of<<<ns, 128, 0, stream_>>>(w_.scene, scenes_, ns);
         if (d->n_hull_vertices) {
@@ -1040,6 +1043,7 @@ class Engine final : public EngineBase {
         DIO_CK(cudaMemsetAsync(w_.scene, 0, (size_t)std::max(n, 1u) * 4, stream_));
         w_.n_scenes = 1;
         w_.origin = nullptr;
+        k_scene_walls<P, R><<<1, 32, 0, stream_>>>(w_, scenes_, 1u, walls_);
         w_.n = n;
         // the API path is single-scene FP32; keep host scene table in sync
         scenes_host_.assign(1, x);
@@ -1739,6 +1743,7 @@ class Engine final : public EngineBase {
     uint2* tree_scratch_ = nullptr;
     uint32_t scratch_k_ = 2;
     A4<P>* origin_ = nullptr;
+    A4<R>* walls_ = nullptr;
     A4<R>* hull_ = nullptr;
     Counters* ctr_ = nullptr;
     Counters* hctr_ = nullptr;

@@ -123,11 +123,7 @@ template <class P, class R>
 __device__ __forceinline__ uint32_t container_rows(const DevWorld<P, R>& w, uint32_t i, const SceneDesc& sc,
                                                    const PrepParams<R>& o, bool write_out, uint32_t r) {
     NB<R> b = load_nb(w, i);
-    V3<P> org{P(0), P(0), P(0)};
-    if (w.origin) org = xyz(w.origin[w.scene[i]]);
-    V3<R> center = cast3<R>(sub(V3<P>{P(sc.center[0]), P(sc.center[1]), P(sc.center[2])}, org));
-    Q4<R> crot{R(sc.rotation[0]), R(sc.rotation[1]), R(sc.rotation[2]), R(sc.rotation[3])};
-    R half = R(sc.half_extent);
+    const A4<R>* walls = w.walls + 6 * (size_t)w.scene[i];
     V3<R> vel = cast3<R>(xyz(w.vel[i]));
     const bool boxy = b.shape.tag == DIO_SHAPE_CUBE || b.shape.tag == DIO_SHAPE_BOX;
     // Quick reject: every support point lies within an L1 bounding radius of
@@ -151,10 +147,9 @@ __device__ __forceinline__ uint32_t container_rows(const DevWorld<P, R>& w, uint
     uint32_t count = 0;
 #pragma unroll 1
     for (int k = 0; k < 6; ++k) {
-        V3<R> axis = k < 2 ? V3<R>{R(1), R(0), R(0)} : (k < 4 ? V3<R>{R(0), R(1), R(0)} : V3<R>{R(0), R(0), R(1)});
-        R sign = (k & 1) ? R(-1) : R(1);
-        V3<R> outward = rotate(crot, scale(axis, sign));
-        R plane = dot(center, outward) + half;
+        const A4<R> wall = walls[k];
+        const V3<R> outward = xyz(wall);
+        const R plane = wall.w;
         if (rbound >= R(0)) {
             const R d = dot(b.pos, outward);
             const R slack = R(1e-4) * (R(1) + dabs(plane) + dabs(d));
@@ -194,6 +189,27 @@ __device__ __forceinline__ uint32_t container_rows(const DevWorld<P, R>& w, uint
         }
     }
     return count;
+}
+
+// The six walls of each scene's container (container_collide,
+// engine/src/physics/gpu.rs): outward normal = rotation * (+-axis), plane
+// offset = centre . outward + half extent; centre rebased to the scene's
+// detection origin.  Computed once per upload.
+template <class P, class R>
+__global__ void k_scene_walls(DevWorld<P, R> w, const SceneDesc* scenes, uint32_t ns, A4<R>* walls) {
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < 6 * ns; t += gridDim.x * blockDim.x) {
+        const uint32_t s = t / 6, k = t % 6;
+        const SceneDesc sc = scenes[s];
+        V3<P> org{P(0), P(0), P(0)};
+        if (w.origin) org = xyz(w.origin[s]);
+        const V3<R> center = cast3<R>(sub(V3<P>{P(sc.center[0]), P(sc.center[1]), P(sc.center[2])}, org));
+        const Q4<R> crot{R(sc.rotation[0]), R(sc.rotation[1]), R(sc.rotation[2]), R(sc.rotation[3])};
+        const R half = R(sc.half_extent);
+        const V3<R> axis = k < 2 ? V3<R>{R(1), R(0), R(0)} : (k < 4 ? V3<R>{R(0), R(1), R(0)} : V3<R>{R(0), R(0), R(1)});
+        const R sign = (k & 1) ? R(-1) : R(1);
+        const V3<R> outward = rotate(crot, scale(axis, sign));
+        walls[t] = A4<R>{outward.x, outward.y, outward.z, dot(center, outward) + half};
+    }
 }
 
 template <class P, class R>
