@@ -183,6 +183,27 @@ struct TileFetch {
     __device__ __forceinline__ A4<P> irot(uint32_t j) const { return j - lo < (uint32_t)T ? sr[j - lo] : w.init_rot[j]; }
 };
 
+// Clamped row forces shared by avbd_primal and avbd_dual (avbd/src/lib.rs:
+// 380-406, 606-631): normal f0 <= 0, friction (f1, f2) scaled back onto the
+// cone |f_t| <= mu |f0|; `tm` (unclamped friction magnitude) and `bounds`
+// feed the dual's penalty rule.
+template <class P, class R>
+__device__ __forceinline__ void row_forces(const RowDual<P, R>& du, R mu, R c0, R c1, R c2, P& f0, P& f1, P& f2,
+                                           P& tm, P& bounds) {
+    f0 = fmin_(P(du.penalty.x * c0) + du.lambda.x, P(0));
+    const P f1r = P(du.penalty.y * c1) + du.lambda.y;
+    const P f2r = P(du.penalty.z * c2) + du.lambda.z;
+    bounds = dabs(f0) * P(mu);
+    tm = dsqrt(f1r * f1r + f2r * f2r);
+    f1 = f1r;
+    f2 = f2r;
+    if (tm > bounds && tm > P(0)) {
+        const P s = bounds / tm;
+        f1 = f1r * s;
+        f2 = f2r * s;
+    }
+}
+
 // One contact row seen from body i (avbd/src/lib.rs:321-418).
 template <class P, class R, class F>
 __device__ __forceinline__ void primal_row_f(const DevWorld<P, R>& w, uint32_t r, uint32_t oth, const F& fetch,
@@ -210,17 +231,8 @@ __device__ __forceinline__ void primal_row_f(const DevWorld<P, R>& w, uint32_t r
     c0 = c0 + (dot(r0, dqsl) + dot(j0, dqsa) - dot(r0, dol) - dot(cross(rot_other, r0), doa));
     c1 = c1 + (dot(r1, dqsl) + dot(j1, dqsa) - dot(r1, dol) - dot(cross(rot_other, r1), doa));
     c2 = c2 + (dot(r2, dqsl) + dot(j2, dqsa) - dot(r2, dol) - dot(cross(rot_other, r2), doa));
-    P f0 = fmin_(P(du.penalty.x * c0) + du.lambda.x, P(0));
-    P f1r = P(du.penalty.y * c1) + du.lambda.y;
-    P f2r = P(du.penalty.z * c2) + du.lambda.z;
-    P bounds = dabs(f0) * P(rs.n.w);
-    P tm = dsqrt(f1r * f1r + f2r * f2r);
-    P f1 = f1r, f2 = f2r;
-    if (tm > bounds && tm > P(0)) {
-        P s = bounds / tm;
-        f1 = f1r * s;
-        f2 = f2r * s;
-    }
+    P f0, f1, f2, tm, bounds;
+    row_forces(du, rs.n.w, c0, c1, c2, f0, f1, f2, tm, bounds);
     stamp(B, r0, j0, du.penalty.x, R(f0));
     stamp(B, r1, j1, du.penalty.y, R(f1));
     stamp(B, r2, j2, du.penalty.z, R(f2));
@@ -502,17 +514,8 @@ __device__ __forceinline__ void dual_row(const DevWorld<P, R>& w, uint32_t c, in
     c0 = c0 + (dot(r0, dal) + dot(cross(raw, r0), daa) - dot(r0, dbl) - dot(cross(rbw, r0), dba));
     c1 = c1 + (dot(r1, dal) + dot(cross(raw, r1), daa) - dot(r1, dbl) - dot(cross(rbw, r1), dba));
     c2 = c2 + (dot(r2, dal) + dot(cross(raw, r2), daa) - dot(r2, dbl) - dot(cross(rbw, r2), dba));
-    P f0 = fmin_(P(du.penalty.x * c0) + du.lambda.x, P(0));
-    P f1r = P(du.penalty.y * c1) + du.lambda.y;
-    P f2r = P(du.penalty.z * c2) + du.lambda.z;
-    P bounds = dabs(f0) * P(rs.n.w);
-    P tm = dsqrt(f1r * f1r + f2r * f2r);
-    P f1 = f1r, f2 = f2r;
-    if (tm > bounds && tm > P(0)) {
-        P s = bounds / tm;
-        f1 = f1r * s;
-        f2 = f2r * s;
-    }
+    P f0, f1, f2, tm, bounds;
+    row_forces(du, rs.n.w, c0, c1, c2, f0, f1, f2, tm, bounds);
     du.lambda.x = f0;
     du.lambda.y = f1;
     du.lambda.z = f2;

@@ -143,6 +143,36 @@ def test_world_steps_match_oracle(steps, use_graph):
         assert np.array_equal(_bits(gc), _bits(rc)), (sc.name, steps)
 
 
+def _scene_with_static_overlap():
+    """A pyramid plus two overlapping static boxes: their contact rows have no
+    dynamic endpoint (no primal visits them; the dual still updates them)."""
+    sc = scenes.pyramid(levels=4)
+    extra = [ph.cube((6.0, 0.5, 0.0), 0.5, 0.0), ph.cube((6.6, 0.5, 0.0), 0.5, 0.0)]
+    b, s = ph.pack_bodies(extra)
+    return scenes.Scene("pyramid+static", np.concatenate([sc.bodies, b]), np.concatenate([sc.state, s]),
+                        containers=sc.containers, options=sc.options)
+
+
+def test_rows_without_dynamic_endpoint_match_oracle():
+    """Rows between two static bodies are never visited by a primal thread
+    but the dual still advances their lambda / penalty every iteration: the
+    contact output matches the oracle's bits (and the rest of the world)."""
+    for sc in [_scene_with_static_overlap(), scenes.box_demo()]:
+        ow = O.World(sc)
+        ow.step(sc.options, 12)
+        with _world(sc) as w:
+            w.step(sc.options, 12)
+            gb, gs = w.download()
+            gc = w.contacts()
+        rb, rs = ow.download()
+        rc = ow.contacts()
+        if sc.name == "pyramid+static":
+            n0 = sc.n - 2
+            assert np.any((rc["a"] >= n0) & (rc["b"] >= n0)), "no static-static row"
+        assert np.array_equal(_bits(gb), _bits(rb)) and np.array_equal(_bits(gs), _bits(rs)), sc.name
+        assert np.array_equal(_bits(gc), _bits(rc)), sc.name
+
+
 def test_batched_world_equals_each_scene_alone():
     parts = [scenes.pyramid(levels=3), scenes.constraints_demo(), scenes.box_demo(),
              scenes.cube_field(nx=3, nz=3, ny=2)]
