@@ -434,7 +434,7 @@ __global__ void __launch_bounds__(kSceneTreeThreads)
         while (true) {
             const uint2 c = ch[node];
             const uint32_t cc[2] = {c.x, c.y};
-            uint32_t next[2];
+            uint32_t n0 = 0, n1 = 0;  // internal children to visit (registers)
             uint32_t push = 0;
 #pragma unroll
             for (int k = 0; k < 2; ++k) {
@@ -456,17 +456,21 @@ __global__ void __launch_bounds__(kSceneTreeThreads)
                         }
                     }
                 } else if ((WRITE || nhi[idx] > p) && overlap(qmn, qmx, nmn[idx], nmx[idx])) {
-                    next[push++] = idx;
+                    if (push == 0)
+                        n0 = idx;
+                    else
+                        n1 = idx;
+                    ++push;
                 }
             }
             if (push == 0) {
                 if (sp == 0) break;
                 node = stack[--sp];
             } else {
-                node = next[0];
+                node = n0;
                 if (push == 2) {
                     if (sp < kStack)
-                        stack[sp++] = next[1];
+                        stack[sp++] = n1;
                     else
                         atomicOr(t.err, kErrIndexOverflow);
                 }
