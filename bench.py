@@ -8,9 +8,9 @@ and stepped by dio_step (broad -> narrow -> rows + warm start -> solve).
 One JSON line on rank 0:
   value      body-steps/s with the world resident in HBM (CUDA events on the
              library's stream, K steps, max over ranks)
-  e2e        the same metric through the public API with host buffers: every
-             step re-uploads poses + state (dio_world_set_state) and reads
-             poses + state back (dio_world_download)
+  e2e        the same metric through the public API with pinned host buffers:
+             every step re-uploads poses + state (dio_world_set_state) and
+             reads poses + state back (dio_world_download)
   plain      the one-scene-per-launch path (one context per scene) on a
              sample of scenes, for the batched-vs-plain ratio
   roofline   the primal kernel: algorithmic bytes per launch / event time
@@ -275,8 +275,11 @@ def main():
     # end to end through the public API with host buffers
     e2e = None
     if not args.no_e2e:
-        hb = np.zeros(sc.n, sc.bodies.dtype)
-        hs = np.zeros(sc.n, sc.state.dtype)
+        # the caller's host buffers: page-locked (cudaHostAlloc through torch)
+        hb = torch.empty(sc.n * sc.bodies.dtype.itemsize, dtype=torch.uint8,
+                         pin_memory=True).numpy().view(sc.bodies.dtype)
+        hs = torch.empty(sc.n * sc.state.dtype.itemsize, dtype=torch.uint8,
+                         pin_memory=True).numpy().view(sc.state.dtype)
         w.download_into(hb, hs)
         k2 = max(3, args.steps // 2)
         torch.cuda.synchronize()

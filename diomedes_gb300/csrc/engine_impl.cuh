@@ -264,9 +264,19 @@ __global__ void k_pack_world(DevWorld<P, R> w, DioGpuBody* bodies, DioBodyState*
 }
 
 template <class P, class R>
-__global__ void k_dyn_flags(DevWorld<P, R> w, uint32_t n, uint32_t* flags) {
+__global__ void k_dyn_flags(DevWorld<P, R> w, uint32_t n, uint32_t* flags, uint32_t* keep) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t f = w.inv[i].w != R(0) ? 1u : 0u;
+        flags[i] = f;
+        keep[i] = f;
+    }
+}
+
+// did the set of dynamic bodies change since the list was built?
+template <class P, class R>
+__global__ void k_dyn_changed(DevWorld<P, R> w, uint32_t n, const uint32_t* keep, uint32_t* changed) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        flags[i] = w.inv[i].w != R(0) ? 1u : 0u;
+        if ((w.inv[i].w != R(0) ? 1u : 0u) != keep[i]) *changed = 1u;
 }
 
 static __global__ void k_dyn_fill(const uint32_t* flags, const uint32_t* pos, uint32_t n, uint32_t* list) {
@@ -439,6 +449,7 @@ class Engine final : public EngineBase {
         DIO_TRY(alloc(&jview_, 2ull * J));
         DIO_TRY(alloc(&dyn_list_, N));
         DIO_TRY(alloc(&dyn_tmp_, N));
+        DIO_TRY(alloc(&dyn_keep_, N));
         DIO_TRY(alloc(&color_hist_, kMaxColors + 2));
         const size_t CNT = std::max<size_t>(std::max<size_t>(N, (size_t)PP * per_cap_), 2ull * M) + 2;
         DIO_TRY(alloc(&counts_, CNT));
@@ -839,7 +850,7 @@ class Engine final : public EngineBase {
             ++launches_;
         }
         if (state) {
-            DIO_TRY(upload_state(state, n));
+            DIO_TRY(upload_state(state, n, true));
             ++launches_;
         }
         return DIO_OK;
@@ -991,18 +1002,29 @@ class Engine final : public EngineBase {
         w_.n = n;
         return DIO_OK;
     }
-    int upload_state(const DioBodyState* state, uint32_t n) {
+    // keep_list: the body count and set of dynamic bodies are expected to be
+    // unchanged (a state update of the same world): the list is rebuilt only
+    // if a body changed between static and dynamic
+    int upload_state(const DioBodyState* state, uint32_t n, bool keep_list = false) {
         if (!n) return DIO_OK;
         if (!state) return inval("null state");
         DioBodyState* ds = reinterpret_cast<DioBodyState*>(reinterpret_cast<char*>(dstage_) +
                                                            align256((size_t)n * sizeof(DioGpuBody)));
         DIO_CK(cudaMemcpyAsync(ds, state, (size_t)n * sizeof(DioBodyState), cudaMemcpyHostToDevice, stream_));
         k_unpack_state<P, R><<<grid_for(n, 256), 256, 0, stream_>>>(w_, ds, n);
+        if (keep_list && dyn_list_n_ == n) {
+            DIO_CK(cudaMemsetAsync(&ctr_->dyn_changed, 0, 4, stream_));
+            k_dyn_changed<P, R><<<grid_for(n, 256), 256, 0, stream_>>>(w_, n, dyn_keep_, &ctr_->dyn_changed);
+            DIO_CK(cudaMemcpyAsync(&hctr_->dyn_changed, &ctr_->dyn_changed, 4, cudaMemcpyDeviceToHost, stream_));
+            DIO_CK(cudaStreamSynchronize(stream_));
+            if (!hctr_->dyn_changed) return DIO_OK;
+        }
         return build_dyn_list(n);
     }
     // compacted list of dynamic bodies (inverse mass != 0), index order
     int build_dyn_list(uint32_t n) {
-        k_dyn_flags<P, R><<<grid_for(n, 256), 256, 0, stream_>>>(w_, n, counts2_);
+        dyn_list_n_ = n;
+        k_dyn_flags<P, R><<<grid_for(n, 256), 256, 0, stream_>>>(w_, n, counts2_, dyn_keep_);
         DIO_CK(cudaMemsetAsync(counts2_ + n, 0, 4, stream_));
         size_t tb = cub_bytes_;
         DIO_CK(cub::DeviceScan::ExclusiveSum(cub_tmp_, tb, counts2_, offsets2_, (int)n + 1, stream_));
@@ -1728,6 +1750,8 @@ class Engine final : public EngineBase {
     JView* jview_ = nullptr;
     uint32_t* dyn_list_ = nullptr;
     uint32_t* dyn_tmp_ = nullptr;
+    uint32_t* dyn_keep_ = nullptr;  // dynamic flags the list was built from
+    uint32_t dyn_list_n_ = 0xFFFFFFFFu;
     uint32_t* color_hist_ = nullptr;
     uint32_t ncolors_ = 0;
     uint32_t color_off_h_[kMaxColors + 1] = {};

@@ -173,6 +173,35 @@ def test_rows_without_dynamic_endpoint_match_oracle():
         assert np.array_equal(_bits(gc), _bits(rc)), sc.name
 
 
+def test_set_state_that_changes_dynamic_bodies_rebuilds_the_list():
+    """dio_world_set_state keeps the dynamic-body list unless a body turns
+    static or dynamic; then the list is rebuilt and the body moves (or stops)."""
+    sc = _scene_with_static_overlap()
+    k = sc.n - 1  # a static box overlapping another static box
+    with _world(sc) as w:
+        w.step(sc.options, 2)
+        b0, s0 = w.download()
+        s1 = s0.copy()
+        s1["inv_mass"][k] = 1.0
+        s1["inv_moment"][k, :3] = 6.0
+        w.set_state(None, s1)
+        w.step(sc.options, 4)
+        b1, s1b = w.download()
+        assert not np.array_equal(b1["position"][k], b0["position"][k])  # now dynamic: it moves
+        s2 = s1b.copy()
+        s2["inv_mass"][k] = 0.0
+        s2["inv_moment"][k, :3] = 0.0
+        s2["vel"][k] = 0.0
+        s2["ang"][k] = 0.0
+        w.set_state(None, s2)
+        w.step(sc.options, 3)
+        b2, _ = w.download()
+        assert np.array_equal(b2["position"][k], b1["position"][k])  # static again: it stays
+        assert w.stats()["error_flags"] == 0
+        # an unchanged state keeps the list: stepping matches a world stepped without it
+        w.set_state(None, w.download()[1])
+
+
 def test_batched_world_equals_each_scene_alone():
     parts = [scenes.pyramid(levels=3), scenes.constraints_demo(), scenes.box_demo(),
              scenes.cube_field(nx=3, nz=3, ny=2)]
