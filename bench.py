@@ -143,6 +143,16 @@ def primal_bytes(n_dyn, m, j_inc):
 PRIMAL_TRAFFIC_RATIO = 94.77 / 85.44
 
 
+def primal_gather_bytes(n_dyn, pair_rows, cont_rows, j_inc):
+    """Gather-inclusive upper bound of one primal launch: the compulsory bytes
+    plus, per row incidence, the row payload and CSR entries again and the
+    other body's snapshot and step-start pose (64 B, SoA float4) for pair
+    rows; per joint incidence the 48 B joint view and the other body's
+    snapshot pose (32 B)."""
+    incid = 2 * pair_rows + cont_rows
+    return 132 * n_dyn + incid * (108 + 8) + 2 * pair_rows * 64 + j_inc * (48 + 32)
+
+
 def run_cpu(sc, steps, warmup, threads, budget_s=20.0):
     """CPU oracle (f32) on a scene: body-steps/s."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
@@ -271,6 +281,9 @@ def main():
     j_inc = 2 * len(sc.constraints)
     pb = primal_bytes(n_dyn, stp["contacts"], j_inc)
     achieved = pb / (prim_ms / 1e3) / 1e9 if prim_ms > 0 else None
+    rows_now = w.contacts()
+    cont_rows = int((rows_now["b"] == 0xFFFFFFFF).sum())
+    pg = primal_gather_bytes(n_dyn, len(rows_now) - cont_rows, cont_rows, j_inc)
 
     # end to end through the public API with host buffers
     e2e = None
@@ -346,8 +359,10 @@ def main():
         sample = sample_scenes(scenes, sc, 32)
         threads = os.cpu_count() or 1
         v, done, dt = run_cpu(sample, 5, 1, threads, budget_s=20.0)
+        v1, done1, _ = run_cpu(sample, 3, 1, 1, budget_s=10.0)
         cpu = {"value": v, "unit": "body-steps/s", "cores": threads, "kind": "port",
-               "sample": f"first 32 of {sc.n_scenes} scenes ({sample.n} bodies), {done} steps after 1 warm-up"}
+               "sample": f"first 32 of {sc.n_scenes} scenes ({sample.n} bodies), {done} steps after 1 warm-up",
+               "single_thread": {"value": v1, "cores": 1, "steps": done1}}
 
     if rank == 0:
         line = {
@@ -368,7 +383,9 @@ def main():
                          "traffic": PRIMAL_TRAFFIC_RATIO * pb,
                          "traffic_source": "ncu DRAM bytes of one launch (step 1), scaled by algorithmic bytes",
                          "kernel": "k_primal", "bytes_per_launch": pb, "avg_launch_ms": prim_ms,
-                         "peak_kind": peak_kind},
+                         "peak_kind": peak_kind,
+                         "gather_bytes_per_launch": pg,
+                         "achieved_gather": pg / (prim_ms / 1e3) / 1e9 if prim_ms > 0 else None},
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "gpu_launches": st["kernel_launches"],

@@ -25,6 +25,13 @@ SPHERE, CUBE, TETRAHEDRON, BOX, HULL = 0, 1, 2, 3, 4
 CONTAINER = 0xFFFFFFFF
 SPRING, ROD, BALL_SOCKET, ROPE = 0, 1, 2, 3
 CONTACTS_PER_PAIR = 4
+# header of a dio_world_checkpoint image (16-byte aligned sections follow:
+# bodies, state, joints, scene table, hull vertices, poses / velocities in
+# the world's precision, the last step's rows)
+CKPT_HEADER = np.dtype([("magic", "S8"), ("version", "<u4"), ("precision", "<u4"), ("p_bytes", "<u4"),
+                        ("r_bytes", "<u4"), ("n", "<u4"), ("n_joints", "<u4"), ("n_scenes", "<u4"),
+                        ("n_hull", "<u4"), ("rows", "<u4"), ("pair_rows", "<u4"), ("has_container", "<u4"),
+                        ("pad", "<u4"), ("steps", "<u8"), ("total_bytes", "<u8")])
 PRIMAL_VARIANTS = 10  # DIO_PRIMAL_VARIANTS
 
 SOLVER_JACOBI, SOLVER_COLORED = 0, 1
@@ -139,6 +146,8 @@ _PROTOS = {
     "dio_world_colors": [_P, _vp, _u32, ctypes.POINTER(_u32)],
     "dio_world_stats": [_P, ctypes.POINTER(StepStats)],
     "dio_world_reset_timers": [_P],
+    "dio_world_checkpoint": [_P, _vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)],
+    "dio_world_resume": [_P, _vp, ctypes.c_size_t],
     "dio_autotune": [_P, ctypes.POINTER(AvbdOptions), _u32, ctypes.c_char_p, ctypes.POINTER(Config)],
 }
 

@@ -184,6 +184,11 @@ class AvbdCompute(Context):
         return out[: m.value].copy(), offsets, indices[: offsets[-1]].copy()
 
 
+def checkpoint_header(image):
+    """The header fields of a checkpoint image (abi.CKPT_HEADER)."""
+    return np.frombuffer(image[: abi.CKPT_HEADER.itemsize], abi.CKPT_HEADER)[0]
+
+
 class World(Context):
     """A device-resident world of one or more packed scenes (dio_world_*)."""
 
@@ -291,3 +296,17 @@ class World(Context):
 
     def reset_timers(self):
         check(self.L.dio_world_reset_timers(self.h), self.h, "reset_timers")
+
+    def checkpoint(self):
+        """The world as a versioned byte image (dio_world_checkpoint)."""
+        size = ctypes.c_size_t()
+        check(self.L.dio_world_checkpoint(self.h, None, 0, ctypes.byref(size)), self.h, "checkpoint")
+        buf = np.zeros(size.value, np.uint8)
+        check(self.L.dio_world_checkpoint(self.h, ptr(buf), size.value, ctypes.byref(size)), self.h, "checkpoint")
+        return buf.tobytes()
+
+    def resume(self, image):
+        """Replace this context's world with a checkpoint image (dio_world_resume)."""
+        buf = np.frombuffer(image, np.uint8)
+        check(self.L.dio_world_resume(self.h, ptr(buf), buf.size), self.h, "resume")
+        self.n = int(checkpoint_header(image)["n"])

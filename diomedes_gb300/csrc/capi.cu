@@ -279,6 +279,14 @@ int dio_world_stats(DioCtx* ctx, DioStepStats* out) {
 int dio_world_reset_timers(DioCtx* ctx) {
     return with_world(ctx, false, [&](dio::EngineBase* e) { return e->reset_timers(); });
 }
+int dio_world_checkpoint(DioCtx* ctx, void* buffer, size_t capacity, size_t* size) {
+    if (!size) return DIO_ERR_INVALID;
+    return with_world(ctx, false, [&](dio::EngineBase* e) { return e->checkpoint(buffer, capacity, size); });
+}
+int dio_world_resume(DioCtx* ctx, const void* buffer, size_t size) {
+    if (!buffer) return DIO_ERR_INVALID;
+    return with_world(ctx, true, [&](dio::EngineBase* e) { return e->resume(buffer, size); });
+}
 
 }  // extern "C"
 

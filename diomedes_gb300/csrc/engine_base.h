@@ -46,6 +46,9 @@ struct EngineBase {
     // counters) and its restoration; used by the autotuner's trials
     virtual int snapshot() = 0;
     virtual int restore() = 0;
+    // host byte image of the whole world for checkpoint / resume
+    virtual int checkpoint(void* out, size_t cap, size_t* size) = 0;
+    virtual int resume(const void* in, size_t size) = 0;
     virtual int world_sizes(uint32_t* n, uint32_t* n_dyn, uint32_t* n_joints, uint32_t* n_scenes) = 0;
     virtual void set_stream(cudaStream_t s) = 0;
     virtual void set_config(const DioConfig& c) = 0;

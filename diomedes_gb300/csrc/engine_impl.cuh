@@ -807,6 +807,7 @@ class Engine final : public EngineBase {
         k_scene_walls<P, R><<<grid_for(6ull * ns, 128), 128, 0, stream_>>>(w_, scenes_, ns, walls_);
         w_.n_scenes = ns;
         k_scene_of<<<ns, 128, 0, stream_>>>(w_.scene, scenes_, ns);
+        n_hull_ = d->n_hull_vertices;
         if (d->n_hull_vertices) {
             std::vector<A4<R>> hv(d->n_hull_vertices);
             for (uint32_t i = 0; i < d->n_hull_vertices; ++i)
@@ -1406,6 +1407,155 @@ class Engine final : public EngineBase {
         lbvh_valid_ = snap_valid_;
         return DIO_OK;
     }
+    // ------------------------------------------------------- checkpoint
+    // Image: header, then 16-byte aligned sections in kCkptSections order.
+    struct CkptHeader {
+        char magic[8];
+        uint32_t version, precision, p_bytes, r_bytes;
+        uint32_t n, n_joints, n_scenes, n_hull;
+        uint32_t rows, pair_rows, has_container, pad;
+        uint64_t steps, total_bytes;
+    };
+    enum { kCkBodies, kCkState, kCkJoints, kCkScenes, kCkHull, kCkPos, kCkRot, kCkVel, kCkAng, kCkPrevVel,
+           kCkRowStatic, kCkRowDual, kCkRowAb, kCkptSections };
+    static size_t ckpt_layout(const CkptHeader& h, size_t off[kCkptSections]) {
+        const size_t a4 = (size_t)h.n * sizeof(A4<P>);
+        const size_t sz[kCkptSections] = {(size_t)h.n * sizeof(DioGpuBody),     (size_t)h.n * sizeof(DioBodyState),
+                                          (size_t)h.n_joints * sizeof(DioConstraint),
+                                          (size_t)h.n_scenes * sizeof(SceneDesc), (size_t)h.n_hull * 16,
+                                          a4, a4, a4, a4, a4,
+                                          (size_t)h.rows * sizeof(RowStatic<R>),
+                                          (size_t)h.rows * sizeof(RowDual<P, R>), (size_t)h.rows * sizeof(uint2)};
+        size_t o = (sizeof(CkptHeader) + 15) & ~size_t(15);
+        for (int k = 0; k < kCkptSections; ++k) {
+            off[k] = o;
+            o += (sz[k] + 15) & ~size_t(15);
+        }
+        return o;
+    }
+    static constexpr char kCkptMagic[8] = {'D', 'I', 'O', 'C', 'K', 'P', 'T', '1'};
+
+   public:
+    int checkpoint(void* out, size_t cap, size_t* size) override {
+        if (!world_ready_) return state_err("no world uploaded");
+        DIO_TRY(pull_counters());
+        CkptHeader h;
+        std::memset(&h, 0, sizeof h);
+        std::memcpy(h.magic, kCkptMagic, 8);
+        h.version = 1;
+        h.precision = cfg_.precision;
+        h.p_bytes = sizeof(P);
+        h.r_bytes = sizeof(R);
+        h.n = w_.n;
+        h.n_joints = w_.n_joints;
+        h.n_scenes = (uint32_t)scenes_host_.size();
+        h.n_hull = n_hull_;
+        h.rows = steps_ ? std::min(hctr_->rows, cap_.max_contacts) : 0u;
+        h.pair_rows = std::min(steps_ ? hctr_->pair_rows : 0u, h.rows);
+        h.has_container = !scenes_host_.empty() && scenes_host_[0].has_container;
+        h.steps = steps_;
+        size_t off[kCkptSections];
+        h.total_bytes = ckpt_layout(h, off);
+        *size = h.total_bytes;
+        if (!out) return DIO_OK;
+        if (cap < h.total_bytes) return cap_err("checkpoint buffer smaller than the image");
+        char* b = static_cast<char*>(out);
+        std::memset(b, 0, h.total_bytes);
+        std::memcpy(b, &h, sizeof h);
+        DIO_TRY(download(reinterpret_cast<DioGpuBody*>(b + off[kCkBodies]),
+                         reinterpret_cast<DioBodyState*>(b + off[kCkState])));
+        if (h.n_joints)
+            DIO_CK(cudaMemcpyAsync(b + off[kCkJoints], joints_, (size_t)h.n_joints * sizeof(DioConstraint),
+                                   cudaMemcpyDeviceToHost, stream_));
+        if (h.n_scenes) std::memcpy(b + off[kCkScenes], scenes_host_.data(), h.n_scenes * sizeof(SceneDesc));
+        std::vector<A4<R>> hv(h.n_hull);
+        if (h.n_hull)
+            DIO_CK(cudaMemcpyAsync(hv.data(), hull_, hv.size() * sizeof(A4<R>), cudaMemcpyDeviceToHost, stream_));
+        const size_t a4 = (size_t)h.n * sizeof(A4<P>);
+        A4<P>* src[5] = {w_.pos[0], w_.rot[0], w_.vel, w_.ang, w_.prev_vel};
+        for (int k = 0; k < 5; ++k)
+            if (a4) DIO_CK(cudaMemcpyAsync(b + off[kCkPos + k], src[k], a4, cudaMemcpyDeviceToHost, stream_));
+        const int pb = 1 - cur_;  // the last step's rows
+        if (h.rows) {
+            DIO_CK(cudaMemcpyAsync(b + off[kCkRowStatic], rs_[pb], (size_t)h.rows * sizeof(RowStatic<R>),
+                                   cudaMemcpyDeviceToHost, stream_));
+            DIO_CK(cudaMemcpyAsync(b + off[kCkRowDual], rd_[pb], (size_t)h.rows * sizeof(RowDual<P, R>),
+                                   cudaMemcpyDeviceToHost, stream_));
+            DIO_CK(cudaMemcpyAsync(b + off[kCkRowAb], ab_[pb], (size_t)h.rows * sizeof(uint2), cudaMemcpyDeviceToHost,
+                                   stream_));
+        }
+        DIO_CK(cudaStreamSynchronize(stream_));
+        float* hf = reinterpret_cast<float*>(b + off[kCkHull]);
+        for (uint32_t i = 0; i < h.n_hull; ++i) {
+            hf[4 * i] = float(hv[i].x);
+            hf[4 * i + 1] = float(hv[i].y);
+            hf[4 * i + 2] = float(hv[i].z);
+            hf[4 * i + 3] = 0.f;
+        }
+        return DIO_OK;
+    }
+    int resume(const void* in, size_t size) override {
+        CkptHeader h;
+        if (size < sizeof h) return inval("checkpoint image too small");
+        std::memcpy(&h, in, sizeof h);
+        if (std::memcmp(h.magic, kCkptMagic, 8) || h.version != 1) return inval("not a checkpoint image");
+        if (h.precision != cfg_.precision || h.p_bytes != sizeof(P) || h.r_bytes != sizeof(R))
+            return inval("checkpoint precision differs from the context's");
+        size_t off[kCkptSections];
+        if (ckpt_layout(h, off) != h.total_bytes || size < h.total_bytes) return inval("truncated checkpoint image");
+        if (h.rows > cap_.max_contacts) return cap_err("checkpoint rows exceed the context's contact capacity");
+        if (h.pair_rows > h.rows || !h.n_scenes) return inval("inconsistent checkpoint header");
+        const char* b = static_cast<const char*>(in);
+        std::vector<SceneDesc> sd(h.n_scenes);
+        std::memcpy(sd.data(), b + off[kCkScenes], h.n_scenes * sizeof(SceneDesc));
+        std::vector<uint32_t> offs(h.n_scenes + 1);
+        std::vector<DioContainer> conts(h.n_scenes);
+        for (uint32_t s = 0; s < h.n_scenes; ++s) {
+            if (sd[s].body_lo != (s ? sd[s - 1].body_hi : 0u) || sd[s].body_hi < sd[s].body_lo)
+                return inval("checkpoint scene table is not a partition of the bodies");
+            offs[s] = sd[s].body_lo;
+            std::memcpy(conts[s].center, sd[s].center, 12);
+            conts[s].half_extent = sd[s].half_extent;
+            std::memcpy(conts[s].rotation, sd[s].rotation, 16);
+        }
+        offs[h.n_scenes] = sd[h.n_scenes - 1].body_hi;
+        if (offs[h.n_scenes] != h.n) return inval("checkpoint scene table is not a partition of the bodies");
+        DioWorldDesc d;
+        std::memset(&d, 0, sizeof d);
+        d.n_bodies = h.n;
+        d.n_constraints = h.n_joints;
+        d.n_scenes = h.n_scenes;
+        d.n_hull_vertices = h.n_hull;
+        d.bodies = reinterpret_cast<const DioGpuBody*>(b + off[kCkBodies]);
+        d.state = reinterpret_cast<const DioBodyState*>(b + off[kCkState]);
+        d.constraints = h.n_joints ? reinterpret_cast<const DioConstraint*>(b + off[kCkJoints]) : nullptr;
+        d.scene_offsets = offs.data();
+        d.containers = h.has_container ? conts.data() : nullptr;
+        d.hull_vertices = h.n_hull ? reinterpret_cast<const float*>(b + off[kCkHull]) : nullptr;
+        DIO_TRY(world_upload(&d));
+        // the dynamic state in this world's precision, over the FP32 poses
+        const size_t a4 = (size_t)h.n * sizeof(A4<P>);
+        A4<P>* dst[5] = {w_.pos[0], w_.rot[0], w_.vel, w_.ang, w_.prev_vel};
+        for (int k = 0; k < 5; ++k)
+            if (a4) DIO_CK(cudaMemcpyAsync(dst[k], b + off[kCkPos + k], a4, cudaMemcpyHostToDevice, stream_));
+        // the last step's rows: the next step's warm-start source
+        const int pb = 1 - cur_;
+        if (h.rows) {
+            DIO_CK(cudaMemcpyAsync(rs_[pb], b + off[kCkRowStatic], (size_t)h.rows * sizeof(RowStatic<R>),
+                                   cudaMemcpyHostToDevice, stream_));
+            DIO_CK(cudaMemcpyAsync(rd_[pb], b + off[kCkRowDual], (size_t)h.rows * sizeof(RowDual<P, R>),
+                                   cudaMemcpyHostToDevice, stream_));
+            DIO_CK(cudaMemcpyAsync(ab_[pb], b + off[kCkRowAb], (size_t)h.rows * sizeof(uint2), cudaMemcpyHostToDevice,
+                                   stream_));
+        }
+        k_set_u32<<<1, 1, 0, stream_>>>(&ctr_->rows, h.rows);
+        k_set_u32<<<1, 1, 0, stream_>>>(&ctr_->pair_rows, h.pair_rows);
+        n_prev_rows_ = h.rows;
+        steps_ = h.steps;
+        DIO_CK(cudaStreamSynchronize(stream_));
+        return check_flags();
+    }
+
     int world_sizes(uint32_t* n, uint32_t* n_dyn, uint32_t* n_joints, uint32_t* n_scenes) override {
         *n = w_.n;
         *n_dyn = w_.n_dyn;
@@ -1700,36 +1850,6 @@ class Engine final : public EngineBase {
     }
     uint64_t launches_per_step_ = 0;
 
-    int step_once(const DioAvbdOptions& opt) {
-        uint32_t n = w_.n;
-        PrepParams<R> pp = opts_prep(opt);
-        set_rows(cur_);
-        DIO_CK(cudaMemsetAsync(ctr_, 0, offsetof(Counters, error_flags), stream_));
-        cudaEvent_t e = span_begin();
-        if (n) DIO_TRY(run_broad(0, n));
-        span_end(e, 2);
-        e = span_begin();
-        DIO_TRY(run_narrow(cap_.max_pairs, &ctr_->pairs));
-        span_end(e, 3);
-        // pair-row groups are the pairs (bounded by the device pair count)
-        e = span_begin();
-        DIO_TRY(build_rows(pp, cap_.max_pairs, cfg_.contacts_per_pair, &ctr_->pairs, n));
-        DIO_TRY(pull_counters());
-        if (hctr_->error_flags) DIO_TRY(check_flags());
-        uint32_t M = hctr_->rows;
-        DIO_TRY(finish_rows(pp, M, n));
-        span_end(e, 4);
-        SolveParams<R> so = solve_params(opt.dt, opt.gravity, opt.alpha, opt.beta_lin, opt.penalty_max, opt.iterations);
-        e = span_begin();
-        DIO_TRY(solve(so, n, M));
-        span_end(e, 5);
-        n_prev_rows_ = M;
-        cur_ = 1 - cur_;
-        set_rows(cur_);
-        ++steps_;
-        return DIO_OK;
-    }
-
     DioCapacity cap_;
     cudaStream_t stream_;
     DioConfig cfg_;
@@ -1778,6 +1898,7 @@ class Engine final : public EngineBase {
     size_t stage_bytes_ = 0;
     int cur_ = 0;
     uint32_t n_prev_rows_ = 0;
+    uint32_t n_hull_ = 0;  // hull vertices of the uploaded world
     uint32_t api_bodies_ = 0, api_n_ = 0, api_m_ = 0, api_iters_ = 0, last_np_ = 0;
     uint64_t steps_ = 0;
     bool world_ready_ = false;

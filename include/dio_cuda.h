@@ -386,6 +386,20 @@ int dio_world_colors(DioCtx* ctx, uint32_t* out, uint32_t cap, uint32_t* n);
 int dio_world_stats(DioCtx* ctx, DioStepStats* out);
 /* Reset the kernel timers and launch counter of the world (extension). */
 int dio_world_reset_timers(DioCtx* ctx);
+/* Checkpoint (extension; no reference counterpart -- the reference's state
+ * round trip is sync_bodies_from_gpu, engine/src/physics/gpu.rs:212-237,
+ * which drops the warm-start rows and the FP64 poses).  Serialises the world
+ * into a versioned byte image: bodies and shapes, state, joints, scene table
+ * with containers, hull vertices, the poses / velocities in the world's own
+ * precision and the last step's rows with their lambda / penalty (the next
+ * warm start's source).  With buffer == NULL only *size is set; a capacity
+ * below the image size returns DIO_ERR_CAPACITY. */
+int dio_world_checkpoint(DioCtx* ctx, void* buffer, size_t capacity, size_t* size);
+/* Resume a checkpoint into this context (same precision, enough capacity):
+ * the world is uploaded from the image and its dynamic state and warm-start
+ * rows restored, so stepping continues bit for bit as the checkpointed world
+ * would have.  A damaged or foreign image returns DIO_ERR_INVALID. */
+int dio_world_resume(DioCtx* ctx, const void* buffer, size_t size);
 /* Autotuner (extension): times the primal launch-shape variants and the
  * LBVH rebuild period on the uploaded world (trial_steps timed steps per
  * candidate, starting from a device snapshot that is restored afterwards,

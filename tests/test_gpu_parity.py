@@ -202,6 +202,47 @@ def test_set_state_that_changes_dynamic_bodies_rebuilds_the_list():
         w.set_state(None, w.download()[1])
 
 
+@pytest.mark.parametrize("precision", [abi.PREC_F32, abi.PREC_SPLIT, abi.PREC_F64])
+def test_checkpoint_resume_continues_bit_for_bit(precision):
+    """A world checkpointed after 7 steps and resumed in another context steps
+    on to the same bits -- poses, state, FP64 poses and the contact rows with
+    their lambda / penalty -- as the world that was never interrupted (joints,
+    hulls, containers, several scenes)."""
+    parts = [scenes.pyramid(levels=3), scenes.constraints_demo(), scenes.mixed_pile(n=300, extent=5.0)]
+    for p in parts:
+        p.options = parts[0].options
+    sc = scenes.pack(parts)
+    with _world(sc, precision=precision) as w:
+        w.step(sc.options, 7)
+        img = w.checkpoint()
+        w.step(sc.options, 9)
+        ref_b, ref_s = w.download()
+        ref_p, ref_q = w.download_f64()
+        ref_c = w.contacts()
+    h = compute.checkpoint_header(img)
+    assert h["magic"] == b"DIOCKPT1" and h["version"] == 1 and h["precision"] == precision
+    assert (h["n"], h["n_joints"], h["n_scenes"], h["steps"]) == (sc.n, len(sc.constraints), sc.n_scenes, 7)
+    assert h["n_hull"] == len(sc.hull_vertices) and h["total_bytes"] == len(img) and h["rows"] > 0
+    cap = compute.capacity(sc.n, max_pairs=max(64, 40 * sc.n), max_contacts=max(256, 200 * sc.n),
+                           max_joints=max(1, len(sc.constraints)), max_scenes=sc.n_scenes,
+                           max_hull_vertices=len(sc.hull_vertices))
+    with compute.World(cap, precision=precision) as w2:
+        w2.resume(img)
+        w2.step(sc.options, 9)
+        gb, gs = w2.download()
+        gp, gq = w2.download_f64()
+        gc = w2.contacts()
+        bad = bytearray(img)
+        bad[:8] = b"NOTACKPT"
+        with pytest.raises(abi.DioError):
+            w2.resume(bytes(bad))
+        with pytest.raises(abi.DioError):
+            w2.resume(img[: len(img) // 2])
+    assert np.array_equal(_bits(gb), _bits(ref_b)) and np.array_equal(_bits(gs), _bits(ref_s))
+    assert np.array_equal(gp, ref_p) and np.array_equal(gq, ref_q)
+    assert np.array_equal(_bits(gc), _bits(ref_c))
+
+
 def test_batched_world_equals_each_scene_alone():
     parts = [scenes.pyramid(levels=3), scenes.constraints_demo(), scenes.box_demo(),
              scenes.cube_field(nx=3, nz=3, ny=2)]
