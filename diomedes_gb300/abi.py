@@ -33,6 +33,7 @@ CKPT_HEADER = np.dtype([("magic", "S8"), ("version", "<u4"), ("precision", "<u4"
                         ("n_hull", "<u4"), ("rows", "<u4"), ("pair_rows", "<u4"), ("has_container", "<u4"),
                         ("pad", "<u4"), ("steps", "<u8"), ("total_bytes", "<u8")])
 PRIMAL_VARIANTS = 10  # DIO_PRIMAL_VARIANTS
+XFORM_POSE, XFORM_MAT4 = 0, 1  # DIO_XFORM_*
 
 SOLVER_JACOBI, SOLVER_COLORED = 0, 1
 PREC_F32, PREC_SPLIT, PREC_F64 = 0, 1, 2
@@ -146,6 +147,9 @@ _PROTOS = {
     "dio_world_colors": [_P, _vp, _u32, ctypes.POINTER(_u32)],
     "dio_world_stats": [_P, ctypes.POINTER(StepStats)],
     "dio_world_reset_timers": [_P],
+    "dio_world_export_transforms": [_P, _u32, _vp, _vp, ctypes.c_size_t],
+    "dio_step_async": [_P, ctypes.POINTER(AvbdOptions), _u32],
+    "dio_world_download_async": [_P, _vp, _vp],
     "dio_world_checkpoint": [_P, _vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)],
     "dio_world_resume": [_P, _vp, ctypes.c_size_t],
     "dio_autotune": [_P, ctypes.POINTER(AvbdOptions), _u32, ctypes.c_char_p, ctypes.POINTER(Config)],

@@ -241,6 +241,14 @@ class World(Context):
     def step(self, options, steps=1):
         check(self.L.dio_step(self.h, ctypes.byref(options), steps), self.h, "dio_step")
 
+    def step_async(self, options, steps=1):
+        """Enqueue steps without waiting; errors surface at synchronize()."""
+        check(self.L.dio_step_async(self.h, ctypes.byref(options), steps), self.h, "dio_step_async")
+
+    def download_async(self, bodies, state):
+        """Enqueue the copy of poses / state into caller buffers (pinned for overlap)."""
+        check(self.L.dio_world_download_async(self.h, ptr(bodies), ptr(state)), self.h, "download_async")
+
     def set_stream(self, cuda_stream_handle):
         check(self.L.dio_ctx_set_stream(self.h, cuda_stream_handle), self.h, "set_stream")
 
@@ -296,6 +304,11 @@ class World(Context):
 
     def reset_timers(self):
         check(self.L.dio_world_reset_timers(self.h), self.h, "reset_timers")
+
+    def export_transforms(self, out_ptr, stride, fmt=abi.XFORM_POSE, scales_ptr=None):
+        """Write every body's transform into a device buffer (stream-ordered)."""
+        check(self.L.dio_world_export_transforms(self.h, fmt, scales_ptr, out_ptr, stride), self.h,
+              "export_transforms")
 
     def checkpoint(self):
         """The world as a versioned byte image (dio_world_checkpoint)."""

@@ -202,7 +202,9 @@ int dio_ctx_set_stream(DioCtx* ctx, void* cuda_stream) {
 int dio_ctx_synchronize(DioCtx* ctx) {
     if (!ctx) return DIO_ERR_INVALID;
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
-    return e == cudaSuccess ? DIO_OK : fail(ctx, DIO_ERR_CUDA, cudaGetErrorString(e));
+    if (e != cudaSuccess) return fail(ctx, DIO_ERR_CUDA, cudaGetErrorString(e));
+    if (!ctx->world) return DIO_OK;
+    return with_world(ctx, false, [&](dio::EngineBase* w) { return w->sync_check(); });
 }
 
 int dio_broad_submit(DioCtx* ctx, const DioGpuBody* bodies, uint32_t n) {
@@ -258,6 +260,12 @@ int dio_world_upload(DioCtx* ctx, const DioWorldDesc* desc) {
 int dio_step(DioCtx* ctx, const DioAvbdOptions* options, uint32_t steps) {
     return with_world(ctx, false, [&](dio::EngineBase* e) { return e->step(options, steps); });
 }
+int dio_step_async(DioCtx* ctx, const DioAvbdOptions* options, uint32_t steps) {
+    return with_world(ctx, false, [&](dio::EngineBase* e) { return e->step_async(options, steps); });
+}
+int dio_world_download_async(DioCtx* ctx, DioGpuBody* bodies, DioBodyState* state) {
+    return with_world(ctx, false, [&](dio::EngineBase* e) { return e->download_async(bodies, state); });
+}
 int dio_world_set_state(DioCtx* ctx, const DioGpuBody* bodies, const DioBodyState* state) {
     return with_world(ctx, false, [&](dio::EngineBase* e) { return e->set_state(bodies, state); });
 }
@@ -278,6 +286,11 @@ int dio_world_stats(DioCtx* ctx, DioStepStats* out) {
 }
 int dio_world_reset_timers(DioCtx* ctx) {
     return with_world(ctx, false, [&](dio::EngineBase* e) { return e->reset_timers(); });
+}
+int dio_world_export_transforms(DioCtx* ctx, uint32_t format, const float* scales, void* out,
+                                size_t stride_bytes) {
+    return with_world(ctx, false,
+                      [&](dio::EngineBase* e) { return e->export_transforms(format, scales, out, stride_bytes); });
 }
 int dio_world_checkpoint(DioCtx* ctx, void* buffer, size_t capacity, size_t* size) {
     if (!size) return DIO_ERR_INVALID;

@@ -35,6 +35,9 @@ struct EngineBase {
     // fused world
     virtual int world_upload(const DioWorldDesc* desc) = 0;
     virtual int step(const DioAvbdOptions* options, uint32_t steps) = 0;
+    virtual int step_async(const DioAvbdOptions* options, uint32_t steps) = 0;
+    virtual int download_async(DioGpuBody* bodies, DioBodyState* state) = 0;
+    virtual int sync_check() = 0;  // synchronise and report the device error flags
     virtual int set_state(const DioGpuBody* bodies, const DioBodyState* state) = 0;
     virtual int download(DioGpuBody* bodies, DioBodyState* state) = 0;
     virtual int download_f64(double* positions, double* orientations) = 0;
@@ -46,6 +49,7 @@ struct EngineBase {
     // counters) and its restoration; used by the autotuner's trials
     virtual int snapshot() = 0;
     virtual int restore() = 0;
+    virtual int export_transforms(uint32_t format, const float* scales, void* out, size_t stride) = 0;
     // host byte image of the whole world for checkpoint / resume
     virtual int checkpoint(void* out, size_t cap, size_t* size) = 0;
     virtual int resume(const void* in, size_t size) = 0;

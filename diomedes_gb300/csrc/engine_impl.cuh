@@ -180,6 +180,35 @@ static __global__ void k_csr_other(const uint32_t* off, const uint32_t* idx, con
     }
 }
 
+// Per-body transform records for a renderer (dio_world_export_transforms).
+// The matrix is the standard unit-quaternion rotation (columns
+// (1-2(y^2+z^2), 2(xy+wz), 2(xz-wy)), ...) scaled per body and translated,
+// the same construction as Mat4::from_scale_rotation_translation.
+template <class P, class R>
+__global__ void k_export_xform(const A4<P>* pos, const A4<P>* rot, uint32_t n, uint32_t format, const float* scales,
+                               char* out, size_t stride) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const A4<P> p = pos[i], q = rot[i];
+        const float px = float(p.x), py = float(p.y), pz = float(p.z);
+        const float x = float(q.x), y = float(q.y), z = float(q.z), w = float(q.w);
+        float4* o = reinterpret_cast<float4*>(out + (size_t)i * stride);
+        if (format == DIO_XFORM_POSE) {
+            o[0] = make_float4(px, py, pz, 0.f);
+            o[1] = make_float4(x, y, z, w);
+            continue;
+        }
+        const float s = scales ? scales[i] : 1.f;
+        const float x2 = x + x, y2 = y + y, z2 = z + z;
+        const float xx = x * x2, xy = x * y2, xz = x * z2;
+        const float yy = y * y2, yz = y * z2, zz = z * z2;
+        const float wx = w * x2, wy = w * y2, wz = w * z2;
+        o[0] = make_float4((1.f - (yy + zz)) * s, (xy + wz) * s, (xz - wy) * s, 0.f);
+        o[1] = make_float4((xy - wz) * s, (1.f - (xx + zz)) * s, (yz + wx) * s, 0.f);
+        o[2] = make_float4((xz + wy) * s, (yz - wx) * s, (1.f - (xx + yy)) * s, 0.f);
+        o[3] = make_float4(px, py, pz, 1.f);
+    }
+}
+
 template <class P, class R>
 __global__ void k_pack_result(DevWorld<P, R> w, uint32_t n, int buf, float* pos3, float* quat4, float* vel,
                               float* ang, float* prev) {
@@ -827,6 +856,11 @@ class Engine final : public EngineBase {
     }
 
     int step(const DioAvbdOptions* options, uint32_t steps) override {
+        DIO_TRY(step_async(options, steps));
+        // one synchronisation per call: device-side error flags
+        return check_flags();
+    }
+    int step_async(const DioAvbdOptions* options, uint32_t steps) override {
         if (!options) return inval("null options");
         if (!world_ready_) return state_err("no world uploaded");
         for (uint32_t k = 0; k < steps; ++k) {
@@ -837,9 +871,9 @@ class Engine final : public EngineBase {
             else
                 DIO_TRY(step_once_dev(*options));
         }
-        // one synchronisation per call: device-side error flags
-        return check_flags();
+        return DIO_OK;
     }
+    int sync_check() override { return check_flags(); }
 
     int set_state(const DioGpuBody* bodies, const DioBodyState* state) override {
         if (!world_ready_) return state_err("no world uploaded");
@@ -858,6 +892,11 @@ class Engine final : public EngineBase {
     }
 
     int download(DioGpuBody* bodies, DioBodyState* state) override {
+        DIO_TRY(download_async(bodies, state));
+        DIO_CK(cudaStreamSynchronize(stream_));
+        return DIO_OK;
+    }
+    int download_async(DioGpuBody* bodies, DioBodyState* state) override {
         if (!world_ready_) return state_err("no world uploaded");
         uint32_t n = w_.n;
         if (!n) return DIO_OK;
@@ -868,7 +907,6 @@ class Engine final : public EngineBase {
                                                                   nullptr, nullptr);
         if (bodies) DIO_CK(cudaMemcpyAsync(bodies, db, (size_t)n * sizeof(DioGpuBody), cudaMemcpyDeviceToHost, stream_));
         if (state) DIO_CK(cudaMemcpyAsync(state, ds, (size_t)n * sizeof(DioBodyState), cudaMemcpyDeviceToHost, stream_));
-        DIO_CK(cudaStreamSynchronize(stream_));
         return DIO_OK;
     }
 
@@ -1407,6 +1445,19 @@ class Engine final : public EngineBase {
         lbvh_valid_ = snap_valid_;
         return DIO_OK;
     }
+    int export_transforms(uint32_t format, const float* scales, void* out, size_t stride) override {
+        if (!world_ready_) return state_err("no world uploaded");
+        if (format != DIO_XFORM_POSE && format != DIO_XFORM_MAT4) return inval("unknown transform format");
+        const size_t rec = format == DIO_XFORM_POSE ? 32 : 64;
+        if (!out || stride < rec || stride % 16 || reinterpret_cast<uintptr_t>(out) % 16)
+            return inval("output must be 16-byte aligned with a stride of at least one record");
+        if (!w_.n) return DIO_OK;
+        k_export_xform<P, R><<<grid_for(w_.n, 256), 256, 0, stream_>>>(w_.pos[0], w_.rot[0], w_.n, format, scales,
+                                                                     static_cast<char*>(out), stride);
+        DIO_CK(cudaGetLastError());
+        return DIO_OK;
+    }
+
     // ------------------------------------------------------- checkpoint
     // Image: header, then 16-byte aligned sections in kCkptSections order.
     struct CkptHeader {

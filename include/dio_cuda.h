@@ -279,7 +279,7 @@ int dio_ctx_get_config(const DioCtx* ctx, DioConfig* out);
 /* Run work on a caller's cudaStream_t (NULL = the context's own stream). */
 int dio_ctx_set_stream(DioCtx* ctx, void* cuda_stream);
 /* Block until all work on the context's stream has finished. */
-int dio_ctx_synchronize(DioCtx* ctx);
+int dio_ctx_synchronize(DioCtx* ctx);  /* also reports deferred device error flags */
 
 /* ----------------------------------------------- broad + narrow phase */
 /* NarrowPhaseCompute::submit_broad, engine/src/render/compute.rs:490-567:
@@ -368,6 +368,17 @@ int dio_world_upload(DioCtx* ctx, const DioWorldDesc* desc);
  * one-frame contact lag).  Scenes are packed into the same launches; a
  * one-scene world per context is the plain one-scene-per-launch path. */
 int dio_step(DioCtx* ctx, const DioAvbdOptions* options, uint32_t steps);
+/* dio_step without the closing synchronisation (the async submit of the
+ * reference's frame loop, engine/src/render/gpu_physics.rs:435-561): the
+ * steps are enqueued on the context's stream and the call returns; device
+ * error flags are reported by the next synchronising call
+ * (dio_ctx_synchronize, dio_step, dio_world_download, dio_world_stats). */
+int dio_step_async(DioCtx* ctx, const DioAvbdOptions* options, uint32_t steps);
+/* dio_world_download enqueued without waiting (the double-buffered read of
+ * engine/src/render/compute.rs:160-165,423-425): the copies into the
+ * caller's buffers (page-locked for a truly asynchronous copy) complete in
+ * stream order; wait with dio_ctx_synchronize or an event on the stream. */
+int dio_world_download_async(DioCtx* ctx, DioGpuBody* bodies, DioBodyState* state);
 /* Per-frame pose/state upload of the demos (demos/avbd_box/src/main.rs:232-
  * 257): replace every body's pose (position, orientation) and state
  * (velocities, inverse mass/moment) from host arrays, keeping shapes, joints
@@ -386,6 +397,19 @@ int dio_world_colors(DioCtx* ctx, uint32_t* out, uint32_t cap, uint32_t* n);
 int dio_world_stats(DioCtx* ctx, DioStepStats* out);
 /* Reset the kernel timers and launch counter of the world (extension). */
 int dio_world_reset_timers(DioCtx* ctx);
+/* Headless transform export: every body's transform written, in body order
+ * and stream-ordered on the context's stream (no synchronisation), into a
+ * DEVICE buffer the caller owns -- e.g. a renderer's instance buffer.
+ * Replaces the per-instance host copy of demos/avbd_box/src/main.rs:276-280
+ * and the model matrices of engine/src/render/renderer.rs:251-255.
+ *   DIO_XFORM_POSE  32 B: float4 position (w = 0), float4 quaternion xyzw
+ *   DIO_XFORM_MAT4  64 B: column-major 4x4 model matrix = translation *
+ *                   rotation * scale (Mat4::from_scale_rotation_translation)
+ * `scales` (device, one float per body, uniform scale) may be NULL (1).
+ * `out` and `stride_bytes` must be multiples of 16, stride >= the record. */
+enum { DIO_XFORM_POSE = 0, DIO_XFORM_MAT4 = 1 };
+int dio_world_export_transforms(DioCtx* ctx, uint32_t format, const float* scales, void* out,
+                                size_t stride_bytes);
 /* Checkpoint (extension; no reference counterpart -- the reference's state
  * round trip is sync_bodies_from_gpu, engine/src/physics/gpu.rs:212-237,
  * which drops the warm-start rows and the FP64 poses).  Serialises the world

@@ -74,6 +74,8 @@ def test_header_constants_match_the_python_mirror():
         text = f.read()
     m = re.search(r"#define DIO_PRIMAL_VARIANTS (\d+)", text)
     assert m and int(m.group(1)) == abi.PRIMAL_VARIANTS
+    m = re.search(r"DIO_XFORM_POSE = (\d+), DIO_XFORM_MAT4 = (\d+)", text)
+    assert m and (int(m.group(1)), int(m.group(2))) == (abi.XFORM_POSE, abi.XFORM_MAT4)
     for name in ("DIO_OK", "DIO_ERR_INVALID", "DIO_ERR_CAPACITY", "DIO_ERR_TIMEOUT", "DIO_ERR_CUDA",
                  "DIO_ERR_NONFINITE", "DIO_ERR_STATE"):
         m = re.search(name + r"\s*=\s*(\d+)", text)

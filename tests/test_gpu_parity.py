@@ -202,6 +202,83 @@ def test_set_state_that_changes_dynamic_bodies_rebuilds_the_list():
         w.set_state(None, w.download()[1])
 
 
+def test_pipelined_frames_match_synchronous_steps():
+    """A frame loop of dio_step_async + dio_world_download_async into two
+    alternating page-locked buffers (read frame t-1 while t computes) yields
+    the same per-frame states as synchronous stepping; a device error raised
+    by an asynchronous step is reported by the next synchronisation."""
+    torch = pytest.importorskip("torch")
+    sc = scenes.constraints_demo()
+    frames = 6
+    ref = []
+    with _world(sc) as w:
+        for _ in range(frames):
+            w.step(sc.options, 1)
+            ref.append(w.download())
+
+    def pinned(dt):
+        return torch.empty(sc.n * dt.itemsize, dtype=torch.uint8, pin_memory=True).numpy().view(dt)
+
+    bufs = [(pinned(abi.BODY), pinned(abi.BODY_STATE)) for _ in range(2)]
+    seen = []
+    with _world(sc) as w:
+        for t in range(frames):
+            w.step_async(sc.options, 1)
+            w.download_async(*bufs[t % 2])
+            if t:
+                w.synchronize()  # frame t-1's buffer is complete (and t's, here)
+                seen.append((bufs[(t - 1) % 2][0].copy(), bufs[(t - 1) % 2][1].copy()))
+        w.synchronize()
+        seen.append((bufs[(frames - 1) % 2][0].copy(), bufs[(frames - 1) % 2][1].copy()))
+        for (gb, gs), (rb, rs) in zip(seen, ref):
+            assert np.array_equal(_bits(gb), _bits(rb)) and np.array_equal(_bits(gs), _bits(rs))
+        b, s = w.download()
+        bad = s.copy()
+        bad["vel"][1, 0] = np.nan
+        w.set_state(None, bad)
+        w.step_async(sc.options, 1)  # returns without waiting
+        with pytest.raises(abi.DioError) as e:
+            w.synchronize()
+        assert e.value.status == abi.DIO_ERR_NONFINITE
+
+
+def test_transform_export_matches_the_poses():
+    """Headless transform export into a device buffer: pose records are the
+    downloaded poses; model matrices are translation * rotation * scale built
+    from them (float32 restatement, bit for bit); a misaligned buffer is
+    rejected."""
+    torch = pytest.importorskip("torch")
+    sc = scenes.mixed_pile(n=400, extent=5.0)
+    with _world(sc) as w:
+        w.step(sc.options, 5)
+        b, _ = w.download()
+        pose = torch.zeros((sc.n, 8), dtype=torch.float32, device="cuda")
+        w.export_transforms(pose.data_ptr(), 32, abi.XFORM_POSE)
+        scales = torch.linspace(0.5, 2.0, sc.n, dtype=torch.float32, device="cuda")
+        mats = torch.zeros((sc.n, 20), dtype=torch.float32, device="cuda")  # 80-byte stride
+        w.export_transforms(mats.data_ptr(), 80, abi.XFORM_MAT4, scales.data_ptr())
+        torch.cuda.synchronize()
+        with pytest.raises(abi.DioError):
+            w.export_transforms(pose.data_ptr() + 4, 32, abi.XFORM_POSE)
+        with pytest.raises(abi.DioError):
+            w.export_transforms(pose.data_ptr(), 16, abi.XFORM_POSE)
+        pose, mats, s = pose.cpu().numpy(), mats.cpu().numpy()[:, :16], scales.cpu().numpy()
+    assert np.array_equal(pose[:, :3], b["position"][:, :3]) and not pose[:, 3].any()
+    assert np.array_equal(pose[:, 4:], b["orientation"])
+    f = np.float32
+    x, y, z, w_ = (b["orientation"][:, k].astype(f) for k in range(4))
+    x2, y2, z2 = x + x, y + y, z + z
+    xx, xy, xz, yy, yz, zz = x * x2, x * y2, x * z2, y * y2, y * z2, z * z2
+    wx, wy, wz = w_ * x2, w_ * y2, w_ * z2
+    one, zero = f(1), np.zeros_like(x)
+    cols = [((one - (yy + zz)) * s, (xy + wz) * s, (xz - wy) * s, zero),
+            ((xy - wz) * s, (one - (xx + zz)) * s, (yz + wx) * s, zero),
+            ((xz + wy) * s, (yz - wx) * s, (one - (xx + yy)) * s, zero),
+            (b["position"][:, 0], b["position"][:, 1], b["position"][:, 2], np.ones_like(x))]
+    want = np.stack([c for col in cols for c in col], axis=1).astype(f)
+    assert np.array_equal(mats, want)
+
+
 @pytest.mark.parametrize("precision", [abi.PREC_F32, abi.PREC_SPLIT, abi.PREC_F64])
 def test_checkpoint_resume_continues_bit_for_bit(precision):
     """A world checkpointed after 7 steps and resumed in another context steps
