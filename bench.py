@@ -74,7 +74,7 @@ class Clocks:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except OSError:
@@ -233,7 +233,7 @@ def main():
     else:
         tuned = w.autotune(o, trial_steps=4)  # launch shape + LBVH rebuild period; state restored
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    # the clock sampler starts with the warm-up so that its 200 ms samples
+    # the clock sampler starts with the warm-up so that its 50 ms samples
     # cover the (sub-second) timed region
     with Clocks(local) as clk:
         w.step(o, args.warmup)
