@@ -122,39 +122,52 @@ __device__ __forceinline__ void support_face(const NB<R>& b, V3<R> outward, V3<R
 template <class P, class R>
 __device__ __forceinline__ uint32_t container_rows(const DevWorld<P, R>& w, uint32_t i, const SceneDesc& sc,
                                                    const PrepParams<R>& o, bool write_out, uint32_t r) {
-    NB<R> b = load_nb(w, i);
     const A4<R>* walls = w.walls + 6 * (size_t)w.scene[i];
     V3<R> vel = cast3<R>(xyz(w.vel[i]));
-    const bool boxy = b.shape.tag == DIO_SHAPE_CUBE || b.shape.tag == DIO_SHAPE_BOX;
     // Quick reject: every support point lies within an L1 bounding radius of
     // the body centre, so when the centre plus that radius plus this step's
     // travel is (with rounding slack) inside a wall, that wall has no row
-    // with depth > 0 -- the same empty set the full test produces.
+    // with depth > 0 -- the same empty set the full test produces.  The
+    // bound needs only the shape's tag and first corner and the position, so
+    // the orientation and the rest of the shape are read only for a body
+    // that can reach a wall.
+    const uint32_t tag = reinterpret_cast<const uint4*>(&w.shape[i])->x;
+    const float4 c0 = reinterpret_cast<const float4*>(w.shape[i].corners)[0];
+    V3<P> org{P(0), P(0), P(0)};
+    if (w.origin) org = xyz(w.origin[w.scene[i]]);
+    const V3<R> pos = cast3<R>(sub(xyz(w.pos[0][i]), org));  // as load_nb forms it
+    const bool boxy = tag == DIO_SHAPE_CUBE || tag == DIO_SHAPE_BOX;
     R rbound = R(-1);
     if (boxy) {
-        rbound = dabs(b.shape.c[0].x) + dabs(b.shape.c[0].y) + dabs(b.shape.c[0].z);
-    } else if (b.shape.tag == DIO_SHAPE_SPHERE) {
-        rbound = dabs(b.shape.c[0].x);
-    } else if (b.shape.tag == DIO_SHAPE_TETRAHEDRON) {
+        rbound = dabs(R(c0.x)) + dabs(R(c0.y)) + dabs(R(c0.z));
+    } else if (tag == DIO_SHAPE_SPHERE) {
+        rbound = dabs(R(c0.x));
+    } else if (tag == DIO_SHAPE_TETRAHEDRON) {
+        const ShapeR<R> sh = load_shape<R>(&w.shape[i]);
         rbound = R(0);
         for (int k = 0; k < 4; ++k)
-            rbound = fmax_(rbound, dabs(b.shape.c[k].x) + dabs(b.shape.c[k].y) + dabs(b.shape.c[k].z));
+            rbound = fmax_(rbound, dabs(sh.c[k].x) + dabs(sh.c[k].y) + dabs(sh.c[k].z));
     }
-    // The bound is applied per wall: a wall that no support point can reach
-    // this step yields no row, so it is skipped (the other walls, and every
-    // wall of a body without a bound, take the full test).
     const R travel = rbound >= R(0) ? length(vel) * o.dt : R(0);
+    uint32_t reach = 0x3Fu;  // walls a support point may reach this step
+    if (rbound >= R(0)) {
+        reach = 0;
+        for (int k = 0; k < 6; ++k) {
+            const A4<R> wall = walls[k];
+            const R d = dot(pos, xyz(wall));
+            const R slack = R(1e-4) * (R(1) + dabs(wall.w) + dabs(d));
+            if (!(d + rbound + travel + slack < wall.w)) reach |= 1u << k;
+        }
+    }
+    if (!reach) return 0;
+    NB<R> b = load_nb(w, i);
     uint32_t count = 0;
 #pragma unroll 1
     for (int k = 0; k < 6; ++k) {
+        if (!((reach >> k) & 1u)) continue;
         const A4<R> wall = walls[k];
         const V3<R> outward = xyz(wall);
         const R plane = wall.w;
-        if (rbound >= R(0)) {
-            const R d = dot(b.pos, outward);
-            const R slack = R(1e-4) * (R(1) + dabs(plane) + dabs(d));
-            if (d + rbound + travel + slack < plane) continue;
-        }
         V3<R> pts[4];
         uint32_t np;
         if (boxy) {
