@@ -27,11 +27,13 @@ SPRING, ROD, BALL_SOCKET, ROPE = 0, 1, 2, 3
 CONTACTS_PER_PAIR = 4
 # header of a dio_world_checkpoint image (16-byte aligned sections follow:
 # bodies, state, joints, scene table, hull vertices, poses / velocities in
-# the world's precision, the last step's rows)
+# the world's precision, the last step's rows, the last step's narrow slots
+# of a contact-lag world)
 CKPT_HEADER = np.dtype([("magic", "S8"), ("version", "<u4"), ("precision", "<u4"), ("p_bytes", "<u4"),
                         ("r_bytes", "<u4"), ("n", "<u4"), ("n_joints", "<u4"), ("n_scenes", "<u4"),
                         ("n_hull", "<u4"), ("rows", "<u4"), ("pair_rows", "<u4"), ("has_container", "<u4"),
-                        ("pad", "<u4"), ("steps", "<u8"), ("total_bytes", "<u8")])
+                        ("per_pair", "<u4"), ("lag_pairs", "<u4"), ("pad", "<u4"), ("steps", "<u8"),
+                        ("total_bytes", "<u8")])
 PRIMAL_VARIANTS = 10  # DIO_PRIMAL_VARIANTS
 XFORM_POSE, XFORM_MAT4 = 0, 1  # DIO_XFORM_*
 
@@ -94,7 +96,7 @@ class Config(ctypes.Structure):
     _fields_ = [("solver_mode", _u32), ("precision", _u32), ("contacts_per_pair", _u32),
                 ("use_graph", _u32), ("primal_variant", _u32), ("block_size", _u32),
                 ("batched_solver", _u32), ("profile", _u32), ("broad_phase", _u32),
-                ("bvh_rebuild_period", _u32), ("reserved", _u32 * 2)]
+                ("bvh_rebuild_period", _u32), ("contact_lag", _u32), ("reserved", _u32 * 1)]
 
 
 class WorldDesc(ctypes.Structure):

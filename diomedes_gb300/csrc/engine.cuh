@@ -58,7 +58,8 @@ struct Counters {
     uint32_t prev_pair_rows;  // of which from narrow-phase slots
     uint32_t long_count;      // CSR segments too long for the in-thread sort
     uint32_t dyn_changed;     // a state update turned a body static or dynamic
-    uint32_t pad[2];
+    uint32_t prev_pairs;      // pairs of the previous step (contact-lag rows)
+    uint32_t pad[1];
 };
 
 // Static part of one contact row (80 B at R = float):

@@ -436,6 +436,7 @@ class Engine final : public EngineBase {
         DIO_TRY(alloc(&w_.color_off, 1025));
         DIO_TRY(alloc(&w_.pairs, PP));
         DIO_TRY(alloc(&w_.slots, (size_t)PP * per_cap_));
+        slots_[0] = w_.slots;  // slots_[1]: allocated when contact_lag is first used
         DIO_TRY(alloc(&w_.gjk_list, PP));
         DIO_TRY(alloc(&w_.epa_list, PP));
         DIO_TRY(alloc(&w_.simplex, (size_t)PP * 8));
@@ -580,6 +581,8 @@ class Engine final : public EngineBase {
         cfg_ = c;
         if (c.contacts_per_pair != 4 && c.contacts_per_pair != 8) cfg_.contacts_per_pair = per;
         if (cfg_.contacts_per_pair > per_cap_) cfg_.contacts_per_pair = per_cap_;
+        // lagged rows need the previous step's slots in this layout
+        if (cfg_.contacts_per_pair != per || !cfg_.contact_lag) lag_primed_ = false;
     }
 
     // ------------------------------------------------ reference-mirror API
@@ -850,6 +853,7 @@ class Engine final : public EngineBase {
         DIO_TRY(upload_joints(d->constraints, d->n_constraints, n));
         n_prev_rows_ = 0;
         steps_ = 0;
+        lag_primed_ = false;
         world_ready_ = true;
         DIO_CK(cudaStreamSynchronize(stream_));
         return check_flags();
@@ -863,6 +867,17 @@ class Engine final : public EngineBase {
     int step_async(const DioAvbdOptions* options, uint32_t steps) override {
         if (!options) return inval("null options");
         if (!world_ready_) return state_err("no world uploaded");
+        if (cfg_.contact_lag) {
+            if (!slots_[1]) DIO_TRY(alloc(&slots_[1], (size_t)cap_.max_pairs * per_cap_));
+            if (!lag_primed_) {
+                // first lagged step: no previous detection (the roll at the
+                // step's start turns this count into the previous one)
+                k_set_u32<<<1, 1, 0, stream_>>>(&ctr_->pairs, 0u);
+                lag_primed_ = true;
+            }
+        } else {
+            lag_primed_ = false;
+        }
         for (uint32_t k = 0; k < steps; ++k) {
             if (cfg_.solver_mode == DIO_SOLVER_COLORED)
                 DIO_TRY(step_once_colored(*options));
@@ -1284,14 +1299,18 @@ class Engine final : public EngineBase {
     }
 
     // Rows from `groups` groups of `per` slots (+ container rows for bodies).
-    int build_rows(const PrepParams<R>& o, uint32_t groups, uint32_t per, const uint32_t* groups_dev, uint32_t n) {
+    // src: the narrow slots the pair rows come from (w_.slots, or the
+    // previous step's with contact_lag)
+    int build_rows(const PrepParams<R>& o, uint32_t groups, uint32_t per, const uint32_t* groups_dev, uint32_t n,
+                   const Slot<R>* src = nullptr) {
         uint32_t G = groups;
+        if (!src) src = w_.slots;
         if (G) {
-            k_slot_count<R><<<grid_for(G, 256), 256, 0, stream_>>>(w_.slots, per, groups_dev, G, counts_);
+            k_slot_count<R><<<grid_for(G, 256), 256, 0, stream_>>>(src, per, groups_dev, G, counts_);
             DIO_CK(cudaMemsetAsync(counts_ + G, 0, 4, stream_));
             size_t tb = cub_bytes_;
             DIO_CK(cub::DeviceScan::ExclusiveSum(cub_tmp_, tb, counts_, offsets_, (int)G + 1, stream_));
-            k_slot_rows<P, R><<<grid_for(G, 128), 128, 0, stream_>>>(w_, w_.slots, per, groups_dev, G, offsets_, o);
+            k_slot_rows<P, R><<<grid_for(G, 128), 128, 0, stream_>>>(w_, src, per, groups_dev, G, offsets_, o);
         } else {
             DIO_CK(cudaMemsetAsync(offsets_, 0, 4, stream_));
         }
@@ -1464,11 +1483,11 @@ class Engine final : public EngineBase {
         char magic[8];
         uint32_t version, precision, p_bytes, r_bytes;
         uint32_t n, n_joints, n_scenes, n_hull;
-        uint32_t rows, pair_rows, has_container, pad;
+        uint32_t rows, pair_rows, has_container, per_pair, lag_pairs, pad;
         uint64_t steps, total_bytes;
     };
     enum { kCkBodies, kCkState, kCkJoints, kCkScenes, kCkHull, kCkPos, kCkRot, kCkVel, kCkAng, kCkPrevVel,
-           kCkRowStatic, kCkRowDual, kCkRowAb, kCkptSections };
+           kCkRowStatic, kCkRowDual, kCkRowAb, kCkSlots, kCkptSections };
     static size_t ckpt_layout(const CkptHeader& h, size_t off[kCkptSections]) {
         const size_t a4 = (size_t)h.n * sizeof(A4<P>);
         const size_t sz[kCkptSections] = {(size_t)h.n * sizeof(DioGpuBody),     (size_t)h.n * sizeof(DioBodyState),
@@ -1476,7 +1495,8 @@ class Engine final : public EngineBase {
                                           (size_t)h.n_scenes * sizeof(SceneDesc), (size_t)h.n_hull * 16,
                                           a4, a4, a4, a4, a4,
                                           (size_t)h.rows * sizeof(RowStatic<R>),
-                                          (size_t)h.rows * sizeof(RowDual<P, R>), (size_t)h.rows * sizeof(uint2)};
+                                          (size_t)h.rows * sizeof(RowDual<P, R>), (size_t)h.rows * sizeof(uint2),
+                                          (size_t)h.lag_pairs * h.per_pair * sizeof(Slot<R>)};
         size_t o = (sizeof(CkptHeader) + 15) & ~size_t(15);
         for (int k = 0; k < kCkptSections; ++k) {
             off[k] = o;
@@ -1504,6 +1524,10 @@ class Engine final : public EngineBase {
         h.rows = steps_ ? std::min(hctr_->rows, cap_.max_contacts) : 0u;
         h.pair_rows = std::min(steps_ ? hctr_->pair_rows : 0u, h.rows);
         h.has_container = !scenes_host_.empty() && scenes_host_[0].has_container;
+        h.per_pair = cfg_.contacts_per_pair;
+        // a contact-lag world's next rows come from the last step's slots
+        const bool lagged = cfg_.contact_lag && slots_[1] && lag_primed_ && steps_;
+        h.lag_pairs = lagged ? std::min(hctr_->pairs, cap_.max_pairs) : 0u;
         h.steps = steps_;
         size_t off[kCkptSections];
         h.total_bytes = ckpt_layout(h, off);
@@ -1535,6 +1559,9 @@ class Engine final : public EngineBase {
             DIO_CK(cudaMemcpyAsync(b + off[kCkRowAb], ab_[pb], (size_t)h.rows * sizeof(uint2), cudaMemcpyDeviceToHost,
                                    stream_));
         }
+        if (h.lag_pairs)
+            DIO_CK(cudaMemcpyAsync(b + off[kCkSlots], slots_[pb], (size_t)h.lag_pairs * h.per_pair * sizeof(Slot<R>),
+                                   cudaMemcpyDeviceToHost, stream_));
         DIO_CK(cudaStreamSynchronize(stream_));
         float* hf = reinterpret_cast<float*>(b + off[kCkHull]);
         for (uint32_t i = 0; i < h.n_hull; ++i) {
@@ -1556,6 +1583,8 @@ class Engine final : public EngineBase {
         if (ckpt_layout(h, off) != h.total_bytes || size < h.total_bytes) return inval("truncated checkpoint image");
         if (h.rows > cap_.max_contacts) return cap_err("checkpoint rows exceed the context's contact capacity");
         if (h.pair_rows > h.rows || !h.n_scenes) return inval("inconsistent checkpoint header");
+        if (h.lag_pairs && (h.lag_pairs > cap_.max_pairs || h.per_pair != cfg_.contacts_per_pair || !cfg_.contact_lag))
+            return inval("a contact-lag checkpoint needs a contact-lag context with the same slots per pair");
         const char* b = static_cast<const char*>(in);
         std::vector<SceneDesc> sd(h.n_scenes);
         std::memcpy(sd.data(), b + off[kCkScenes], h.n_scenes * sizeof(SceneDesc));
@@ -1601,6 +1630,13 @@ class Engine final : public EngineBase {
         }
         k_set_u32<<<1, 1, 0, stream_>>>(&ctr_->rows, h.rows);
         k_set_u32<<<1, 1, 0, stream_>>>(&ctr_->pair_rows, h.pair_rows);
+        if (h.lag_pairs) {
+            if (!slots_[1]) DIO_TRY(alloc(&slots_[1], (size_t)cap_.max_pairs * per_cap_));
+            DIO_CK(cudaMemcpyAsync(slots_[pb], b + off[kCkSlots], (size_t)h.lag_pairs * h.per_pair * sizeof(Slot<R>),
+                                   cudaMemcpyHostToDevice, stream_));
+            k_set_u32<<<1, 1, 0, stream_>>>(&ctr_->pairs, h.lag_pairs);
+            lag_primed_ = true;
+        }
         n_prev_rows_ = h.rows;
         steps_ = h.steps;
         DIO_CK(cudaStreamSynchronize(stream_));
@@ -1660,10 +1696,20 @@ class Engine final : public EngineBase {
 
     // One step with every count kept on the device: no host synchronisation,
     // fixed launch shapes, so the whole step can be captured in a graph.
+    // the world step's narrow slots: one buffer, or with contact_lag this
+    // step's (written by the narrow phase) and the previous step's (read by
+    // the pair rows), alternating with the row buffers
+    void set_slots() { w_.slots = cfg_.contact_lag && slots_[1] ? slots_[cur_] : slots_[0]; }
+    int build_world_rows(const PrepParams<R>& pp, uint32_t n) {
+        if (cfg_.contact_lag && slots_[1])
+            return build_rows(pp, cap_.max_pairs, cfg_.contacts_per_pair, &ctr_->prev_pairs, n, slots_[1 - cur_]);
+        return build_rows(pp, cap_.max_pairs, cfg_.contacts_per_pair, &ctr_->pairs, n);
+    }
     int step_body_dev(const DioAvbdOptions& opt) {
         uint32_t n = w_.n;
         PrepParams<R> pp = opts_prep(opt);
         set_rows(cur_);
+        set_slots();
         k_roll_counters<<<1, 1, 0, stream_>>>(ctr_);
         ++launches_;
         cudaEvent_t e = span_begin();
@@ -1673,7 +1719,7 @@ class Engine final : public EngineBase {
         DIO_TRY(run_narrow(cap_.max_pairs, &ctr_->pairs));
         span_end(e, 3);
         e = span_begin();
-        DIO_TRY(build_rows(pp, cap_.max_pairs, cfg_.contacts_per_pair, &ctr_->pairs, n));
+        DIO_TRY(build_world_rows(pp, n));
         DIO_TRY(finish_rows_world(pp, n));
         span_end(e, 4);
         SolveParams<R> so = solve_params(opt.dt, opt.gravity, opt.alpha, opt.beta_lin, opt.penalty_max, opt.iterations);
@@ -1690,6 +1736,7 @@ class Engine final : public EngineBase {
         uint32_t n = w_.n;
         PrepParams<R> pp = opts_prep(opt);
         set_rows(cur_);
+        set_slots();
         k_roll_counters<<<1, 1, 0, stream_>>>(ctr_);
         cudaEvent_t e = span_begin();
         if (n) DIO_TRY(run_broad(0, n));
@@ -1698,7 +1745,7 @@ class Engine final : public EngineBase {
         DIO_TRY(run_narrow(cap_.max_pairs, &ctr_->pairs));
         span_end(e, 3);
         e = span_begin();
-        DIO_TRY(build_rows(pp, cap_.max_pairs, cfg_.contacts_per_pair, &ctr_->pairs, n));
+        DIO_TRY(build_world_rows(pp, n));
         DIO_TRY(finish_rows_world(pp, n));
         span_end(e, 4);
         DIO_TRY(color_world(n));
@@ -1933,6 +1980,8 @@ class Engine final : public EngineBase {
     uint32_t chunk_max_ = 0;  // bodies in the largest scene chunk
     std::vector<uint2> chunks_host_;
     uint2* chunks_ = nullptr;
+    Slot<R>* slots_[2] = {nullptr, nullptr};
+    bool lag_primed_ = false;  // the previous step's slots are this mode's
     uint32_t* chunk_n_ = nullptr;
     uint32_t* chunk_ovf_ = nullptr;
     uint2* tree_scratch_ = nullptr;

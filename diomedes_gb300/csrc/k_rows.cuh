@@ -374,6 +374,7 @@ __device__ __forceinline__ bool key_eq(uint2 a, uint2 b) { return a.x == b.x && 
 static __global__ void k_roll_counters(Counters* c) {
     c->prev_rows = c->rows;
     c->prev_pair_rows = c->pair_rows;
+    c->prev_pairs = c->pairs;
     c->pairs = 0;
     c->rows = 0;
     c->pair_rows = 0;

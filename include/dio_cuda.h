@@ -223,7 +223,13 @@ typedef struct DioConfig {
     uint32_t broad_phase;       /* 0: LBVH (default), 1: dense sweep        */
     uint32_t bvh_rebuild_period; /* LBVH topology rebuilt every N steps and
                                     refitted in between (0: every 4)     */
-    uint32_t reserved[2];
+    uint32_t contact_lag;       /* 1: the demos' frame pipelining -- pair
+                                   rows of step t come from the narrow phase
+                                   of step t-1 (its witness points, this
+                                   step's transforms; demos/avbd_box/src/
+                                   main.rs:203-207,244-249); container rows
+                                   are current.  0 (default): no lag      */
+    uint32_t reserved[1];
 } DioConfig;
 
 /* World description for the fused device-resident step (extension of the

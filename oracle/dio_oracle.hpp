@@ -1497,6 +1497,12 @@ struct World {
     uint32_t ncolors = 0;
     uint32_t per_pair = 4;
     bool colored = false;
+    // the demos' frame pipelining (demos/avbd_box/src/main.rs:203-207,244-249):
+    // the narrow phase read at frame t was submitted at frame t-1, and
+    // raw_contact (engine/src/physics/gpu.rs:239-264) applies its witness
+    // points to the current transforms
+    bool lag = false;
+    std::vector<Slot<R>> prev_slots;
     bool split_rebase = false;  // detect in scene-local R coordinates
     bool use_sap = true;
     int threads = 1;
@@ -1547,6 +1553,7 @@ struct World {
         }
         epa_overflow = ovf;
         std::vector<Row<P, R>> nrows;
+        if (lag) prev_slots.swap(slots);  // rows from the previous step's detection
         for (auto& sl : slots)
             if (sl.valid)
                 nrows.push_back(raw_contact<P, R>(sl.a, sl.b, nb[sl.a], nb[sl.b], sl.normal, sl.depth, sl.point_a,

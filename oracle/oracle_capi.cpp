@@ -144,12 +144,18 @@ struct WorldBase {
     virtual uint32_t contacts(DioContact* out, uint32_t cap) = 0;
     virtual uint32_t colors(uint32_t* out, uint32_t cap) = 0;
     virtual void stats(DioStepStats* s) = 0;
+    virtual void set_lag(bool on) = 0;
     uint64_t steps_done = 0;
 };
 
 template <class P, class R>
 struct WorldT : WorldBase {
     World<P, R> w;
+    // switching the lag on starts from no previous detection
+    void set_lag(bool on) override {
+        if (on && !w.lag) w.prev_slots.clear();
+        w.lag = on;
+    }
     std::vector<DioShape> raw_shapes;
     void step(const DioAvbdOptions& o, uint32_t steps) override {
         Options<R> opt = to_options<R>(o);
@@ -266,6 +272,7 @@ WorldBase* make_world(const DioWorldDesc& d, const DioConfig& cfg, int threads) 
     w.hull = to_hull<R>(d.hull_vertices, d.n_hull_vertices);
     w.per_pair = cfg.contacts_per_pair == 8 ? 8 : 4;
     w.colored = cfg.solver_mode == DIO_SOLVER_COLORED;
+    w.lag = cfg.contact_lag != 0;
     w.split_rebase = cfg.precision == DIO_PREC_SPLIT;
     w.threads = threads < 1 ? 1 : threads;
     return W;
@@ -507,6 +514,10 @@ void* oracle_world_create(const DioWorldDesc* desc, const DioConfig* cfg, int th
     return make_world<float, float>(*desc, c, threads);
 }
 void oracle_world_destroy(void* h) { delete static_cast<WorldBase*>(h); }
+int oracle_world_set_lag(void* h, int on) {
+    static_cast<WorldBase*>(h)->set_lag(on != 0);
+    return 0;
+}
 int oracle_world_step(void* h, const DioAvbdOptions* o, uint32_t steps) {
     static_cast<WorldBase*>(h)->step(*o, steps);
     return 0;

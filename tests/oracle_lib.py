@@ -38,6 +38,7 @@ def lib():
             "oracle_avbd_run": [_u32, _vp, _vp, _vp, _u32, _vp, _u32, _vp, _u32, _vp, _vp,
                                 ctypes.POINTER(abi.RunOptions), _u32, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
             "oracle_world_step": [_vp, ctypes.POINTER(abi.AvbdOptions), _u32],
+            "oracle_world_set_lag": [_vp, ctypes.c_int],
             "oracle_world_download": [_vp, _vp, _vp],
             "oracle_world_download_f64": [_vp, _vp, _vp],
             "oracle_world_contacts": [_vp, _vp, _u32, ctypes.POINTER(_u32)],
@@ -145,7 +146,7 @@ def avbd_run(state, positions, orientations, contacts, constraints, offsets, ind
 class World:
     """Oracle world: same descriptor as the CUDA world."""
 
-    def __init__(self, scene, precision=0, solver_mode=0, contacts_per_pair=4, threads=1):
+    def __init__(self, scene, precision=0, solver_mode=0, contacts_per_pair=4, threads=1, contact_lag=0):
         self._keep = []
         d = abi.WorldDesc()
         b = np.ascontiguousarray(scene.bodies, abi.BODY)
@@ -178,6 +179,7 @@ class World:
         cfg.precision = precision
         cfg.solver_mode = solver_mode
         cfg.contacts_per_pair = contacts_per_pair
+        cfg.contact_lag = contact_lag
         self.h = lib().oracle_world_create(ctypes.byref(d), ctypes.byref(cfg), threads)
         self.n = len(b)
 
@@ -188,6 +190,9 @@ class World:
 
     def step(self, options, steps=1):
         lib().oracle_world_step(self.h, ctypes.byref(options), steps)
+
+    def set_lag(self, on):
+        lib().oracle_world_set_lag(self.h, int(on))
 
     def download(self):
         b = np.zeros(self.n, abi.BODY)

@@ -202,6 +202,70 @@ def test_set_state_that_changes_dynamic_bodies_rebuilds_the_list():
         w.set_state(None, w.download()[1])
 
 
+def _lag_scenes():
+    parts = [scenes.pyramid(levels=3), scenes.constraints_demo(), scenes.box_demo()]
+    for p in parts:
+        p.options = parts[0].options
+    return [scenes.box_demo(), scenes.mixed_pile(n=600, extent=6.0), scenes.pack(parts)]
+
+
+@pytest.mark.parametrize("use_graph", [0, 1])
+def test_contact_lag_matches_oracle(use_graph):
+    """contact_lag = 1 reproduces the demos' frame pipelining: the pair rows of
+    step t come from the narrow phase of step t-1 (its witness points, this
+    step's transforms), container rows are current.  Bit for bit against the
+    oracle in the same mode, from upload and when switched on mid-run."""
+    for sc in _lag_scenes():
+        ow = O.World(sc, contact_lag=1)
+        with _world(sc, use_graph=use_graph, contact_lag=1) as w:
+            ow.step(sc.options, 1)
+            w.step(sc.options, 1)
+            gc, rc = w.contacts(), ow.contacts()
+            assert not np.any(rc["b"] != 0xFFFFFFFF)  # no detection before the first step
+            assert np.array_equal(_bits(gc), _bits(rc)), sc.name
+            ow.step(sc.options, 11)
+            w.step(sc.options, 11)
+            gb, gs = w.download()
+            gc = w.contacts()
+        rb, rs = ow.download()
+        assert np.array_equal(_bits(gb), _bits(rb)) and np.array_equal(_bits(gs), _bits(rs)), sc.name
+        assert np.array_equal(_bits(gc), _bits(ow.contacts())), sc.name
+        ow2 = O.World(sc)
+        ow2.step(sc.options, 4)
+        ow2.set_lag(1)
+        ow2.step(sc.options, 6)
+        with _world(sc, use_graph=use_graph) as w2:
+            w2.step(sc.options, 4)
+            w2.configure(contact_lag=1)
+            w2.step(sc.options, 6)
+            gb2, gs2 = w2.download()
+        rb2, rs2 = ow2.download()
+        assert np.array_equal(_bits(gb2), _bits(rb2)) and np.array_equal(_bits(gs2), _bits(rs2)), sc.name
+
+
+def test_checkpoint_resume_in_contact_lag_mode():
+    """A lagged world's checkpoint carries the last step's narrow slots: the
+    resumed world continues bit for bit."""
+    sc = _lag_scenes()[1]
+    with _world(sc, contact_lag=1) as w:
+        w.step(sc.options, 5)
+        img = w.checkpoint()
+        w.step(sc.options, 6)
+        ref_b, ref_s = w.download()
+    h = compute.checkpoint_header(img)
+    assert h["lag_pairs"] > 0 and h["per_pair"] == 4
+    cap = compute.capacity(sc.n, max_pairs=max(64, 40 * sc.n), max_contacts=max(256, 200 * sc.n),
+                           max_joints=1, max_scenes=1, max_hull_vertices=len(sc.hull_vertices))
+    with compute.World(cap) as w2:
+        with pytest.raises(abi.DioError):  # a lagged image needs a lagged context
+            w2.resume(img)
+        w2.configure(contact_lag=1)
+        w2.resume(img)
+        w2.step(sc.options, 6)
+        gb, gs = w2.download()
+    assert np.array_equal(_bits(gb), _bits(ref_b)) and np.array_equal(_bits(gs), _bits(ref_s))
+
+
 def test_pipelined_frames_match_synchronous_steps():
     """A frame loop of dio_step_async + dio_world_download_async into two
     alternating page-locked buffers (read frame t-1 while t computes) yields
