@@ -16,7 +16,7 @@ One JSON line on rank 0:
   roofline   the primal kernel: algorithmic bytes per launch / event time
   cpu_baseline  the CPU oracle (OpenMP over bodies / rows) on a sample
 --impl reference times the CPU restatement of the reference path (the
-reference is Rust + Vulkan and cannot run on the GPU machine).
+reference is Rust + Vulkan; neither toolchain nor a Vulkan device exists here).
 """
 import argparse
 import json

@@ -1,8 +1,8 @@
 // dio_oracle.hpp -- CPU oracle for the Diomedes per-step rigid-body path.
 //
 // TEST INFRASTRUCTURE ONLY.  This header is a plain C++ restatement of the
-// reference's algorithm (nathenjacobe/diomedes) used as the checker for the
-// CUDA implementation and as the timed CPU baseline.  Nothing in the shipped
+// reference's algorithm (nathenjacobe/diomedes) that the tests compare the
+// CUDA implementation with and that the bench times as the CPU baseline.  Nothing in the shipped
 // library includes or links it.
 //
 // Parity status: the reference is Rust compiled to SPIR-V (rust-gpu) and

@@ -1,7 +1,7 @@
 """ctypes wrapper of the CPU oracle (oracle/liboracle.so) for the tests.
 
-The oracle is the checker: tests feed it the same records they feed the
-CUDA library and compare the results.
+Tests feed the oracle the same records they feed the CUDA library and
+compare the results.
 """
 import ctypes
 import os
