@@ -532,6 +532,8 @@ class Engine final : public EngineBase {
         int dev = 0;
         DIO_CK(cudaGetDevice(&dev));
         DIO_CK(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev));
+        DIO_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&dual_ctas_per_sm_, k_dual<P, R>, 256, 0));
+        dual_ctas_per_sm_ = std::max(1, dual_ctas_per_sm_);
         const int tree_bytes = (int)scene_tree_bytes<R>(scene_tree_cap<R>());
         DIO_CK(cudaFuncSetAttribute(k_scene_tree<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, tree_bytes));
         DIO_CK(cudaFuncSetAttribute(k_scene_tree<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tree_bytes));
@@ -1357,7 +1359,9 @@ class Engine final : public EngineBase {
     int solve(const SolveParams<R>& o, uint32_t n, uint32_t m, const uint32_t* m_dev = nullptr) {
         if (n == 0) return DIO_OK;
         int gb = grid_for(n, 256);
-        int gm = m_dev ? std::min(grid_for(cap_.max_contacts, 256), sms_ * 8) : grid_for(std::max(m, 1u), 256);
+        // device-counted rows: one resident wave, rows strided over it
+        int gm = m_dev ? std::min(grid_for(cap_.max_contacts, 256), sms_ * dual_ctas_per_sm_)
+                       : grid_for(std::max(m, 1u), 256);
         if (m_dev) m = cap_.max_contacts;
         k_init<P, R><<<gb, 256, 0, stream_>>>(w_, 0, n, o);
         launches_ += 2;
@@ -1999,6 +2003,7 @@ class Engine final : public EngineBase {
     int cur_ = 0;
     uint32_t n_prev_rows_ = 0;
     uint32_t n_hull_ = 0;  // hull vertices of the uploaded world
+    int dual_ctas_per_sm_ = 4;
     uint32_t api_bodies_ = 0, api_n_ = 0, api_m_ = 0, api_iters_ = 0, last_np_ = 0;
     uint64_t steps_ = 0;
     bool world_ready_ = false;
