@@ -1,6 +1,9 @@
 """The reference's own unit tests, ported, run against the CPU oracle, plus
 analytic cases that pin the restated arithmetic where the reference has no
 test (free fall, sphere overlap, resting force balance, warm start)."""
+import json
+import os
+
 import numpy as np
 import pytest
 
@@ -16,88 +19,87 @@ def pair01():
     return np.array([(0, 1)], abi.PAIR)
 
 
-# ---- engine/gpu_physics/narrowphase/src/cuboid.rs:403-422
-def test_touching_cubes_have_zero_penetration():
-    b, _ = ph.pack_bodies([cube_at(0.0), cube_at(1.0)])
-    s = O.narrow(b, pair01())
-    v = s[s["valid"] != 0]
-    assert len(v) >= 1
-    assert abs(v["depth"][0]) < 1e-6
-    assert v["normal"][0, 0] > 0.99
+# ---- the reference's own unit tests on this path, as data (tests/golden/
+# reference_cases.json, written by tests/golden/make_reference_cases.py from
+# the cited reference sources)
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "reference_cases.json")
+with open(GOLDEN) as _f:
+    CASES = [c for c in json.load(_f)["cases"] if c["kind"] != "none"]
 
 
-def test_overlapping_cubes_report_four_face_contacts():
-    b, _ = ph.pack_bodies([cube_at(0.0), cube_at(0.9)])
-    s = O.narrow(b, pair01())
-    v = s[s["valid"] != 0]
-    assert abs(v["depth"][0] - 0.1) < 1e-6
-    assert v["normal"][0, 0] > 0.99
-    assert len(v) == 4
+def _run_case(c):
+    i, e = c["input"], c["expect"]
+    k = c["kind"]
+    if k == "sat":
+        b, _ = ph.pack_bodies([cube_at(*i["a"]), cube_at(*i["b"])])
+        v = O.narrow(b, pair01())
+        v = v[v["valid"] != 0]
+        if not e["contact"]:
+            assert len(v) == 0
+            return
+        assert len(v) >= 1
+        assert abs(v["depth"][0] - e["depth"]) < e["depth_tol"]
+        assert v["normal"][0, 0] > e["normal_dot_x_min"]
+        if "count" in e:
+            assert len(v) == e["count"]
+    elif k == "support":
+        s = ph.shape_sphere(i["radius"]) if i["shape"] == "sphere" else ph.shape_cube(i["half_extent"])
+        for d, p in zip(i["dirs"], e["points"]):
+            assert np.array_equal(O.support(s, d), p)
+    elif k == "support_tetra":
+        s = ph.shape_tetrahedron(i["corners"])
+        p = O.support(s, i["tie_dir"])
+        assert p[0] == e["tie_x"] and float(np.dot(p, i["tie_dir"])) == e["tie_x"]
+        # corners 0 and 1 tie along +x; the GPU rule keeps the first (support.rs:232-236)
+        assert np.array_equal(p, i["corners"][0])
+        for d, q in zip(i["dirs"], e["points"]):
+            assert np.array_equal(O.support(s, d), q)
+    elif k == "container":
+        container = ph.container(tuple(i["center"]), i["half_extent"])
+        b, st = ph.pack_bodies([cube_at(*i["cube_at"], h=i["h"], mass=i["mass"])])
+        rows, off, idx = O.prepare_contacts(b, st, np.zeros(0, abi.CONTACT_OUT), None, container,
+                                            ph.avbd_options())
+        assert len(rows) == e["count"]
+        assert np.array_equal(rows["normal"][:, :3], np.tile(e["normal"], (e["count"], 1)).astype(np.float32))
+        assert (rows["r_a"][:, 1] < e["r_a_y_max"]).all()
+        assert rows["b"].tolist() == [abi.CONTAINER] * e["count"]
+        assert off.tolist() == [0, e["count"]] and idx.tolist() == list(range(e["count"]))
+    elif k == "endpoints":
+        half = np.radians(i["b_rot_z_deg"]) / 2
+        q = (0.0, 0.0, np.sin(half), np.cos(half))
+        b, _ = ph.pack_bodies([cube_at(*i["a_pos"], mass=0.0), cube_at(*i["b_pos"], q=q)])
+        j = ph.ball_socket(0, 1, tuple(i["anchor_a"]), tuple(i["anchor_b"]))
+        pa, pb = ph.endpoints(j, b)
+        assert np.allclose(pa, e["a"], atol=e["tol"]) and np.allclose(pb, e["b"], atol=e["tol"])
+    elif k == "names":
+        js = [ph.spring(0, 1, (0, 0, 0), (0, 0, 0), 1.0, 1.0), ph.rod(0, 1, (0, 0, 0), (0, 0, 0), 1.0),
+              ph.ball_socket(0, 1, (0, 0, 0), (0, 0, 0)), ph.rope(0, 1, (0, 0, 0), (0, 0, 0), 1.0)]
+        assert [ph.joint_name(j) for j in js] == e["names"]
+    elif k == "records":
+        js = ph.pack_joints([ph.spring(0, 1, (0, 0, 0), (0, 0, 0), *i["spring"]),
+                             ph.rod(0, 1, (0, 0, 0), (0, 0, 0), i["rod"]),
+                             ph.ball_socket(0, 1, (0, 0, 0), (0, 0, 0)),
+                             ph.rope(0, 1, (0, 0, 0), (0, 0, 0), i["rope"])])
+        assert abi.CONSTRAINT.itemsize == e["record_bytes"]
+        kinds = {"spring": abi.SPRING, "rod": abi.ROD, "ball_socket": abi.BALL_SOCKET, "rope": abi.ROPE}
+        assert js["kind"].tolist() == [kinds[x] for x in e["kinds"]]
+        assert js["anchor_a"][3, 3] == e["rope_anchor_a_w"]
+    else:
+        raise AssertionError(f"unknown case kind {k}")
 
 
-def test_separated_cubes_have_no_contact():
-    b, _ = ph.pack_bodies([cube_at(0.0), cube_at(1.1)])
-    assert (O.narrow(b, pair01())["valid"] == 0).all()
+@pytest.mark.parametrize("case", CASES, ids=[c["id"] for c in CASES])
+def test_reference_known_answer(case):
+    _run_case(case)
 
 
-# ---- engine/src/physics/shape.rs:53-95 (GPU rule: first maximal corner)
-def test_sphere_support_tracks_direction():
-    s = ph.shape_sphere(2.0)
-    assert np.array_equal(O.support(s, (1, 0, 0)), [2, 0, 0])
-    assert np.array_equal(O.support(s, (0, -3, 0)), [0, -2, 0])
-
-
-def test_cube_support_is_a_corner():
-    s = ph.shape_cube(0.5)
-    assert np.array_equal(O.support(s, (1, 1, 1)), [0.5, 0.5, 0.5])
-    assert np.array_equal(O.support(s, (-1, 1, 0)), [-0.5, 0.5, 0.5])
-
-
-def test_tetrahedron_support_is_the_farthest_corner():
-    c = [(1, 1, 1), (1, -1, -1), (-1, 1, -1), (-1, -1, 1)]
-    s = ph.shape_tetrahedron(c)
-    p = O.support(s, (1, 0, 0))
-    assert p[0] == 1.0
-    # corners 0 and 1 tie along +x; the GPU keeps the first (support.rs:232-236)
-    assert np.array_equal(p, [1, 1, 1])
-    assert np.array_equal(O.support(s, (-1, -1, 0)), [-1, -1, 1])
-
-
-# ---- engine/src/physics/gpu.rs:420-433
-def test_penetrating_cube_gets_four_floor_contacts():
-    container = ph.container((0.0, 4.0, 0.0), 4.0)
-    b, s = ph.pack_bodies([cube_at(0.0, y=0.49, mass=1.0)])
-    rows, off, idx = O.prepare_contacts(b, s, np.zeros(0, abi.CONTACT_OUT), None, container, ph.avbd_options())
-    assert len(rows) == 4
-    assert np.array_equal(rows["normal"][:, :3], np.tile([0, 1, 0], (4, 1)).astype(np.float32))
-    assert (rows["r_a"][:, 1] < -0.49).all()
-    assert rows["b"].tolist() == [abi.CONTAINER] * 4
-    assert off.tolist() == [0, 4] and idx.tolist() == [0, 1, 2, 3]
-
-
-# ---- engine/src/physics/constraints.rs:158-186
-def test_endpoints_apply_body_rotation_and_local_anchors():
-    q = (0.0, 0.0, np.sin(np.pi / 4), np.cos(np.pi / 4))
-    b, _ = ph.pack_bodies([cube_at(0.0, mass=0.0), cube_at(2.0, q=q)])
-    j = ph.ball_socket(0, 1, (0.5, 0, 0), (0, -0.5, 0))
-    pa, pb = ph.endpoints(j, b)
-    assert np.allclose(pa, [0.5, 0, 0], atol=1e-6)
-    assert np.allclose(pb, [2.5, 0, 0], atol=1e-6)
-
-
-def test_constraint_names_cover_all_kinds():
-    js = [ph.spring(0, 1, (0, 0, 0), (0, 0, 0), 1.0, 1.0), ph.rod(0, 1, (0, 0, 0), (0, 0, 0), 1.0),
-          ph.ball_socket(0, 1, (0, 0, 0), (0, 0, 0)), ph.rope(0, 1, (0, 0, 0), (0, 0, 0), 1.0)]
-    assert [ph.joint_name(j) for j in js] == ["spring", "rod", "ball and socket", "rope"]
-
-
-# ---- engine/src/render/gpu_physics.rs:701-721
-def test_constraint_records_keep_shader_layout_and_kinds():
-    js = ph.pack_joints([ph.spring(0, 1, (0, 0, 0), (0, 0, 0), 2.0, 1.0), ph.rod(0, 1, (0, 0, 0), (0, 0, 0), 1.0),
-                         ph.ball_socket(0, 1, (0, 0, 0), (0, 0, 0)), ph.rope(0, 1, (0, 0, 0), (0, 0, 0), 3.0)])
-    assert abi.CONSTRAINT.itemsize == 48
-    assert js["kind"].tolist() == [abi.SPRING, abi.ROD, abi.BALL_SOCKET, abi.ROPE]
-    assert js["anchor_a"][3, 3] == 3.0
+def test_golden_fixture_names_its_sources():
+    with open(GOLDEN) as f:
+        data = json.load(f)
+    assert data["checked_against_reference_sources"]
+    for c in data["cases"]:
+        path, rng = c["source"].rsplit(":", 1)
+        assert path.endswith(".rs") and "-" in rng and c["anchors"], c["id"]
 
 
 # ---- analytic cases (no reference test covers them)
