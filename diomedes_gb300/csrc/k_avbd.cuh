@@ -111,13 +111,18 @@ template <class P, class R>
 __device__ __forceinline__ void init_body(const DevWorld<P, R>& w, uint32_t i, const SolveParams<R>& o) {
     A4<P> p4 = w.pos[0][i];
     A4<P> q4 = w.rot[0][i];
-    w.pos[1][i] = p4;
-    w.rot[1][i] = q4;
+    R inv_mass = w.inv[i].w;
+    // buffer 1 holds the un-warm-started pose for bodies the primal never
+    // writes (static ones); a dynamic body's copy is overwritten by the first
+    // primal before anything reads it, unless there is no iteration at all
+    if (inv_mass == R(0) || o.iterations == 0) {
+        w.pos[1][i] = p4;
+        w.rot[1][i] = q4;
+    }
     V3<P> pos = xyz(p4);
     Q4<P> rot = quat(q4);
     V3<P> vel = xyz(w.vel[i]);
     V3<P> ang = xyz(w.ang[i]);
-    R inv_mass = w.inv[i].w;
     P dt = P(o.dt);
     V3<P> g{P(o.gx), P(o.gy), P(o.gz)};
     w.init_pos[i] = pack(pos);
