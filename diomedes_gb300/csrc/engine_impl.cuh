@@ -570,6 +570,11 @@ class Engine final : public EngineBase {
             open_bodies += sz;
         }
         close((uint32_t)scenes_host_.size());
+        // largest chunks first: CTAs start in chunk order, so the last wave
+        // holds the short ones
+        auto bodies_of = [&](const uint2& c) { return scenes_host_[c.y - 1].body_hi - scenes_host_[c.x].body_lo; };
+        std::stable_sort(chunks_host_.begin(), chunks_host_.end(),
+                         [&](const uint2& a, const uint2& b) { return bodies_of(a) > bodies_of(b); });
         if (!chunks_host_.empty())
             DIO_CK(cudaMemcpyAsync(chunks_, chunks_host_.data(), chunks_host_.size() * sizeof(uint2),
                                    cudaMemcpyHostToDevice, stream_));
