@@ -555,6 +555,40 @@ def test_every_primal_variant_matches_oracle(variant):
     assert np.array_equal(_bits(gb), _bits(rb)) and np.array_equal(_bits(gs), _bits(rs))
 
 
+def _fib_sphere(n, r):
+    k = np.arange(n) + 0.5
+    phi = np.arccos(1 - 2 * k / n)
+    th = np.pi * (1 + 5 ** 0.5) * k
+    return (r * np.stack([np.cos(th) * np.sin(phi), np.sin(th) * np.sin(phi), np.cos(phi)], 1)).astype(np.float32)
+
+
+def test_hulls_beyond_the_staging_area_match_oracle():
+    """EPA on hulls of 150 vertices -- more than the 64 per hull staged in
+    shared memory, so read from global memory -- next to staged 42-vertex
+    icospheres and against each other."""
+    big, small = _fib_sphere(150, 0.5), (scenes.icosphere42() * 0.4).astype(np.float32)
+    rng = np.random.default_rng(3)
+    items, hv, first = [], [], 0
+    for k in range(60):
+        verts = big if k % 2 == 0 else small
+        q = rng.normal(size=4)
+        q /= np.linalg.norm(q)
+        items.append(ph.hull(tuple(rng.uniform(-1.5, 1.5, 3)), first, verts, 1.0, orientation=tuple(q)))
+        hv.append(verts)
+        first += len(verts)
+    b, _ = ph.pack_bodies(items)
+    hvs = np.zeros((first, 4), np.float32)
+    hvs[:, :3] = np.concatenate(hv)
+    pairs, _ = O.broad(b, hull=hvs)
+    ref = O.narrow(b, pairs, hull=hvs)
+    with compute.NarrowPhaseCompute(len(b), len(pairs), max_hull_vertices=len(hvs)) as npc:
+        npc.set_hull_vertices(hvs)
+        got = npc.run(b, pairs)
+    big_pairs = ((ref["a"] % 2 == 0) & (ref["b"] % 2 == 0) & (ref["valid"] != 0)).sum()
+    assert int(ref["valid"].sum()) > 20 and big_pairs > 0
+    assert np.array_equal(_bits(got), _bits(ref))
+
+
 def test_autotune_keeps_state_and_results(tmp_path):
     """Every tuned variant computes the same bits, and the trials run from a
     snapshot that is restored: stepping after tuning still matches the
