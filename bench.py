@@ -251,6 +251,7 @@ def main():
     ms = e0.elapsed_time(e1)
     st = w.stats()
     b32_after, _ = w.download()  # for the FP64 comparison below
+    rows_after = w.contacts()
 
     # a second pass of the same K steps with the per-phase / per-launch event
     # timers on (they add an event pair per span, so the headline pass above
@@ -349,10 +350,49 @@ def main():
         wf = compute.World(world_capacity(sc), precision=2)
         wf.upload(sc.bodies, sc.state, **sc.upload_kwargs())
         wf.step(o, steps_done)
-        p64, _ = wf.download_f64()
-        err = np.abs(b32["position"][:, :3].astype(np.float64) - p64).max(axis=1)
-        f64 = {"max_pos_err_m": float(err.max()), "median_pos_err_m": float(np.median(err)), "steps": steps_done}
+        p64, q64 = wf.download_f64()
+        rows64 = wf.contacts()
         wf.close()
+
+        def pos_err(p):
+            return np.abs(p - p64).max(axis=1)
+
+        def ang_err(q):  # rotation angle between the two orientations
+            c = np.abs((q.astype(np.float64) * q64).sum(axis=1))
+            return 2.0 * np.arccos(np.clip(c, 0.0, 1.0))
+
+        def max_pen(rows):  # deepest row of the last step: depth = margin - c0.x
+            return float((o.margin - rows["c0"][:, 0]).max()) if len(rows) else 0.0
+
+        err = pos_err(b32["position"][:, :3].astype(np.float64))
+        aerr = ang_err(b32["orientation"])
+        f64 = {"max_pos_err_m": float(err.max()), "median_pos_err_m": float(np.median(err)),
+               "max_angle_err_rad": float(aerr.max()), "median_angle_err_rad": float(np.median(aerr)),
+               "max_penetration_m": max_pen(rows_after), "max_penetration_m_fp64": max_pen(rows64),
+               "steps": steps_done}
+        # the split-precision path on the same batch (FP64 poses / inertial
+        # terms / lambda, FP32 Hessian, LDL^T and detection): throughput and
+        # its own error against the FP64 world
+        ws = compute.World(world_capacity(sc), precision=1)
+        ws.set_stream(stream.cuda_stream)
+        ws.upload(sc.bodies, sc.state, **sc.upload_kwargs())
+        ws.configure(primal_variant=tuned["primal_variant"], bvh_rebuild_period=tuned["bvh_rebuild_period"])
+        ws.step(o, args.warmup)
+        torch.cuda.synchronize()
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
+        ws.step(o, args.steps)
+        s1.record(stream)
+        torch.cuda.synchronize()
+        ps, qs = ws.download_f64()
+        rows_s = ws.contacts()
+        ws.close()
+        es, ea = pos_err(ps), ang_err(qs)
+        f64["split"] = {"value": sc.n * args.steps / (s0.elapsed_time(s1) / 1e3), "unit": "body-steps/s",
+                        "batched_over_plain": (sc.n * args.steps / (s0.elapsed_time(s1) / 1e3)) / plain["value"]
+                        if plain else None,
+                        "max_pos_err_m": float(es.max()), "median_pos_err_m": float(np.median(es)),
+                        "max_angle_err_rad": float(ea.max()), "max_penetration_m": max_pen(rows_s)}
 
     cpu = None
     if not args.no_cpu and rank == 0:
