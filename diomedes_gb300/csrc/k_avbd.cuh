@@ -297,16 +297,11 @@ __device__ __forceinline__ void primal_jview_p(const JView& jv, A4<P> op4, A4<P>
     const uint32_t kind = jv.kind & ~kIsB;
     const V3<R> anc_s{R(jv.self_anchor.x), R(jv.self_anchor.y), R(jv.self_anchor.z)};
     const V3<R> anc_o{R(jv.other_anchor.x), R(jv.other_anchor.y), R(jv.other_anchor.z)};
-    V3<R> r_self;
-    V3<P> p_self;
-    if constexpr (std::is_same<P, R>::value) {
-        r_self = rotate(sqr, anc_s);  // identical expression: evaluate once
-        p_self = add(sp, r_self);
-    } else {
-        p_self = add(sp, rotate(sq, cast3<P>(anc_s)));
-        r_self = rotate(sqr, anc_s);
-    }
-    const V3<P> p_other = add(xyz(op4), rotate(quat(oq4), cast3<P>(anc_o)));
+    // anchor offsets are rotated in R (small body-frame vectors) and added to
+    // the P positions; with P == R this is the reference's expression
+    const V3<R> r_self = rotate(sqr, anc_s);
+    const V3<P> p_self = add(sp, cast3<P>(r_self));
+    const V3<P> p_other = add(xyz(op4), cast3<P>(rotate(castq<R>(quat(oq4)), anc_o)));
     const V3<R> delta = cast3<R>(is_a ? sub(p_self, p_other) : sub(p_other, p_self));
     const R sign = is_a ? R(1) : R(-1);
     const R stiff = R(jv.other_anchor.w);

@@ -1242,8 +1242,10 @@ struct Avbd {
             V3<P> pb = !is_a ? sp : B.pos[rd][jt.b];
             Qt<P> qa = is_a ? sq : B.rot[rd][jt.a];
             Qt<P> qb = !is_a ? sq : B.rot[rd][jt.b];
-            V3<P> wpa = pa + rotate(qa, cast3<P>(jt.anchor_a));
-            V3<P> wpb = pb + rotate(qb, cast3<P>(jt.anchor_b));
+            // anchor offsets rotated in R (body-frame vectors), added to the
+            // P positions: identical to the reference's form when P == R
+            V3<P> wpa = pa + cast3<P>(rotate(castq<R>(qa), jt.anchor_a));
+            V3<P> wpb = pb + cast3<P>(rotate(castq<R>(qb), jt.anchor_b));
             V3<R> self_anchor = is_a ? jt.anchor_a : jt.anchor_b;
             R sign = is_a ? R(1) : R(-1);
             V3<R> delta = cast3<R>(wpa - wpb);
