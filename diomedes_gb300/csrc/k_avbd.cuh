@@ -228,7 +228,7 @@ __device__ __forceinline__ void primal_row_f(const DevWorld<P, R>& w, uint32_t r
         A4<P> op = fetch.pos(other);
         A4<P> oq = fetch.rot(other);
         dol = cast3<R>(sub(xyz(op), xyz(fetch.ipos(other))));
-        doa = cast3<R>(ang_diff(quat(oq), quat(fetch.irot(other))));
+        doa = ang_diff(castq<R>(quat(oq)), castq<R>(quat(fetch.irot(other))));
         rot_other = rotate(castq<R>(quat(oq)), is_a ? xyz(rs.rb) : xyz(rs.ra));
     }
     V3<R> j0 = cross(rw, r0), j1 = cross(rw, r1), j2 = cross(rw, r2);
@@ -370,7 +370,7 @@ __device__ __forceinline__ void primal_body_f(const DevWorld<P, R>& w, uint32_t 
     B.h[tri(4, 4)] = idt2.y;
     B.h[tri(5, 5)] = idt2.z;
     const V3<R> rl = mulv(V3<R>{mdt2, mdt2, mdt2}, cast3<R>(sub(sp, xyz(w.inert_pos[i]))));
-    const V3<R> ra = mulv(idt2, cast3<R>(ang_diff(sq, quat(w.inert_rot[i]))));
+    const V3<R> ra = mulv(idt2, ang_diff(sqr, castq<R>(quat(w.inert_rot[i]))));
     B.g[0] = rl.x;
     B.g[1] = rl.y;
     B.g[2] = rl.z;
@@ -381,7 +381,7 @@ __device__ __forceinline__ void primal_body_f(const DevWorld<P, R>& w, uint32_t 
     if (j0 < j1) {
         // displacement since the step start: read only by contact rows
         const V3<R> dqsl = cast3<R>(sub(sp, xyz(fetch.ipos(i))));
-        const V3<R> dqsa = cast3<R>(ang_diff(sq, quat(fetch.irot(i))));
+        const V3<R> dqsa = ang_diff(sqr, castq<R>(quat(fetch.irot(i))));
         const R k_alpha = R(1) - o.alpha;
         for (uint32_t j = j0; j < j1; ++j)
             primal_row_f(w, w.row_idx[j], w.row_oth[j], fetch, sqr, dqsl, dqsa, k_alpha, B);
@@ -498,13 +498,13 @@ __device__ __forceinline__ void dual_row(const DevWorld<P, R>& w, uint32_t c, in
     A4<P> pa4 = w.pos[rd][ab.x];
     A4<P> qa4 = w.rot[rd][ab.x];
     V3<R> dal = cast3<R>(sub(xyz(pa4), xyz(w.init_pos[ab.x])));
-    V3<R> daa = cast3<R>(ang_diff(quat(qa4), quat(w.init_rot[ab.x])));
+    V3<R> daa = ang_diff(castq<R>(quat(qa4)), castq<R>(quat(w.init_rot[ab.x])));
     V3<R> dbl{R(0), R(0), R(0)}, dba{R(0), R(0), R(0)}, rbw{R(0), R(0), R(0)};
     if (ab.y != kContainer) {
         A4<P> pb4 = w.pos[rd][ab.y];
         A4<P> qb4 = w.rot[rd][ab.y];
         dbl = cast3<R>(sub(xyz(pb4), xyz(w.init_pos[ab.y])));
-        dba = cast3<R>(ang_diff(quat(qb4), quat(w.init_rot[ab.y])));
+        dba = ang_diff(castq<R>(quat(qb4)), castq<R>(quat(w.init_rot[ab.y])));
         rbw = rotate(castq<R>(quat(qb4)), xyz(rs.rb));
     }
     V3<R> raw = rotate(castq<R>(quat(qa4)), xyz(rs.ra));

@@ -1189,7 +1189,7 @@ struct Avbd {
         H[4][4] = i_dt2.y;
         H[5][5] = i_dt2.z;
         V3<R> rl = mulv(m_dt2, cast3<R>(sp - B.inert_lin[i]));
-        V3<R> ra = mulv(i_dt2, cast3<R>(ang_diff(sq, B.inert_ang[i])));
+        V3<R> ra = mulv(i_dt2, ang_diff(castq<R>(sq), castq<R>(B.inert_ang[i])));
         g[0] = rl.x;
         g[1] = rl.y;
         g[2] = rl.z;
@@ -1197,7 +1197,7 @@ struct Avbd {
         g[4] = ra.y;
         g[5] = ra.z;
         V3<R> dq_self_lin = cast3<R>(sp - B.init_lin[i]);
-        V3<R> dq_self_ang = cast3<R>(ang_diff(sq, B.init_ang[i]));
+        V3<R> dq_self_ang = ang_diff(castq<R>(sq), castq<R>(B.init_ang[i]));
         R k_alpha = R(1) - o.alpha;
         for (uint32_t j = off[i]; j < off[i + 1]; ++j) {
             const Row<P, R>& c = rows[idx[j]];
@@ -1212,7 +1212,7 @@ struct Avbd {
                 V3<P> op = B.pos[rd][other];
                 Qt<P> oq = B.rot[rd][other];
                 dol = cast3<R>(op - B.init_lin[other]);
-                doa = cast3<R>(ang_diff(oq, B.init_ang[other]));
+                doa = ang_diff(castq<R>(oq), castq<R>(B.init_ang[other]));
                 rot_other = rotate(castq<R>(oq), is_a ? c.rb : c.ra);
             }
             V3<R> j0 = cross(rw, r0), j1 = cross(rw, r1), j2 = cross(rw, r2);
@@ -1289,13 +1289,13 @@ struct Avbd {
         V3<P> pa = B.pos[rd][c.a];
         Qt<P> qa = B.rot[rd][c.a];
         V3<R> dal = cast3<R>(pa - B.init_lin[c.a]);
-        V3<R> daa = cast3<R>(ang_diff(qa, B.init_ang[c.a]));
+        V3<R> daa = ang_diff(castq<R>(qa), castq<R>(B.init_ang[c.a]));
         V3<R> dbl{}, dba{}, rbw{};
         if (c.b != CONTAINER) {
             V3<P> pb = B.pos[rd][c.b];
             Qt<P> qb = B.rot[rd][c.b];
             dbl = cast3<R>(pb - B.init_lin[c.b]);
-            dba = cast3<R>(ang_diff(qb, B.init_ang[c.b]));
+            dba = ang_diff(castq<R>(qb), castq<R>(B.init_ang[c.b]));
             rbw = rotate(castq<R>(qb), c.rb);
         }
         V3<R> raw = rotate(castq<R>(qa), c.ra);
