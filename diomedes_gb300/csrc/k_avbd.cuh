@@ -236,8 +236,12 @@ __device__ __forceinline__ void primal_row_f(const DevWorld<P, R>& w, uint32_t r
     c0 = c0 + (dot(r0, dqsl) + dot(j0, dqsa) - dot(r0, dol) - dot(cross(rot_other, r0), doa));
     c1 = c1 + (dot(r1, dqsl) + dot(j1, dqsa) - dot(r1, dol) - dot(cross(rot_other, r1), doa));
     c2 = c2 + (dot(r2, dqsl) + dot(j2, dqsa) - dot(r2, dol) - dot(cross(rot_other, r2), doa));
-    P f0, f1, f2, tm, bounds;
-    row_forces(du, rs.n.w, c0, c1, c2, f0, f1, f2, tm, bounds);
+    // the forces only feed the R Hessian: in the split mode they are formed
+    // in R from the P lambda (the dual accumulates lambda in P)
+    using Fq = std::conditional_t<std::is_same<P, R>::value, P, R>;
+    const RowDual<Fq, R> dv{du.penalty, A4<Fq>{Fq(du.lambda.x), Fq(du.lambda.y), Fq(du.lambda.z), Fq(0)}};
+    Fq f0, f1, f2, tm, bounds;
+    row_forces(dv, rs.n.w, c0, c1, c2, f0, f1, f2, tm, bounds);
     stamp(B, r0, j0, du.penalty.x, R(f0));
     stamp(B, r1, j1, du.penalty.y, R(f1));
     stamp(B, r2, j2, du.penalty.z, R(f2));
@@ -393,7 +397,10 @@ __device__ __forceinline__ void primal_body_f(const DevWorld<P, R>& w, uint32_t 
     R dx[6];
     solve6(B, dx);
     w.pos[wr][i] = pack(add(sp, cast3<P>(V3<R>{dx[0], dx[1], dx[2]})));
-    w.rot[wr][i] = packq(quat_step(sq, cast3<P>(V3<R>{dx[3], dx[4], dx[5]})));
+    if constexpr (std::is_same<P, R>::value)
+        w.rot[wr][i] = packq(quat_step(sq, V3<P>{dx[3], dx[4], dx[5]}));
+    else
+        w.rot[wr][i] = packq(quat_step_split<P, R>(sq, V3<R>{dx[3], dx[4], dx[5]}));
 }
 
 template <class P, class R>

@@ -35,6 +35,7 @@
 #include <limits>
 #include <map>
 #include <utility>
+#include <type_traits>
 #include <vector>
 
 namespace dio_oracle {
@@ -118,6 +119,21 @@ inline Qt<R> quat_step(Qt<R> q, V3<R> d) {
     Qt<R> s = qmul(p, q);
     s = {s.x * R(0.5), s.y * R(0.5), s.z * R(0.5), s.w * R(0.5)};
     return qnormalize(Qt<R>{q.x + s.x, q.y + s.y, q.z + s.z, q.w + s.w});
+}
+// quat_step of the split mode: the increment (d, 0) * q / 2 is formed in R
+// from the rounded quaternion and added to the P quaternion; 1/|q| is seeded
+// in R (correctly rounded sqrt and division) and refined by two Newton steps
+// in P, which reach P accuracy.
+template <class P, class R>
+inline Qt<P> quat_step_split(Qt<P> q, V3<R> d) {
+    Qt<R> s = qmul(Qt<R>{d.x, d.y, d.z, R(0)}, castq<R>(q));
+    s = {s.x * R(0.5), s.y * R(0.5), s.z * R(0.5), s.w * R(0.5)};
+    const Qt<P> u{q.x + P(s.x), q.y + P(s.y), q.z + P(s.z), q.w + P(s.w)};
+    const P n = u.x * u.x + u.y * u.y + u.z * u.z + u.w * u.w;
+    P r = P(R(1) / std::sqrt(R(n)));
+    r = r * (P(1.5) - P(0.5) * n * r * r);
+    r = r * (P(1.5) - P(0.5) * n * r * r);
+    return {u.x * r, u.y * r, u.z * r, u.w * r};
 }
 // ang_diff, engine/gpu_physics/avbd/src/lib.rs:96-99: 2 * vec(to * from^-1)
 template <class R>
@@ -1220,15 +1236,18 @@ struct Avbd {
             c0 = c0 + (dot(r0, dq_self_lin) + dot(j0, dq_self_ang) - dot(r0, dol) - dot(cross(rot_other, r0), doa));
             c1 = c1 + (dot(r1, dq_self_lin) + dot(j1, dq_self_ang) - dot(r1, dol) - dot(cross(rot_other, r1), doa));
             c2 = c2 + (dot(r2, dq_self_lin) + dot(j2, dq_self_ang) - dot(r2, dol) - dot(cross(rot_other, r2), doa));
-            P f0p = P(c.penalty.x * c0) + c.lambda.x;
-            f0p = std::fmin(f0p, P(0));  // f32::min: NaN-ignoring
-            P f1r = P(c.penalty.y * c1) + c.lambda.y;
-            P f2r = P(c.penalty.z * c2) + c.lambda.z;
-            P bounds = std::fabs(f0p) * P(c.friction);
-            P tm = std::sqrt(f1r * f1r + f2r * f2r);
-            P f1 = f1r, f2 = f2r;
-            if (tm > bounds && tm > P(0)) {
-                P s = bounds / tm;
+            // the forces only feed the R Hessian: in the split mode they are
+            // formed in R from the P lambda (the dual accumulates lambda in P)
+            using F = std::conditional_t<std::is_same<P, R>::value, P, R>;
+            F f0p = F(c.penalty.x * c0) + F(c.lambda.x);
+            f0p = std::fmin(f0p, F(0));  // f32::min: NaN-ignoring
+            F f1r = F(c.penalty.y * c1) + F(c.lambda.y);
+            F f2r = F(c.penalty.z * c2) + F(c.lambda.z);
+            F bounds = std::fabs(f0p) * F(c.friction);
+            F tm = std::sqrt(f1r * f1r + f2r * f2r);
+            F f1 = f1r, f2 = f2r;
+            if (tm > bounds && tm > F(0)) {
+                F s = bounds / tm;
                 f1 = f1r * s;
                 f2 = f2r * s;
             }
@@ -1280,7 +1299,10 @@ struct Avbd {
         R dx[6];
         solve6(H, rhs, dx);
         B.pos[wr][i] = sp + cast3<P>(V3<R>{dx[0], dx[1], dx[2]});
-        B.rot[wr][i] = quat_step(sq, cast3<P>(V3<R>{dx[3], dx[4], dx[5]}));
+        if constexpr (std::is_same<P, R>::value)
+            B.rot[wr][i] = quat_step(sq, V3<P>{dx[3], dx[4], dx[5]});
+        else
+            B.rot[wr][i] = quat_step_split<P, R>(sq, V3<R>{dx[3], dx[4], dx[5]});
     }
 
     // avbd_dual, avbd/src/lib.rs:565-663; `rd` is the buffer holding the new
