@@ -142,15 +142,20 @@ __device__ __forceinline__ void init_body(const DevWorld<P, R>& w, uint32_t i, c
         w.mdt2[i] = A4<R>{mass / dt2, idt2.x, idt2.y, idt2.z};
     }
     if (inv_mass > R(0)) {
-        V3<P> accel = divs(sub(vel, xyz(w.prev_vel[i])), dt);
-        P gm = length(g);
-        P wgt = P(0);
-        if (gm > P(0)) {
-            wgt = dot(accel, divs(g, gm)) / gm;
-            wgt = wgt < P(0) ? P(0) : (wgt > P(1) ? P(1) : wgt);
+        // adaptive gravity weight, clamped to [0, 1]: formed in R in the split
+        // mode (it only scales the warm-start offset)
+        using Fq = std::conditional_t<std::is_same<P, R>::value, P, R>;
+        const Fq dtf = Fq(o.dt);
+        const V3<Fq> gf{Fq(o.gx), Fq(o.gy), Fq(o.gz)};
+        V3<Fq> accel = divs(cast3<Fq>(sub(vel, xyz(w.prev_vel[i]))), dtf);
+        Fq gm = length(gf);
+        Fq wgt = Fq(0);
+        if (gm > Fq(0)) {
+            wgt = dot(accel, divs(gf, gm)) / gm;
+            wgt = wgt < Fq(0) ? Fq(0) : (wgt > Fq(1) ? Fq(1) : wgt);
         }
-        w.pos[0][i] = pack(add(add(pos, scale(vel, dt)), scale(g, wgt * dt * dt)));
-        w.rot[0][i] = packq(quat_step(rot, scale(ang, dt)));
+        w.pos[0][i] = pack(add(add(pos, scale(vel, dt)), scale(g, P(wgt) * dt * dt)));
+        w.rot[0][i] = packq(irot);  // the same quat_step(rot, ang dt)
     }
 }
 
@@ -553,10 +558,17 @@ __device__ __forceinline__ void recover_body(const DevWorld<P, R>& w, uint32_t i
     P dt = P(o.dt);
     A4<P> v = w.vel[i];
     w.prev_vel[i] = v;
-    const V3<P> nv = divs(sub(xyz(p4), xyz(w.init_pos[i])), dt);
+    const Q4<P> rel = qmul(quat(q4), conj(quat(w.init_rot[i])));
+    V3<P> nv, na;
+    if constexpr (std::is_same<P, R>::value) {
+        nv = divs(sub(xyz(p4), xyz(w.init_pos[i])), dt);
+        na = divs(V3<P>{P(2) * rel.x, P(2) * rel.y, P(2) * rel.z}, dt);
+    } else {  // split mode: one division, then products (within an ulp of P)
+        const P inv_dt = P(1) / dt;
+        nv = scale(sub(xyz(p4), xyz(w.init_pos[i])), inv_dt);
+        na = scale(V3<P>{P(2) * rel.x, P(2) * rel.y, P(2) * rel.z}, inv_dt);
+    }
     w.vel[i] = pack(nv);
-    Q4<P> rel = qmul(quat(q4), conj(quat(w.init_rot[i])));
-    const V3<P> na = divs(V3<P>{P(2) * rel.x, P(2) * rel.y, P(2) * rel.z}, dt);
     w.ang[i] = pack(na);
     // a non-finite pose or velocity is reported (DIO_ERR_NONFINITE), as the
     // reference demos' constraint tracing reports it (demos/constraints/src/main.rs:24-60)

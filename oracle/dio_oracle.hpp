@@ -1162,15 +1162,20 @@ struct Avbd {
         B.inert_lin[i] = ip;
         B.inert_ang[i] = quat_step(rot, st.ang * dt);
         if (st.inv_mass > R(0)) {
-            V3<P> accel = divs(st.vel - st.prev_vel, dt);
-            P gm = length(g);
-            P w = P(0);
-            if (gm > P(0)) {
-                w = dot(accel, divs(g, gm)) / gm;
-                w = w < P(0) ? P(0) : (w > P(1) ? P(1) : w);
+            // adaptive gravity weight, clamped to [0, 1]: formed in R in the
+            // split mode (it only scales the warm-start offset)
+            using F = std::conditional_t<std::is_same<P, R>::value, P, R>;
+            const F dtf = F(o.dt);
+            const V3<F> gf = cast3<F>(o.gravity);
+            V3<F> accel = divs(cast3<F>(st.vel - st.prev_vel), dtf);
+            F gm = length(gf);
+            F w = F(0);
+            if (gm > F(0)) {
+                w = dot(accel, divs(gf, gm)) / gm;
+                w = w < F(0) ? F(0) : (w > F(1) ? F(1) : w);
             }
-            B.pos[0][i] = pos + st.vel * dt + g * (w * dt * dt);
-            B.rot[0][i] = quat_step(rot, st.ang * dt);
+            B.pos[0][i] = pos + st.vel * dt + g * (P(w) * dt * dt);
+            B.rot[0][i] = B.inert_ang[i];  // the same quat_step(rot, ang dt)
         } else {
             B.pos[0][i] = pos;
             B.rot[0][i] = rot;
@@ -1354,9 +1359,15 @@ struct Avbd {
         Qt<P> rot = B.rot[rd][i];
         P dt = P(o.dt);
         st.prev_vel = st.vel;
-        st.vel = divs(pos - B.init_lin[i], dt);
         Qt<P> rel = qmul(rot, conj(B.init_ang[i]));
-        st.ang = divs(V3<P>{P(2) * rel.x, P(2) * rel.y, P(2) * rel.z}, dt);
+        if constexpr (std::is_same<P, R>::value) {
+            st.vel = divs(pos - B.init_lin[i], dt);
+            st.ang = divs(V3<P>{P(2) * rel.x, P(2) * rel.y, P(2) * rel.z}, dt);
+        } else {  // split mode: one division, then products (within an ulp of P)
+            const P inv_dt = P(1) / dt;
+            st.vel = (pos - B.init_lin[i]) * inv_dt;
+            st.ang = V3<P>{P(2) * rel.x, P(2) * rel.y, P(2) * rel.z} * inv_dt;
+        }
     }
 };
 
