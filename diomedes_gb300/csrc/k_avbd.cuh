@@ -306,12 +306,19 @@ __device__ __forceinline__ void primal_jview_p(const JView& jv, A4<P> op4, A4<P>
     const uint32_t kind = jv.kind & ~kIsB;
     const V3<R> anc_s{R(jv.self_anchor.x), R(jv.self_anchor.y), R(jv.self_anchor.z)};
     const V3<R> anc_o{R(jv.other_anchor.x), R(jv.other_anchor.y), R(jv.other_anchor.z)};
-    // anchor offsets are rotated in R (small body-frame vectors) and added to
-    // the P positions; with P == R this is the reference's expression
     const V3<R> r_self = rotate(sqr, anc_s);
-    const V3<P> p_self = add(sp, cast3<P>(r_self));
-    const V3<P> p_other = add(xyz(op4), cast3<P>(rotate(castq<R>(quat(oq4)), anc_o)));
-    const V3<R> delta = cast3<R>(is_a ? sub(p_self, p_other) : sub(p_other, p_self));
+    V3<R> delta;  // joint a's anchor point minus joint b's
+    if constexpr (std::is_same<P, R>::value) {
+        const V3<P> p_self = add(sp, r_self);
+        const V3<P> p_other = add(xyz(op4), rotate(quat(oq4), anc_o));
+        delta = is_a ? sub(p_self, p_other) : sub(p_other, p_self);
+    } else {
+        // split mode: the position difference in P, the anchor offsets (small
+        // body-frame vectors) rotated and differenced in R
+        const V3<R> r_other = rotate(castq<R>(quat(oq4)), anc_o);
+        delta = is_a ? add(cast3<R>(sub(sp, xyz(op4))), sub(r_self, r_other))
+                     : add(cast3<R>(sub(xyz(op4), sp)), sub(r_other, r_self));
+    }
     const R sign = is_a ? R(1) : R(-1);
     const R stiff = R(jv.other_anchor.w);
     if (kind == DIO_CONSTRAINT_BALL_SOCKET) {

@@ -122,8 +122,8 @@ inline Qt<R> quat_step(Qt<R> q, V3<R> d) {
 }
 // quat_step of the split mode: the increment (d, 0) * q / 2 is formed in R
 // from the rounded quaternion and added to the P quaternion; 1/|q| is seeded
-// in R (correctly rounded sqrt and division) and refined by two Newton steps
-// in P, which reach P accuracy.
+// in R (correctly rounded sqrt and division) and refined by one Newton step
+// in P (relative error ~1e-14; the quaternion is renormalised every step).
 template <class P, class R>
 inline Qt<P> quat_step_split(Qt<P> q, V3<R> d) {
     Qt<R> s = qmul(Qt<R>{d.x, d.y, d.z, R(0)}, castq<R>(q));
@@ -131,7 +131,6 @@ inline Qt<P> quat_step_split(Qt<P> q, V3<R> d) {
     const Qt<P> u{q.x + P(s.x), q.y + P(s.y), q.z + P(s.z), q.w + P(s.w)};
     const P n = u.x * u.x + u.y * u.y + u.z * u.z + u.w * u.w;
     P r = P(R(1) / std::sqrt(R(n)));
-    r = r * (P(1.5) - P(0.5) * n * r * r);
     r = r * (P(1.5) - P(0.5) * n * r * r);
     return {u.x * r, u.y * r, u.z * r, u.w * r};
 }
@@ -1266,13 +1265,19 @@ struct Avbd {
             V3<P> pb = !is_a ? sp : B.pos[rd][jt.b];
             Qt<P> qa = is_a ? sq : B.rot[rd][jt.a];
             Qt<P> qb = !is_a ? sq : B.rot[rd][jt.b];
-            // anchor offsets rotated in R (body-frame vectors), added to the
-            // P positions: identical to the reference's form when P == R
-            V3<P> wpa = pa + cast3<P>(rotate(castq<R>(qa), jt.anchor_a));
-            V3<P> wpb = pb + cast3<P>(rotate(castq<R>(qb), jt.anchor_b));
             V3<R> self_anchor = is_a ? jt.anchor_a : jt.anchor_b;
             R sign = is_a ? R(1) : R(-1);
-            V3<R> delta = cast3<R>(wpa - wpb);
+            V3<R> delta;
+            if constexpr (std::is_same<P, R>::value) {
+                V3<P> wpa = pa + rotate(qa, jt.anchor_a);
+                V3<P> wpb = pb + rotate(qb, jt.anchor_b);
+                delta = wpa - wpb;
+            } else {
+                // split mode: the position difference in P, the anchor
+                // offsets (small body-frame vectors) rotated and differenced in R
+                delta = cast3<R>(pa - pb) +
+                        (rotate(castq<R>(qa), jt.anchor_a) - rotate(castq<R>(qb), jt.anchor_b));
+            }
             V3<R> r_self = rotate(sqr, self_anchor);
             R stiff = jt.bw;
             if (jt.kind == BALL_SOCKET) {
