@@ -204,13 +204,26 @@ __device__ __forceinline__ void row_forces(const RowDual<P, R>& du, R mu, R c0, 
     const P f1r = P(du.penalty.y * c1) + du.lambda.y;
     const P f2r = P(du.penalty.z * c2) + du.lambda.z;
     bounds = dabs(f0) * P(mu);
-    tm = dsqrt(f1r * f1r + f2r * f2r);
     f1 = f1r;
     f2 = f2r;
-    if (tm > bounds && tm > P(0)) {
-        const P s = bounds / tm;
-        f1 = f1r * s;
-        f2 = f2r * s;
+    if constexpr (std::is_same<P, R>::value) {
+        tm = dsqrt(f1r * f1r + f2r * f2r);
+        if (tm > bounds && tm > P(0)) {
+            const P s = bounds / tm;
+            f1 = f1r * s;
+            f2 = f2r * s;
+        }
+    } else {
+        // split mode: the cone magnitude and its scale factor in R, applied to
+        // the P forces (lambda still accumulates in P)
+        const R f1q = R(f1r), f2q = R(f2r);
+        const R tmr = dsqrt(f1q * f1q + f2q * f2q);
+        tm = P(tmr);
+        if (tm > bounds && tm > P(0)) {
+            const R sr = R(bounds) / tmr;
+            f1 = f1r * P(sr);
+            f2 = f2r * P(sr);
+        }
     }
 }
 

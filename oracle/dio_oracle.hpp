@@ -1341,12 +1341,25 @@ struct Avbd {
         P f1r = P(c.penalty.y * c1) + c.lambda.y;
         P f2r = P(c.penalty.z * c2) + c.lambda.z;
         P bounds = std::fabs(f0) * P(c.friction);
-        P tm = std::sqrt(f1r * f1r + f2r * f2r);
-        P f1 = f1r, f2 = f2r;
-        if (tm > bounds && tm > P(0)) {
-            P s = bounds / tm;
-            f1 = f1r * s;
-            f2 = f2r * s;
+        P tm, f1 = f1r, f2 = f2r;
+        if constexpr (std::is_same<P, R>::value) {
+            tm = std::sqrt(f1r * f1r + f2r * f2r);
+            if (tm > bounds && tm > P(0)) {
+                P s = bounds / tm;
+                f1 = f1r * s;
+                f2 = f2r * s;
+            }
+        } else {
+            // split mode: the cone magnitude and its scale factor in R, applied
+            // to the P forces (lambda still accumulates in P)
+            const R f1q = R(f1r), f2q = R(f2r);
+            const R tmr = std::sqrt(f1q * f1q + f2q * f2q);
+            tm = P(tmr);
+            if (tm > bounds && tm > P(0)) {
+                const R sr = R(bounds) / tmr;
+                f1 = f1r * P(sr);
+                f2 = f2r * P(sr);
+            }
         }
         c.lambda = {f0, f1, f2};
         if (f0 < P(0)) c.penalty.x = std::fmin(c.penalty.x + o.beta_lin * std::fabs(c0), o.penalty_max);
