@@ -10,7 +10,9 @@ One JSON line on rank 0:
              library's stream, K steps, max over ranks)
   e2e        the same metric through the public API with pinned host buffers:
              every step re-uploads poses + state (dio_world_set_state) and
-             reads poses + state back (dio_world_download)
+             reads poses + state back (dio_world_download); timed with the
+             batch as one world and as several worlds on several streams
+             (dio_worlds_step_host), the faster reported
   plain      the one-scene-per-launch path (one context per scene) on a
              sample of scenes, for the batched-vs-plain ratio
   roofline   the primal kernel: algorithmic bytes per launch / event time
@@ -44,10 +46,14 @@ def parse():
     ap.add_argument("--scenes", type=int, default=1024)
     ap.add_argument("--plain-scenes", type=int, default=128)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--e2e-worlds", type=int, default=4,
+                    help="e2e: the batch as this many worlds on as many streams (dio_worlds_step_host)")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-f64", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="keep the default configuration (profiling runs)")
+    ap.add_argument("--precision", default="f32", choices=["f32", "split"],
+                    help="arithmetic of the timed world (split: FP64 poses / lambda, FP32 Hessian)")
     return ap.parse_args()
 
 
@@ -223,7 +229,8 @@ def main():
 
     sc = scenes.batched(n_scenes=args.scenes, seed=4 + 1000 * rank)
     stream = torch.cuda.current_stream()
-    w = compute.World(world_capacity(sc), profile=0)
+    prec = 1 if args.precision == "split" else 0
+    w = compute.World(world_capacity(sc), profile=0, precision=prec)
     w.set_stream(stream.cuda_stream)
     w.upload(sc.bodies, sc.state, **sc.upload_kwargs())
     o = sc.options
@@ -251,6 +258,7 @@ def main():
     ms = e0.elapsed_time(e1)
     st = w.stats()
     b32_after, _ = w.download()  # for the FP64 comparison below
+    p_after, q_after = w.download_f64() if prec else (None, None)
     rows_after = w.contacts()
 
     # a second pass of the same K steps with the per-phase / per-launch event
@@ -286,16 +294,18 @@ def main():
     cont_rows = int((rows_now["b"] == 0xFFFFFFFF).sum())
     pg = primal_gather_bytes(n_dyn, len(rows_now) - cont_rows, cont_rows, j_inc)
 
-    # end to end through the public API with host buffers
+    # end to end through the public API with host buffers: the demos'
+    # per-frame loop (upload poses + state, step, read them back)
     e2e = None
     if not args.no_e2e:
-        # the caller's host buffers: page-locked (cudaHostAlloc through torch)
+        # the caller's host arrays: page-locked (cudaHostAlloc through torch)
         hb = torch.empty(sc.n * sc.bodies.dtype.itemsize, dtype=torch.uint8,
                          pin_memory=True).numpy().view(sc.bodies.dtype)
         hs = torch.empty(sc.n * sc.state.dtype.itemsize, dtype=torch.uint8,
                          pin_memory=True).numpy().view(sc.state.dtype)
         w.download_into(hb, hs)
         k2 = max(3, args.steps // 2)
+        # (1) the batch as one world: set_state, dio_step, download in series
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(k2):
@@ -303,9 +313,33 @@ def main():
             w.step(o, 1)
             w.download_into(hb, hs)
         t1 = time.perf_counter()
-        e2e = {"value": total_bodies * k2 / (t1 - t0), "unit": "body-steps/s",
+        single = total_bodies * k2 / (t1 - t0)
+        # (2) the same batch as G worlds (contiguous runs of whole scenes) on
+        # G streams, stepped by dio_worlds_step_host: one world's host copies
+        # overlap the other worlds' steps
+        parts, starts = sc.split(args.e2e_worlds)
+        worlds, streams, vb, vs = [], [], [], []
+        for p, lo in zip(parts, starts):
+            wg = compute.World(world_capacity(p), profile=0, precision=prec)
+            streams.append(torch.cuda.Stream())
+            wg.set_stream(streams[-1].cuda_stream)
+            wg.upload(p.bodies, p.state, **p.upload_kwargs())
+            wg.configure(primal_variant=tuned["primal_variant"], bvh_rebuild_period=tuned["bvh_rebuild_period"])
+            worlds.append(wg)
+            vb.append(hb[lo:lo + p.n])
+            vs.append(hs[lo:lo + p.n])
+        compute.step_host(worlds, vb, vs, o, args.warmup)  # from the state reached above
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        compute.step_host(worlds, vb, vs, o, k2)
+        t1 = time.perf_counter()
+        piped = total_bodies * k2 / (t1 - t0)
+        for wg in worlds:
+            wg.close()
+        e2e = {"value": max(piped, single), "unit": "body-steps/s",
                "h2d_bytes_per_step": int(hb.nbytes + hs.nbytes), "d2h_bytes_per_step": int(hb.nbytes + hs.nbytes),
-               "steps": k2}
+               "steps": k2, "worlds": len(parts) if piped >= single else 1,
+               "one_world": single, "worlds_on_streams": {"worlds": len(parts), "value": piped}}
 
     # plain path: one context per scene, stepped one scene at a time
     plain = None
@@ -364,35 +398,36 @@ def main():
         def max_pen(rows):  # deepest row of the last step: depth = margin - c0.x
             return float((o.margin - rows["c0"][:, 0]).max()) if len(rows) else 0.0
 
-        err = pos_err(b32["position"][:, :3].astype(np.float64))
-        aerr = ang_err(b32["orientation"])
+        err = pos_err(p_after if prec else b32["position"][:, :3].astype(np.float64))
+        aerr = ang_err(q_after if prec else b32["orientation"])
         f64 = {"max_pos_err_m": float(err.max()), "median_pos_err_m": float(np.median(err)),
                "max_angle_err_rad": float(aerr.max()), "median_angle_err_rad": float(np.median(aerr)),
                "max_penetration_m": max_pen(rows_after), "max_penetration_m_fp64": max_pen(rows64),
                "steps": steps_done}
-        # the split-precision path on the same batch (FP64 poses / inertial
-        # terms / lambda, FP32 Hessian, LDL^T and detection): throughput and
-        # its own error against the FP64 world
-        ws = compute.World(world_capacity(sc), precision=1)
-        ws.set_stream(stream.cuda_stream)
-        ws.upload(sc.bodies, sc.state, **sc.upload_kwargs())
-        ws.configure(primal_variant=tuned["primal_variant"], bvh_rebuild_period=tuned["bvh_rebuild_period"])
-        ws.step(o, args.warmup)
-        torch.cuda.synchronize()
-        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        s0.record(stream)
-        ws.step(o, args.steps)
-        s1.record(stream)
-        torch.cuda.synchronize()
-        ps, qs = ws.download_f64()
-        rows_s = ws.contacts()
-        ws.close()
-        es, ea = pos_err(ps), ang_err(qs)
-        f64["split"] = {"value": sc.n * args.steps / (s0.elapsed_time(s1) / 1e3), "unit": "body-steps/s",
-                        "batched_over_plain": (sc.n * args.steps / (s0.elapsed_time(s1) / 1e3)) / plain["value"]
-                        if plain else None,
-                        "max_pos_err_m": float(es.max()), "median_pos_err_m": float(np.median(es)),
-                        "max_angle_err_rad": float(ea.max()), "max_penetration_m": max_pen(rows_s)}
+        if not prec:  # the timed world is FP32: time the split path beside it
+            # the split-precision path on the same batch (FP64 poses / inertial
+            # terms / lambda, FP32 Hessian, LDL^T and detection): throughput and
+            # its own error against the FP64 world
+            ws = compute.World(world_capacity(sc), precision=1)
+            ws.set_stream(stream.cuda_stream)
+            ws.upload(sc.bodies, sc.state, **sc.upload_kwargs())
+            ws.configure(primal_variant=tuned["primal_variant"], bvh_rebuild_period=tuned["bvh_rebuild_period"])
+            ws.step(o, args.warmup)
+            torch.cuda.synchronize()
+            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s0.record(stream)
+            ws.step(o, args.steps)
+            s1.record(stream)
+            torch.cuda.synchronize()
+            ps, qs = ws.download_f64()
+            rows_s = ws.contacts()
+            ws.close()
+            es, ea = pos_err(ps), ang_err(qs)
+            f64["split"] = {"value": sc.n * args.steps / (s0.elapsed_time(s1) / 1e3), "unit": "body-steps/s",
+                            "batched_over_plain": (sc.n * args.steps / (s0.elapsed_time(s1) / 1e3)) / plain["value"]
+                            if plain else None,
+                            "max_pos_err_m": float(es.max()), "median_pos_err_m": float(np.median(es)),
+                            "max_angle_err_rad": float(ea.max()), "max_penetration_m": max_pen(rows_s)}
 
     cpu = None
     if not args.no_cpu and rank == 0:
@@ -408,7 +443,8 @@ def main():
         line = {
             "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64/f32 split" if prec else "f32",
+            "data": "synthetic",
             "config": {"workload": f"batched {sc.n_scenes} scenes (rope / ball-socket / spring chains + loose "
                                    f"boxes), {sc.n} bodies per GPU, dt 1/60, 10 iterations",
                        "bodies_per_gpu": sc.n, "contacts_last_step": st["contacts"],

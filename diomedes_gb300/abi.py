@@ -152,6 +152,8 @@ _PROTOS = {
     "dio_world_export_transforms": [_P, _u32, _vp, _vp, ctypes.c_size_t],
     "dio_step_async": [_P, ctypes.POINTER(AvbdOptions), _u32],
     "dio_world_download_async": [_P, _vp, _vp],
+    "dio_worlds_step_host": [ctypes.POINTER(_P), _u32, ctypes.POINTER(_vp), ctypes.POINTER(_vp),
+                             ctypes.POINTER(AvbdOptions), _u32],
     "dio_world_checkpoint": [_P, _vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)],
     "dio_world_resume": [_P, _vp, ctypes.c_size_t],
     "dio_autotune": [_P, ctypes.POINTER(AvbdOptions), _u32, ctypes.c_char_p, ctypes.POINTER(Config)],

@@ -184,6 +184,28 @@ class AvbdCompute(Context):
         return out[: m.value].copy(), offsets, indices[: offsets[-1]].copy()
 
 
+def step_host(worlds, bodies, states, options, steps=1):
+    """dio_worlds_step_host: the per-frame upload / step / read-back loop over
+    a batch held as several worlds (one per stream).  bodies[g] / states[g]
+    are world g's host arrays (page-locked for overlapped copies), updated in
+    place; returns after every world has finished."""
+    n = len(worlds)
+    if not (len(bodies) == len(states) == n):
+        raise ValueError("one bodies and one state array per world")
+    for g in range(n):
+        if len(bodies[g]) != worlds[g].n or len(states[g]) != worlds[g].n:
+            raise ValueError(f"world {g}: arrays must hold {worlds[g].n} bodies")
+        if not (bodies[g].flags.c_contiguous and states[g].flags.c_contiguous):
+            raise ValueError(f"world {g}: arrays must be contiguous (updated in place)")
+    hs = (ctypes.c_void_p * n)(*[w.h for w in worlds])
+    bp = (ctypes.c_void_p * n)(*[ptr(b) for b in bodies])
+    sp = (ctypes.c_void_p * n)(*[ptr(s) for s in states])
+    rc = abi.lib().dio_worlds_step_host(hs, n, bp, sp, ctypes.byref(options), steps)
+    if rc != abi.DIO_OK:
+        failed = next((w.h for w in worlds if abi.lib().dio_ctx_last_error(w.h)), None)
+        check(rc, failed, "dio_worlds_step_host")
+
+
 def checkpoint_header(image):
     """The header fields of a checkpoint image (abi.CKPT_HEADER)."""
     return np.frombuffer(image[: abi.CKPT_HEADER.itemsize], abi.CKPT_HEADER)[0]

@@ -272,6 +272,37 @@ int dio_world_set_state(DioCtx* ctx, const DioGpuBody* bodies, const DioBodyStat
 int dio_world_download(DioCtx* ctx, DioGpuBody* bodies, DioBodyState* state) {
     return with_world(ctx, false, [&](dio::EngineBase* e) { return e->download(bodies, state); });
 }
+int dio_worlds_step_host(DioCtx* const* ctxs, uint32_t count, DioGpuBody* const* bodies,
+                         DioBodyState* const* states, const DioAvbdOptions* options, uint32_t steps) {
+    if (!count) return DIO_OK;
+    if (!ctxs || !bodies || !states || !options) return DIO_ERR_INVALID;
+    for (uint32_t g = 0; g < count; ++g)
+        if (!ctxs[g] || !bodies[g] || !states[g]) return DIO_ERR_INVALID;
+    int rc = DIO_OK;
+    // every world's state copy is queued (behind that world's previous
+    // read-back) before the host waits on any of them; world g is stepped as
+    // soon as its own copy and dynamic-set check are done, while the copies of
+    // the worlds after it run beside its step
+    for (uint32_t k = 0; k < steps && !rc; ++k) {
+        for (uint32_t g = 0; g < count && !rc; ++g)
+            rc = with_world(ctxs[g], false,
+                            [&](dio::EngineBase* e) { return e->set_state_begin(bodies[g], states[g]); });
+        for (uint32_t g = 0; g < count && !rc; ++g) {
+            rc = with_world(ctxs[g], false, [&](dio::EngineBase* e) { return e->set_state_end(); });
+            if (!rc) rc = dio_step_async(ctxs[g], options, 1);
+            if (!rc) rc = dio_world_download_async(ctxs[g], bodies[g], states[g]);
+        }
+    }
+    // a failure can leave a begun state update: finish it so the world stays usable
+    if (rc)
+        for (uint32_t g = 0; g < count; ++g)
+            with_world(ctxs[g], false, [&](dio::EngineBase* e) { return e->set_state_end(); });
+    for (uint32_t g = 0; g < count; ++g) {
+        int s = dio_ctx_synchronize(ctxs[g]);
+        if (!rc) rc = s;
+    }
+    return rc;
+}
 int dio_world_download_f64(DioCtx* ctx, double* positions, double* orientations) {
     return with_world(ctx, false, [&](dio::EngineBase* e) { return e->download_f64(positions, orientations); });
 }

@@ -39,6 +39,11 @@ struct EngineBase {
     virtual int download_async(DioGpuBody* bodies, DioBodyState* state) = 0;
     virtual int sync_check() = 0;  // synchronise and report the device error flags
     virtual int set_state(const DioGpuBody* bodies, const DioBodyState* state) = 0;
+    // set_state in two halves: _begin enqueues the copies, the unpacking and
+    // the device check of the dynamic-body set; _end waits for that check and
+    // rebuilds the dynamic-body list if the set changed
+    virtual int set_state_begin(const DioGpuBody* bodies, const DioBodyState* state) = 0;
+    virtual int set_state_end() = 0;
     virtual int download(DioGpuBody* bodies, DioBodyState* state) = 0;
     virtual int download_f64(double* positions, double* orientations) = 0;
     virtual int contacts(DioContact* out, uint32_t cap, uint32_t* m) = 0;

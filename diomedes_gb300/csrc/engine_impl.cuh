@@ -898,7 +898,12 @@ class Engine final : public EngineBase {
     int sync_check() override { return check_flags(); }
 
     int set_state(const DioGpuBody* bodies, const DioBodyState* state) override {
+        DIO_TRY(set_state_begin(bodies, state));
+        return set_state_end();
+    }
+    int set_state_begin(const DioGpuBody* bodies, const DioBodyState* state) override {
         if (!world_ready_) return state_err("no world uploaded");
+        if (state_pending_) return state_err("set_state_begin twice without set_state_end");
         uint32_t n = w_.n;
         if (bodies) {
             DioGpuBody* db = reinterpret_cast<DioGpuBody*>(dstage_);
@@ -906,10 +911,32 @@ class Engine final : public EngineBase {
             k_set_pose<P, R><<<grid_for(n, 256), 256, 0, stream_>>>(w_, db, n);
             ++launches_;
         }
-        if (state) {
-            DIO_TRY(upload_state(state, n, true));
+        if (state && n) {
+            DioBodyState* ds = reinterpret_cast<DioBodyState*>(reinterpret_cast<char*>(dstage_) +
+                                                               align256((size_t)n * sizeof(DioGpuBody)));
+            DIO_CK(cudaMemcpyAsync(ds, state, (size_t)n * sizeof(DioBodyState), cudaMemcpyHostToDevice, stream_));
+            k_unpack_state<P, R><<<grid_for(n, 256), 256, 0, stream_>>>(w_, ds, n);
             ++launches_;
+            if (dyn_list_n_ == n) {
+                // the list is kept unless a body turned static or dynamic
+                DIO_CK(cudaMemsetAsync(&ctr_->dyn_changed, 0, 4, stream_));
+                k_dyn_changed<P, R><<<grid_for(n, 256), 256, 0, stream_>>>(w_, n, dyn_keep_, &ctr_->dyn_changed);
+                DIO_CK(cudaMemcpyAsync(&hctr_->dyn_changed, &ctr_->dyn_changed, 4, cudaMemcpyDeviceToHost, stream_));
+                state_pending_ = 1;
+            } else {
+                state_pending_ = 2;
+            }
         }
+        return DIO_OK;
+    }
+    int set_state_end() override {
+        int pending = state_pending_;
+        state_pending_ = 0;
+        if (pending == 1) {
+            DIO_CK(cudaStreamSynchronize(stream_));
+            if (!hctr_->dyn_changed) return DIO_OK;
+        }
+        if (pending) return build_dyn_list(w_.n);
         return DIO_OK;
     }
 
@@ -1063,23 +1090,13 @@ class Engine final : public EngineBase {
         w_.n = n;
         return DIO_OK;
     }
-    // keep_list: the body count and set of dynamic bodies are expected to be
-    // unchanged (a state update of the same world): the list is rebuilt only
-    // if a body changed between static and dynamic
-    int upload_state(const DioBodyState* state, uint32_t n, bool keep_list = false) {
+    int upload_state(const DioBodyState* state, uint32_t n) {
         if (!n) return DIO_OK;
         if (!state) return inval("null state");
         DioBodyState* ds = reinterpret_cast<DioBodyState*>(reinterpret_cast<char*>(dstage_) +
                                                            align256((size_t)n * sizeof(DioGpuBody)));
         DIO_CK(cudaMemcpyAsync(ds, state, (size_t)n * sizeof(DioBodyState), cudaMemcpyHostToDevice, stream_));
         k_unpack_state<P, R><<<grid_for(n, 256), 256, 0, stream_>>>(w_, ds, n);
-        if (keep_list && dyn_list_n_ == n) {
-            DIO_CK(cudaMemsetAsync(&ctr_->dyn_changed, 0, 4, stream_));
-            k_dyn_changed<P, R><<<grid_for(n, 256), 256, 0, stream_>>>(w_, n, dyn_keep_, &ctr_->dyn_changed);
-            DIO_CK(cudaMemcpyAsync(&hctr_->dyn_changed, &ctr_->dyn_changed, 4, cudaMemcpyDeviceToHost, stream_));
-            DIO_CK(cudaStreamSynchronize(stream_));
-            if (!hctr_->dyn_changed) return DIO_OK;
-        }
         return build_dyn_list(n);
     }
     // compacted list of dynamic bodies (inverse mass != 0), index order
@@ -1990,6 +2007,7 @@ class Engine final : public EngineBase {
     std::vector<uint2> chunks_host_;
     uint2* chunks_ = nullptr;
     Slot<R>* slots_[2] = {nullptr, nullptr};
+    int state_pending_ = 0;    // set_state_begin left: 1 the dynamic-set check, 2 a list rebuild
     bool lag_primed_ = false;  // the previous step's slots are this mode's
     uint32_t* chunk_n_ = nullptr;
     uint32_t* chunk_ovf_ = nullptr;

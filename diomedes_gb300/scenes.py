@@ -36,6 +36,38 @@ class Scene:
     def n_scenes(self):
         return 1 if self.scene_offsets is None else len(self.scene_offsets) - 1
 
+    def split(self, groups):
+        """Contiguous runs of whole scenes with about equal body counts, as
+        separate Scenes (joints rebased; hull vertices shared).  Returns the
+        Scenes and the body offset of each in this one."""
+        off = np.zeros(2, np.int64) if self.scene_offsets is None else self.scene_offsets.astype(np.int64)
+        ns = len(off) - 1
+        groups = max(1, min(int(groups), ns))
+        cuts = [0]
+        for g in range(1, groups):
+            s = int(np.searchsorted(off, self.n * g / groups))
+            cuts.append(min(max(s, cuts[-1] + 1), ns - (groups - g)))
+        cuts.append(ns)
+        out, starts = [], []
+        for g in range(groups):
+            s0, s1 = cuts[g], cuts[g + 1]
+            lo, hi = int(off[s0]), int(off[s1])
+            c = self.constraints
+            keep = (c["a"] >= lo) & (c["a"] < hi)
+            c = c[keep].copy()
+            c["a"] -= lo
+            c["b"] -= lo
+            sub = Scene(f"{self.name}[{s0}:{s1}]", self.bodies[lo:hi].copy(), self.state[lo:hi].copy(),
+                        constraints=c, hull_vertices=self.hull_vertices, options=self.options, steps=self.steps,
+                        positions_f64=None if self.positions_f64 is None else self.positions_f64[lo:hi].copy())
+            if self.scene_offsets is not None:
+                sub.scene_offsets = (off[s0:s1 + 1] - lo).astype(np.uint32)
+            if self.containers is not None:
+                sub.containers = self.containers[s0:s1] if self.scene_offsets is not None else self.containers
+            out.append(sub)
+            starts.append(lo)
+        return out, starts
+
     def upload_kwargs(self):
         return dict(constraints=self.constraints, scene_offsets=self.scene_offsets, containers=self.containers,
                     hull_vertices=self.hull_vertices, positions_f64=self.positions_f64)

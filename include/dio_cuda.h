@@ -393,6 +393,17 @@ int dio_world_set_state(DioCtx* ctx, const DioGpuBody* bodies, const DioBodyStat
 /* AvbdSolver::sync_bodies_from_gpu, engine/src/physics/gpu.rs:212-237:
  * read the world's poses (FP32) and state back. Either pointer may be NULL. */
 int dio_world_download(DioCtx* ctx, DioGpuBody* bodies, DioBodyState* state);
+/* The demos' per-frame loop (demos/avbd_box/src/main.rs:232-257: upload the
+ * poses, step, read them back) over a batch held as `count` worlds, one per
+ * context: for each step and world in order, dio_world_set_state(bodies[g],
+ * states[g]), dio_step_async(1) and dio_world_download_async(bodies[g],
+ * states[g]).  Contexts on separate streams overlap one world's host copies
+ * with another world's steps; page-locked host arrays keep the copies
+ * asynchronous.  Every context is synchronised before the call returns (device
+ * error flags included); the first failure is returned and recorded on the
+ * context it came from.  No argument may be NULL; count == 0 is a no-op. */
+int dio_worlds_step_host(DioCtx* const* ctxs, uint32_t count, DioGpuBody* const* bodies,
+                         DioBodyState* const* states, const DioAvbdOptions* options, uint32_t steps);
 /* FP64 poses (exact in DIO_PREC_SPLIT / DIO_PREC_F64 worlds). */
 int dio_world_download_f64(DioCtx* ctx, double* positions, double* orientations);
 /* The last step's contact rows with their solved lambda / penalty. */

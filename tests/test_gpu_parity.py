@@ -306,6 +306,52 @@ def test_pipelined_frames_match_synchronous_steps():
         assert e.value.status == abi.DIO_ERR_NONFINITE
 
 
+def test_worlds_stepped_from_host_match_one_packed_world():
+    """dio_worlds_step_host over a batch split into three worlds on three
+    streams (host copies of one overlapping the others' steps) gives, frame
+    by frame, the bits of the packed world stepped by set_state / dio_step /
+    download; a non-finite state in one world is reported by the call."""
+    torch = pytest.importorskip("torch")
+    parts = [scenes.pyramid(levels=3), scenes.constraints_demo(), scenes.box_demo(),
+             scenes.cube_field(nx=3, nz=3, ny=2), scenes.mixed_pile(n=120, extent=3.0)]
+    for p in parts:
+        p.options = parts[0].options
+    packed = scenes.pack(parts)
+    frames = 5
+    with _world(packed) as w:
+        b, s = w.download()
+        for _ in range(frames):
+            w.set_state(b, s)
+            w.step(packed.options, 1)
+            b, s = w.download()
+
+    def pinned(dt):
+        return torch.empty(packed.n * dt.itemsize, dtype=torch.uint8, pin_memory=True).numpy().view(dt)
+
+    hb, hs = pinned(abi.BODY), pinned(abi.BODY_STATE)
+    hb[:], hs[:] = packed.bodies, packed.state
+    groups, starts = packed.split(3)
+    streams = [torch.cuda.Stream() for _ in groups]
+    worlds = [_world(g) for g in groups]
+    try:
+        for wg, st in zip(worlds, streams):
+            wg.set_stream(st.cuda_stream)
+        vb = [hb[lo:lo + g.n] for g, lo in zip(groups, starts)]
+        vs = [hs[lo:lo + g.n] for g, lo in zip(groups, starts)]
+        compute.step_host(worlds, vb, vs, packed.options, 2)
+        compute.step_host(worlds, vb, vs, packed.options, frames - 2)
+        assert np.array_equal(_bits(hb), _bits(b)) and np.array_equal(_bits(hs), _bits(s))
+        bad = hs.copy()
+        bad["vel"][starts[1] + 1, 0] = np.nan
+        vs[1][:] = bad[starts[1]:starts[1] + groups[1].n]
+        with pytest.raises(abi.DioError) as e:
+            compute.step_host(worlds, vb, vs, packed.options, 1)
+        assert e.value.status == abi.DIO_ERR_NONFINITE
+    finally:
+        for wg in worlds:
+            wg.close()
+
+
 def test_transform_export_matches_the_poses():
     """Headless transform export into a device buffer: pose records are the
     downloaded poses; model matrices are translation * rotation * scale built

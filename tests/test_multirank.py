@@ -59,6 +59,30 @@ def _rank(rank, world, port, q):
         dist.destroy_process_group()
 
 
+def test_scene_split_is_contiguous_complete_and_rebased():
+    """Scene.split (the batch held as several worlds): contiguous runs of whole
+    scenes covering every body once, joints rebased into their run."""
+    from diomedes_gb300 import scenes
+
+    sc = scenes.batched(n_scenes=40, lo=16, hi=256, seed=7)
+    for groups in (1, 3, 7, 40, 99):
+        parts, starts = sc.split(groups)
+        assert len(parts) == min(groups, sc.n_scenes)
+        assert starts[0] == 0 and all(p.n > 0 for p in parts)
+        assert [s + p.n for s, p in zip(starts, parts)][:-1] == starts[1:]
+        assert starts[-1] + parts[-1].n == sc.n
+        assert sum(p.n_scenes for p in parts) == sc.n_scenes
+        assert sum(len(p.constraints) for p in parts) == len(sc.constraints)
+        for p, lo in zip(parts, starts):
+            assert np.array_equal(p.bodies.view(np.uint8), sc.bodies[lo:lo + p.n].view(np.uint8))
+            assert p.scene_offsets[0] == 0 and p.scene_offsets[-1] == p.n
+            assert len(p.containers) == p.n_scenes
+            if len(p.constraints):
+                assert p.constraints["a"].max() < p.n and p.constraints["b"].max() < p.n
+    parts, _ = sc.split(4)
+    assert max(p.n for p in parts) < 0.5 * sc.n  # balanced by bodies, not by scenes
+
+
 def test_two_gloo_ranks_shard_and_reduce():
     pytest.importorskip("torch")
     ctx = mp.get_context("spawn")
