@@ -52,6 +52,10 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-f64", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="keep the default configuration (profiling runs)")
+    ap.add_argument("--save-state", default=None, metavar="PATH",
+                    help="after the timed region, write the world as a checkpoint image")
+    ap.add_argument("--load-state", default=None, metavar="PATH",
+                    help="resume the world from a checkpoint image before the warm-up (profiling a late step)")
     ap.add_argument("--precision", default="f32", choices=["f32", "split"],
                     help="arithmetic of the timed world (split: FP64 poses / lambda, FP32 Hessian)")
     return ap.parse_args()
@@ -212,6 +216,8 @@ def reference_arm(args, rank):
 
 def main():
     args = parse()
+    if args.load_state:
+        args.no_f64 = True  # the FP64 comparison steps from the initial state
     rank, world, local = dist_info()
     if args.impl == "reference":
         return reference_arm(args, rank)
@@ -233,6 +239,9 @@ def main():
     w = compute.World(world_capacity(sc), profile=0, precision=prec)
     w.set_stream(stream.cuda_stream)
     w.upload(sc.bodies, sc.state, **sc.upload_kwargs())
+    if args.load_state:
+        with open(args.load_state, "rb") as f:
+            w.resume(f.read())
     o = sc.options
     if args.no_tune:
         c = w.configure()
@@ -257,6 +266,9 @@ def main():
         dist.barrier()
     ms = e0.elapsed_time(e1)
     st = w.stats()
+    if args.save_state:
+        with open(args.save_state, "wb") as f:
+            f.write(w.checkpoint())
     b32_after, _ = w.download()  # for the FP64 comparison below
     p_after, q_after = w.download_f64() if prec else (None, None)
     rows_after = w.contacts()
