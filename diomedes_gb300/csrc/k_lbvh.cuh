@@ -274,7 +274,10 @@ __global__ void __launch_bounds__(128) k_traverse(const uint32_t* leaf_body, con
 //               only subtrees holding positions > p, so each overlapping pair
 //               is found once, by its lower position; it is counted for body
 //               a = min(i, j) and appended as (a, b) to the chunk's scratch
-//               region (scratch_k slots per body of the chunk)
+//               region (scratch_k slots per body of the chunk).  The w slot
+//               of a leaf's min corner holds its body, of a node's min corner
+//               its highest leaf position, so one box load also brings the
+//               tag a traversal step tests
 //   write pass  places the scratch pairs at the scanned per-body offsets; a
 //               chunk whose scratch overflowed is traversed again and written
 //               directly (body i's partners j > i)
@@ -286,10 +289,18 @@ __host__ __device__ constexpr uint32_t scene_tree_cap() { return sizeof(R) == 4 
 template <class R>
 __host__ __device__ constexpr size_t scene_tree_bytes(uint32_t cap) {
     // leaf min/max, node min/max, children, leaf parent, node parent, visit
-    // flag (then per-body count), leaf body, leaf's scene root, node's
-    // highest leaf position
-    return (size_t)cap * (4 * sizeof(A4<R>) + sizeof(uint2) + 6 * sizeof(uint32_t)) + 16;
+    // flag (then per-body count), leaf's scene root
+    return (size_t)cap * (4 * sizeof(A4<R>) + sizeof(uint2) + 4 * sizeof(uint32_t)) + 16;
 }
+// a 32-bit tag in (and out of) the unused w slot of a box corner, as bits
+__device__ __forceinline__ uint32_t tag_of(const A4<float>& a) { return __float_as_uint(a.w); }
+__device__ __forceinline__ uint32_t tag_of(const A4<double>& a) { return (uint32_t)__double_as_longlong(a.w); }
+template <class R>
+__device__ __forceinline__ R tag_bits(uint32_t v);
+template <>
+__device__ __forceinline__ float tag_bits<float>(uint32_t v) { return __uint_as_float(v); }
+template <>
+__device__ __forceinline__ double tag_bits<double>(uint32_t v) { return __longlong_as_double((long long)v); }
 constexpr int kSceneTreeThreads = 1024;
 constexpr uint32_t kNoRoot = 0xFFFFFFFFu;
 
@@ -312,6 +323,117 @@ struct TreeArgs {
     uint32_t* chunk_ovf;
     uint32_t* err;
 };
+
+// Count-pass traversal from the leaf at chunk position p: pairs with leaves at
+// higher positions, counted for the lower body and appended to the chunk's
+// scratch.  Both children's boxes (and their tags) are loaded before either
+// is tested, so the loads of one step overlap.
+template <class R>
+__device__ __forceinline__ void tree_count_leaf(uint32_t p, uint32_t root, const A4<R>* lmn, const A4<R>* lmx,
+                                                const A4<R>* nmn, const A4<R>* nmx, const uint2* ch, uint32_t* vis,
+                                                uint32_t* s_cursor, uint2* dst, uint32_t region, uint32_t lo,
+                                                uint32_t* err) {
+    const A4<R> qmn = lmn[p], qmx = lmx[p];
+    const uint32_t i = tag_of(qmn);
+    uint32_t stack[kStack];
+    int sp = 0;
+    uint32_t node = root;
+    while (true) {
+        const uint2 c = ch[node];
+        const uint32_t cc[2] = {c.x, c.y};
+        A4<R> bmn[2], bmx[2];
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const uint32_t idx = cc[k] & ~kLeafFlag;
+            const bool leaf = cc[k] & kLeafFlag;
+            bmn[k] = (leaf ? lmn : nmn)[idx];
+            bmx[k] = (leaf ? lmx : nmx)[idx];
+        }
+        uint32_t n0 = 0, n1 = 0, push = 0;
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const uint32_t idx = cc[k] & ~kLeafFlag;
+            const bool leaf = cc[k] & kLeafFlag;
+            const uint32_t tag = tag_of(bmn[k]);  // a leaf's body, a node's highest leaf position
+            if (!((leaf ? idx : tag) > p && overlap(qmn, qmx, bmn[k], bmx[k]))) continue;
+            if (leaf) {
+                const uint32_t a = min(i, tag), b = max(i, tag);
+                atomicAdd(&vis[a - lo], 1u);
+                const uint32_t slot = atomicAdd(s_cursor, 1u);
+                if (slot < region) dst[slot] = make_uint2(a, b);
+            } else {
+                if (push == 0)
+                    n0 = idx;
+                else
+                    n1 = idx;
+                ++push;
+            }
+        }
+        if (push == 0) {
+            if (sp == 0) break;
+            node = stack[--sp];
+        } else {
+            node = n0;
+            if (push == 2) {
+                if (sp < kStack)
+                    stack[sp++] = n1;
+                else
+                    atomicOr(err, kErrIndexOverflow);
+            }
+        }
+    }
+}
+
+// Write-pass fallback for a chunk whose scratch overflowed: the whole tree
+// from the leaf at position p, body i's partners j > i written directly at
+// its scanned offset.
+template <class R>
+__device__ __forceinline__ void tree_write_leaf(uint32_t p, uint32_t root, const A4<R>* lmn, const A4<R>* lmx,
+                                                const A4<R>* nmn, const A4<R>* nmx, const uint2* ch,
+                                                const TreeArgs& t) {
+    const A4<R> qmn = lmn[p], qmx = lmx[p];
+    const uint32_t i = tag_of(qmn);
+    uint32_t out = t.offsets[i];
+    uint32_t stack[kStack];
+    int sp = 0;
+    uint32_t node = root;
+    while (true) {
+        const uint2 c = ch[node];
+        const uint32_t cc[2] = {c.x, c.y};
+        uint32_t n0 = 0, n1 = 0, push = 0;
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const uint32_t idx = cc[k] & ~kLeafFlag;
+            if (cc[k] & kLeafFlag) {
+                if (overlap(qmn, qmx, lmn[idx], lmx[idx])) {
+                    const uint32_t j = tag_of(lmn[idx]);
+                    if (j > i) {
+                        if (out < t.cap) t.pb[out] = j;
+                        ++out;
+                    }
+                }
+            } else if (overlap(qmn, qmx, nmn[idx], nmx[idx])) {
+                if (push == 0)
+                    n0 = idx;
+                else
+                    n1 = idx;
+                ++push;
+            }
+        }
+        if (push == 0) {
+            if (sp == 0) break;
+            node = stack[--sp];
+        } else {
+            node = n0;
+            if (push == 2) {
+                if (sp < kStack)
+                    stack[sp++] = n1;
+                else
+                    atomicOr(t.err, kErrIndexOverflow);
+            }
+        }
+    }
+}
 
 template <class R, bool WRITE>
 __global__ void __launch_bounds__(kSceneTreeThreads)
@@ -337,9 +459,7 @@ __global__ void __launch_bounds__(kSceneTreeThreads)
     uint32_t* lpar = reinterpret_cast<uint32_t*>(ch + cb);
     uint32_t* npar = lpar + cb;
     uint32_t* vis = npar + cb;  // visit flags, then per-body pair counts
-    uint32_t* lbody = vis + cb;
-    uint32_t* lroot = lbody + cb;
-    uint32_t* nhi = lroot + cb;
+    uint32_t* lroot = vis + cb;
     if (WRITE && !t.chunk_ovf[cidx]) {
         // place the scratch pairs: body a's segment starts at offsets[a]
         for (uint32_t p = tid; p < nb; p += nt) vis[p] = 0u;
@@ -359,13 +479,14 @@ __global__ void __launch_bounds__(kSceneTreeThreads)
         const SceneDesc sc = t.scenes[t.scene_of_pos[lo + p]];
         const uint32_t root = sc.body_lo - lo, ns = sc.body_hi - sc.body_lo;
         const uint32_t b = t.leaf_body[lo + p];
-        lbody[p] = b;
         lroot[p] = ns >= 2 ? root : kNoRoot;
         if (WRITE) {
             lmn[p] = g_leaf_min[lo + p];
             lmx[p] = g_leaf_max[lo + p];
         } else {
-            const A4<R> a = aabb_min[b], c = aabb_max[b];
+            A4<R> a = aabb_min[b];
+            const A4<R> c = aabb_max[b];
+            a.w = tag_bits<R>(b);
             lmn[p] = a;
             lmx[p] = c;
             g_leaf_min[lo + p] = a;
@@ -403,9 +524,9 @@ __global__ void __launch_bounds__(kSceneTreeThreads)
                 const bool ll = c.x & kLeafFlag, rl = c.y & kLeafFlag;
                 const A4<R> a0 = ll ? lmn[li] : nmn[li], a1 = ll ? lmx[li] : nmx[li];
                 const A4<R> b0 = rl ? lmn[ri] : nmn[ri], b1 = rl ? lmx[ri] : nmx[ri];
-                nmn[node] = A4<R>{fmin_(a0.x, b0.x), fmin_(a0.y, b0.y), fmin_(a0.z, b0.z), R(0)};
+                const uint32_t hi = max(ll ? li : tag_of(a0), rl ? ri : tag_of(b0));
+                nmn[node] = A4<R>{fmin_(a0.x, b0.x), fmin_(a0.y, b0.y), fmin_(a0.z, b0.z), tag_bits<R>(hi)};
                 nmx[node] = A4<R>{fmax_(a1.x, b1.x), fmax_(a1.y, b1.y), fmax_(a1.z, b1.z), R(0)};
-                nhi[node] = max(ll ? li : nhi[li], rl ? ri : nhi[ri]);
                 if (node == root) break;
                 node = npar[node];
             }
@@ -425,57 +546,10 @@ __global__ void __launch_bounds__(kSceneTreeThreads)
     for (uint32_t p = tid; p < nb; p += nt) {
         const uint32_t root = lroot[p];
         if (root == kNoRoot) continue;
-        const uint32_t i = lbody[p];
-        const A4<R> qmn = lmn[p], qmx = lmx[p];
-        uint32_t out = WRITE ? t.offsets[i] : 0u;
-        uint32_t stack[kStack];
-        int sp = 0;
-        uint32_t node = root;
-        while (true) {
-            const uint2 c = ch[node];
-            const uint32_t cc[2] = {c.x, c.y};
-            uint32_t n0 = 0, n1 = 0;  // internal children to visit (registers)
-            uint32_t push = 0;
-#pragma unroll
-            for (int k = 0; k < 2; ++k) {
-                const uint32_t x = cc[k];
-                const uint32_t idx = x & ~kLeafFlag;
-                if (x & kLeafFlag) {
-                    if ((WRITE || idx > p) && overlap(qmn, qmx, lmn[idx], lmx[idx])) {
-                        const uint32_t j = lbody[idx];
-                        if (WRITE) {  // overflow fallback: body i's partners j > i
-                            if (j > i) {
-                                if (out < t.cap) t.pb[out] = j;
-                                ++out;
-                            }
-                        } else {
-                            const uint32_t a = min(i, j), b = max(i, j);
-                            atomicAdd(&vis[a - lo], 1u);
-                            const uint32_t slot = atomicAdd(s_cursor, 1u);
-                            if (slot < region) dst[slot] = make_uint2(a, b);
-                        }
-                    }
-                } else if ((WRITE || nhi[idx] > p) && overlap(qmn, qmx, nmn[idx], nmx[idx])) {
-                    if (push == 0)
-                        n0 = idx;
-                    else
-                        n1 = idx;
-                    ++push;
-                }
-            }
-            if (push == 0) {
-                if (sp == 0) break;
-                node = stack[--sp];
-            } else {
-                node = n0;
-                if (push == 2) {
-                    if (sp < kStack)
-                        stack[sp++] = n1;
-                    else
-                        atomicOr(t.err, kErrIndexOverflow);
-                }
-            }
-        }
+        if (WRITE)
+            tree_write_leaf<R>(p, root, lmn, lmx, nmn, nmx, ch, t);
+        else
+            tree_count_leaf<R>(p, root, lmn, lmx, nmn, nmx, ch, vis, s_cursor, dst, region, lo, t.err);
     }
     if (!WRITE) {
         __syncthreads();
