@@ -274,10 +274,13 @@ __global__ void __launch_bounds__(128) k_traverse(const uint32_t* leaf_body, con
 //               only subtrees holding positions > p, so each overlapping pair
 //               is found once, by its lower position; it is counted for body
 //               a = min(i, j) and appended as (a, b) to the chunk's scratch
-//               region (scratch_k slots per body of the chunk).  The w slot
-//               of a leaf's min corner holds its body, of a node's min corner
-//               its highest leaf position, so one box load also brings the
-//               tag a traversal step tests
+//               region (scratch_k slots per body of the chunk).  The w slots
+//               of the box corners carry what a traversal step needs next: a
+//               leaf's min corner its body; a node's min corner its two
+//               children (chunk positions and leaf flags, 12 bits each) and
+//               its max corner its highest leaf position.  A step therefore
+//               loads only the two children's boxes, and the stack holds
+//               children words
 //   write pass  places the scratch pairs at the scanned per-body offsets; a
 //               chunk whose scratch overflowed is traversed again and written
 //               directly (body i's partners j > i)
@@ -301,6 +304,15 @@ template <>
 __device__ __forceinline__ float tag_bits<float>(uint32_t v) { return __uint_as_float(v); }
 template <>
 __device__ __forceinline__ double tag_bits<double>(uint32_t v) { return __longlong_as_double((long long)v); }
+// a node's children (chunk positions with leaf flags) as one 24-bit word
+constexpr uint32_t kCwIndex = 0x7FFu, kCwLeaf = 0x800u;
+static_assert(scene_tree_cap<float>() <= kCwIndex + 1 && scene_tree_cap<double>() <= kCwIndex + 1,
+              "chunk positions must fit a children word");
+__device__ __forceinline__ uint32_t children_word(uint2 c) {
+    const uint32_t l = (c.x & ~kLeafFlag) | ((c.x & kLeafFlag) ? kCwLeaf : 0u);
+    const uint32_t r = (c.y & ~kLeafFlag) | ((c.y & kLeafFlag) ? kCwLeaf : 0u);
+    return l | (r << 12);
+}
 constexpr int kSceneTreeThreads = 1024;
 constexpr uint32_t kNoRoot = 0xFFFFFFFFu;
 
@@ -330,53 +342,52 @@ struct TreeArgs {
 // is tested, so the loads of one step overlap.
 template <class R>
 __device__ __forceinline__ void tree_count_leaf(uint32_t p, uint32_t root, const A4<R>* lmn, const A4<R>* lmx,
-                                                const A4<R>* nmn, const A4<R>* nmx, const uint2* ch, uint32_t* vis,
+                                                const A4<R>* nmn, const A4<R>* nmx, uint32_t* vis,
                                                 uint32_t* s_cursor, uint2* dst, uint32_t region, uint32_t lo,
                                                 uint32_t* err) {
     const A4<R> qmn = lmn[p], qmx = lmx[p];
     const uint32_t i = tag_of(qmn);
-    uint32_t stack[kStack];
+    uint32_t stack[kStack];  // children words of the nodes still to visit
     int sp = 0;
-    uint32_t node = root;
+    uint32_t cw = tag_of(nmn[root]);
     while (true) {
-        const uint2 c = ch[node];
-        const uint32_t cc[2] = {c.x, c.y};
+        uint32_t idx[2], leaf[2];
         A4<R> bmn[2], bmx[2];
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
-            const uint32_t idx = cc[k] & ~kLeafFlag;
-            const bool leaf = cc[k] & kLeafFlag;
-            bmn[k] = (leaf ? lmn : nmn)[idx];
-            bmx[k] = (leaf ? lmx : nmx)[idx];
+            const uint32_t c = k ? cw >> 12 : cw;
+            idx[k] = c & kCwIndex;
+            leaf[k] = c & kCwLeaf;
+            bmn[k] = (leaf[k] ? lmn : nmn)[idx[k]];
+            bmx[k] = (leaf[k] ? lmx : nmx)[idx[k]];
         }
-        uint32_t n0 = 0, n1 = 0, push = 0;
+        uint32_t w0 = 0, w1 = 0, push = 0;
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
-            const uint32_t idx = cc[k] & ~kLeafFlag;
-            const bool leaf = cc[k] & kLeafFlag;
-            const uint32_t tag = tag_of(bmn[k]);  // a leaf's body, a node's highest leaf position
-            if (!((leaf ? idx : tag) > p && overlap(qmn, qmx, bmn[k], bmx[k]))) continue;
-            if (leaf) {
-                const uint32_t a = min(i, tag), b = max(i, tag);
+            // highest leaf position below: the leaf itself, or the node's tag
+            if (!((leaf[k] ? idx[k] : tag_of(bmx[k])) > p && overlap(qmn, qmx, bmn[k], bmx[k]))) continue;
+            if (leaf[k]) {
+                const uint32_t j = tag_of(bmn[k]);
+                const uint32_t a = min(i, j), b = max(i, j);
                 atomicAdd(&vis[a - lo], 1u);
                 const uint32_t slot = atomicAdd(s_cursor, 1u);
                 if (slot < region) dst[slot] = make_uint2(a, b);
             } else {
                 if (push == 0)
-                    n0 = idx;
+                    w0 = tag_of(bmn[k]);
                 else
-                    n1 = idx;
+                    w1 = tag_of(bmn[k]);
                 ++push;
             }
         }
         if (push == 0) {
             if (sp == 0) break;
-            node = stack[--sp];
+            cw = stack[--sp];
         } else {
-            node = n0;
+            cw = w0;
             if (push == 2) {
                 if (sp < kStack)
-                    stack[sp++] = n1;
+                    stack[sp++] = w1;
                 else
                     atomicOr(err, kErrIndexOverflow);
             }
@@ -524,9 +535,10 @@ __global__ void __launch_bounds__(kSceneTreeThreads)
                 const bool ll = c.x & kLeafFlag, rl = c.y & kLeafFlag;
                 const A4<R> a0 = ll ? lmn[li] : nmn[li], a1 = ll ? lmx[li] : nmx[li];
                 const A4<R> b0 = rl ? lmn[ri] : nmn[ri], b1 = rl ? lmx[ri] : nmx[ri];
-                const uint32_t hi = max(ll ? li : tag_of(a0), rl ? ri : tag_of(b0));
-                nmn[node] = A4<R>{fmin_(a0.x, b0.x), fmin_(a0.y, b0.y), fmin_(a0.z, b0.z), tag_bits<R>(hi)};
-                nmx[node] = A4<R>{fmax_(a1.x, b1.x), fmax_(a1.y, b1.y), fmax_(a1.z, b1.z), R(0)};
+                const uint32_t hi = max(ll ? li : tag_of(a1), rl ? ri : tag_of(b1));
+                nmn[node] = A4<R>{fmin_(a0.x, b0.x), fmin_(a0.y, b0.y), fmin_(a0.z, b0.z),
+                                  tag_bits<R>(children_word(c))};
+                nmx[node] = A4<R>{fmax_(a1.x, b1.x), fmax_(a1.y, b1.y), fmax_(a1.z, b1.z), tag_bits<R>(hi)};
                 if (node == root) break;
                 node = npar[node];
             }
@@ -549,7 +561,7 @@ __global__ void __launch_bounds__(kSceneTreeThreads)
         if (WRITE)
             tree_write_leaf<R>(p, root, lmn, lmx, nmn, nmx, ch, t);
         else
-            tree_count_leaf<R>(p, root, lmn, lmx, nmn, nmx, ch, vis, s_cursor, dst, region, lo, t.err);
+            tree_count_leaf<R>(p, root, lmn, lmx, nmn, nmx, vis, s_cursor, dst, region, lo, t.err);
     }
     if (!WRITE) {
         __syncthreads();
