@@ -39,6 +39,7 @@ namespace dio {
 static __global__ void k_set_u32(uint32_t* dst, uint32_t v) { *dst = v; }
 static __global__ void k_copy_u32(uint32_t* dst, const uint32_t* src) { *dst = *src; }
 static __global__ void k_sum_rows(Counters* c, const uint32_t* pair_rows, const uint32_t* cont_rows, uint32_t max_rows) {
+    pdl_enter();
     c->pair_rows = *pair_rows;
     c->container_rows = *cont_rows;
     uint64_t t = (uint64_t)*pair_rows + *cont_rows;
@@ -46,6 +47,7 @@ static __global__ void k_sum_rows(Counters* c, const uint32_t* pair_rows, const 
     if (t > max_rows) c->error_flags |= kErrRowOverflow;
 }
 static __global__ void k_pairs_total(Counters* c, const uint32_t* total, uint32_t max_pairs) {
+    pdl_enter();
     c->pairs = *total;
     if (*total > max_pairs) c->error_flags |= kErrPairOverflow;
 }
@@ -1205,7 +1207,7 @@ class Engine final : public EngineBase {
     int run_broad(uint32_t lo, uint32_t hi) {
         uint32_t n = hi - lo;
         int g = grid_for(n, 128);
-        k_aabb<P, R><<<g, 128, 0, stream_>>>(w_, lo, hi);
+        DIO_CK(launch_k(pdl(), k_aabb<P, R>, g, 128, 0, stream_, w_, lo, hi));
         if (cfg_.broad_phase == 0 && lo == 0) return run_lbvh(n);
         constexpr int kB = 128;
         int gd = grid_for(n, kB);
@@ -1224,12 +1226,13 @@ class Engine final : public EngineBase {
         uint32_t ns = std::max(1u, w_.n_scenes);
         int g = grid_for(n, 256);
         if (!rebuild_now_) return run_lbvh_refit(n, g);
-        k_bounds_init<<<grid_for(ns, 128), 128, 0, stream_>>>(lb_bounds_, ns);
-        k_scene_bounds<R><<<g, 256, 0, stream_>>>(w_.aabb_min, w_.aabb_max, w_.scene, n, lb_bounds_);
+        DIO_CK(launch_k(pdl(), k_bounds_init, grid_for(ns, 128), 128, 0, stream_, lb_bounds_, ns));
+        DIO_CK(launch_k(pdl(), k_scene_bounds<R>, g, 256, 0, stream_, (const A4<R>*)w_.aabb_min,
+                        (const A4<R>*)w_.aabb_max, (const uint32_t*)w_.scene, n, lb_bounds_));
         const uint32_t sbits = ns > 1 ? bits_for(ns - 1) : 0;
         const uint32_t abits = std::min(10u, (32u - sbits) / 3u);
-        k_morton<R><<<g, 256, 0, stream_>>>(w_.aabb_min, w_.aabb_max, w_.scene, n, lb_bounds_, sbits, abits, lb_keys_,
-                                            lb_vals_);
+        DIO_CK(launch_k(pdl(), k_morton<R>, g, 256, 0, stream_, (const A4<R>*)w_.aabb_min, (const A4<R>*)w_.aabb_max,
+                        (const uint32_t*)w_.scene, n, (const uint32_t*)lb_bounds_, sbits, abits, lb_keys_, lb_vals_));
         size_t tb = cub_bytes_;
         DIO_CK(cub::DeviceRadixSort::SortPairs(cub_tmp_, tb, lb_keys_, lb_keys_s_, lb_vals_, lb_leaf_, (int)n, 0,
                                                (int)(sbits + 3 * abits), stream_));
@@ -1269,18 +1272,19 @@ class Engine final : public EngineBase {
         ta.chunk_n = chunk_n_;
         ta.chunk_ovf = chunk_ovf_;
         ta.err = &ctr_->error_flags;
-        auto scene_tree = [&](bool write) {
-            if (!nchunks) return;
-            if (write)
-                k_scene_tree<R, true><<<nchunks, kSceneTreeThreads, tbytes, stream_>>>(
-                    w_.aabb_min, w_.aabb_max, lb_leaf_min_, lb_leaf_max_, lb_node_min_, lb_node_max_, ta);
-            else
-                k_scene_tree<R, false><<<nchunks, kSceneTreeThreads, tbytes, stream_>>>(
-                    w_.aabb_min, w_.aabb_max, lb_leaf_min_, lb_leaf_max_, lb_node_min_, lb_node_max_, ta);
+        auto scene_tree = [&](bool write) -> cudaError_t {
+            if (!nchunks) return cudaSuccess;
             ++launches_;
+            if (write)  // after a scan: a plain launch
+                return launch_k(false, k_scene_tree<R, true>, (int)nchunks, kSceneTreeThreads, tbytes, stream_,
+                                (const A4<R>*)w_.aabb_min, (const A4<R>*)w_.aabb_max, lb_leaf_min_, lb_leaf_max_,
+                                lb_node_min_, lb_node_max_, ta);
+            return launch_k(pdl(), k_scene_tree<R, false>, (int)nchunks, kSceneTreeThreads, tbytes, stream_,
+                            (const A4<R>*)w_.aabb_min, (const A4<R>*)w_.aabb_max, lb_leaf_min_, lb_leaf_max_,
+                            lb_node_min_, lb_node_max_, ta);
         };
         int gt = grid_for(n, 128);
-        scene_tree(false);
+        DIO_CK(scene_tree(false));
         if (global_path) {
             DIO_CK(cudaMemsetAsync(lb_visits_, 0, (size_t)n * 4, stream_));
             k_refit<R><<<g, 256, 0, stream_>>>(w_.aabb_min, w_.aabb_max, lb_leaf_, scenes_, w_.scene, n,
@@ -1291,21 +1295,26 @@ class Engine final : public EngineBase {
                                                    lb_pb_, w_.max_pairs, false, &ctr_->error_flags, tcap_skip);
             launches_ += 2;
         }
-        DIO_CK(cudaMemsetAsync(counts_ + n, 0, 4, stream_));
+        if (!world_step_) DIO_CK(cudaMemsetAsync(counts_ + n, 0, 4, stream_));  // else k_roll_counters
         size_t tb = cub_bytes_;
         DIO_CK(cub::DeviceScan::ExclusiveSum(cub_tmp_, tb, counts_, offsets_, (int)n + 1, stream_));
-        scene_tree(true);
+        DIO_CK(scene_tree(true));
         if (global_path) {
             k_traverse<R><<<gt, 128, 0, stream_>>>(lb_leaf_, scenes_, w_.scene, n, lb_children_, lb_leaf_min_,
                                                    lb_leaf_max_, lb_node_min_, lb_node_max_, counts_, offsets_,
                                                    lb_pb_, w_.max_pairs, true, &ctr_->error_flags, tcap_skip);
             ++launches_;
         }
-        k_pairs_total<<<1, 1, 0, stream_>>>(ctr_, offsets_ + n, w_.max_pairs);
-        DIO_CK(cudaMemsetAsync(lb_long_count_, 0, 4, stream_));
-        k_sort_segments<<<g, 256, 0, stream_>>>(offsets_, n, w_.max_pairs, lb_pb_, lb_long_, lb_long_count_);
-        k_sort_long<<<sms_, 512, 0, stream_>>>(offsets_, lb_pb_, lb_long_, lb_long_count_, &ctr_->error_flags);
-        k_pairs_from_segments<<<g, 256, 0, stream_>>>(offsets_, n, lb_pb_, w_.pairs, w_.max_pairs);
+        // a plain launch when nothing of ours ran since the scan
+        DIO_CK(launch_k(pdl() && (nchunks || global_path), k_pairs_total, 1, 1, 0, stream_, ctr_,
+                        (const uint32_t*)(offsets_ + n), w_.max_pairs));
+        if (!world_step_) DIO_CK(cudaMemsetAsync(lb_long_count_, 0, 4, stream_));  // else k_roll_counters
+        DIO_CK(launch_k(pdl(), k_sort_segments, g, 256, 0, stream_, (const uint32_t*)offsets_, n, w_.max_pairs, lb_pb_,
+                        lb_long_, lb_long_count_));
+        DIO_CK(launch_k(pdl(), k_sort_long, sms_, 512, 0, stream_, (const uint32_t*)offsets_, lb_pb_,
+                        (const uint32_t*)lb_long_, (const uint32_t*)lb_long_count_, &ctr_->error_flags));
+        DIO_CK(launch_k(pdl(), k_pairs_from_segments, g, 256, 0, stream_, (const uint32_t*)offsets_, n,
+                        (const uint32_t*)lb_pb_, w_.pairs, w_.max_pairs));
         launches_ += 5;
         return DIO_OK;
     }
@@ -1315,9 +1324,9 @@ class Engine final : public EngineBase {
         uint32_t per = cfg_.contacts_per_pair;
         w_.per_pair = per;
         int g = np_dev ? sms_ * 8 : grid_for(np, 128);
-        k_narrow_main<P, R><<<g, 128, 0, stream_>>>(w_, np_dev, np);
-        k_gjk<P, R><<<sms_ * 4, 128, 0, stream_>>>(w_);
-        k_epa<P, R><<<sms_ * 4, 32 * epa_warps<R>(), 0, stream_>>>(w_);
+        DIO_CK(launch_k(pdl(), k_narrow_main<P, R>, g, 128, 0, stream_, w_, np_dev, np));
+        DIO_CK(launch_k(pdl(), k_gjk<P, R>, sms_ * 4, 128, 0, stream_, w_));
+        DIO_CK(launch_k(pdl(), k_epa<P, R>, sms_ * 4, 32 * epa_warps<R>(), 0, stream_, w_));
         launches_ += 3;
         return DIO_OK;
     }
@@ -1330,8 +1339,8 @@ class Engine final : public EngineBase {
         uint32_t G = groups;
         if (!src) src = w_.slots;
         if (G) {
-            k_slot_count<R><<<grid_for(G, 256), 256, 0, stream_>>>(src, per, groups_dev, G, counts_);
-            DIO_CK(cudaMemsetAsync(counts_ + G, 0, 4, stream_));
+            DIO_CK(launch_k(pdl(), k_slot_count<R>, grid_for(G, 256), 256, 0, stream_, src, per, groups_dev, G,
+                            counts_));
             size_t tb = cub_bytes_;
             DIO_CK(cub::DeviceScan::ExclusiveSum(cub_tmp_, tb, counts_, offsets_, (int)G + 1, stream_));
             k_slot_rows<P, R><<<grid_for(G, 128), 128, 0, stream_>>>(w_, src, per, groups_dev, G, offsets_, o);
@@ -1340,15 +1349,16 @@ class Engine final : public EngineBase {
         }
         const uint32_t* pair_rows = offsets_ + G;
         if (n) {
-            k_cont_count<P, R><<<grid_for(n, 128), 128, 0, stream_>>>(w_, 0, n, o, counts2_);
-            DIO_CK(cudaMemsetAsync(counts2_ + n, 0, 4, stream_));
+            DIO_CK(launch_k(pdl() && G, k_cont_count<P, R>, grid_for(n, 128), 128, 0, stream_, w_, 0u, n, o, counts2_));
             size_t tb = cub_bytes_;
             DIO_CK(cub::DeviceScan::ExclusiveSum(cub_tmp_, tb, counts2_, offsets2_, (int)n + 1, stream_));
-            k_cont_rows<P, R><<<grid_for(n, 128), 128, 0, stream_>>>(w_, 0, n, o, offsets2_, pair_rows);
+            // clears counts2_ for the CSR count of finish_rows_world
+            k_cont_rows<P, R><<<grid_for(n, 128), 128, 0, stream_>>>(w_, 0, n, o, offsets2_, pair_rows, counts2_);
         } else {
             DIO_CK(cudaMemsetAsync(offsets2_, 0, 4, stream_));
         }
-        k_sum_rows<<<1, 1, 0, stream_>>>(ctr_, pair_rows, offsets2_ + n, w_.max_rows);
+        DIO_CK(launch_k(pdl() && n, k_sum_rows, 1, 1, 0, stream_, ctr_, pair_rows, (const uint32_t*)(offsets2_ + n),
+                        w_.max_rows));
         launches_ += 5;
         return DIO_OK;
     }
@@ -1385,7 +1395,7 @@ class Engine final : public EngineBase {
         int gm = m_dev ? std::min(grid_for(cap_.max_contacts, 256), sms_ * dual_ctas_per_sm_)
                        : grid_for(std::max(m, 1u), 256);
         if (m_dev) m = cap_.max_contacts;
-        k_init<P, R><<<gb, 256, 0, stream_>>>(w_, 0, n, o);
+        DIO_CK(launch_k(pdl(), k_init<P, R>, gb, 256, 0, stream_, w_, 0u, n, o));
         launches_ += 2;
         // programmatic dependent launch between the solve's kernels, unless
         // event timers sit between them
@@ -1732,11 +1742,19 @@ class Engine final : public EngineBase {
         return build_rows(pp, cap_.max_pairs, cfg_.contacts_per_pair, &ctr_->pairs, n);
     }
     int step_body_dev(const DioAvbdOptions& opt) {
+        struct WorldStep {  // the flag holds for this step's launches only
+            bool& f;
+            explicit WorldStep(bool& f) : f(f) { f = true; }
+            ~WorldStep() { f = false; }
+        } scope(world_step_);
         uint32_t n = w_.n;
         PrepParams<R> pp = opts_prep(opt);
         set_rows(cur_);
         set_slots();
-        k_roll_counters<<<1, 1, 0, stream_>>>(ctr_);
+        // zeroes the LBVH pair-count scan's closing entry and the long-segment
+        // count of the pair sort (counts_ is written again later in the step)
+        k_roll_counters<<<1, 1, 0, stream_>>>(ctr_, n && cfg_.broad_phase == 0 ? counts_ + n : nullptr,
+                                              lb_long_count_);
         ++launches_;
         cudaEvent_t e = span_begin();
         if (n) DIO_TRY(run_broad(0, n));
@@ -1763,7 +1781,7 @@ class Engine final : public EngineBase {
         PrepParams<R> pp = opts_prep(opt);
         set_rows(cur_);
         set_slots();
-        k_roll_counters<<<1, 1, 0, stream_>>>(ctr_);
+        k_roll_counters<<<1, 1, 0, stream_>>>(ctr_, nullptr, nullptr);
         cudaEvent_t e = span_begin();
         if (n) DIO_TRY(run_broad(0, n));
         span_end(e, 2);
@@ -1862,19 +1880,20 @@ class Engine final : public EngineBase {
     int finish_rows_world(const PrepParams<R>& o, uint32_t n) {
         int pb = 1 - cur_;
         const int gf = std::min(grid_for(cap_.max_contacts, 256), sms_ * 8);
-        k_warm_sections<P, R><<<gf, 256, 0, stream_>>>(w_, ab_[pb], rd_[pb], o);
-        DIO_CK(cudaMemsetAsync(counts2_, 0, ((size_t)n + 1) * 4, stream_));
-        k_csr_count_dyn<P, R><<<gf, 256, 0, stream_>>>(w_, counts2_);
+        DIO_CK(launch_k(pdl(), k_warm_sections<P, R>, gf, 256, 0, stream_, w_, (const uint2*)ab_[pb],
+                        (const RowDual<P, R>*)rd_[pb], o));
+        // counts2_ was cleared by k_cont_rows (build_rows, bodies [0, n))
+        if (!n) DIO_CK(cudaMemsetAsync(counts2_, 0, 4, stream_));
+        DIO_CK(launch_k(pdl() && n, k_csr_count_dyn<P, R>, gf, 256, 0, stream_, w_, counts2_));
         size_t tb = cub_bytes_;
         DIO_CK(cub::DeviceScan::ExclusiveSum(cub_tmp_, tb, counts2_, w_.row_off, (int)n + 1, stream_));
-        DIO_CK(cudaMemsetAsync(counts2_, 0, ((size_t)n + 1) * 4, stream_));
-        k_csr_scatter_dyn<P, R><<<gf, 256, 0, stream_>>>(w_, counts2_);
+        k_csr_scatter_dyn<P, R><<<gf, 256, 0, stream_>>>(w_, counts2_);  // takes the counts back to zero
         int gn = grid_for(n, 256);
-        k_sort_segments<<<gn, 256, 0, stream_>>>(w_.row_off, n, w_.max_incid, w_.row_idx, lb_long_,
-                                                &ctr_->long_count);
-        k_sort_long<<<sms_, 512, 0, stream_>>>(w_.row_off, w_.row_idx, lb_long_, &ctr_->long_count,
-                                              &ctr_->error_flags);
-        k_csr_other_dyn<P, R><<<gn, 256, 0, stream_>>>(w_);
+        DIO_CK(launch_k(pdl(), k_sort_segments, gn, 256, 0, stream_, (const uint32_t*)w_.row_off, n, w_.max_incid,
+                        w_.row_idx, lb_long_, &ctr_->long_count));
+        DIO_CK(launch_k(pdl(), k_sort_long, sms_, 512, 0, stream_, (const uint32_t*)w_.row_off, w_.row_idx,
+                        (const uint32_t*)lb_long_, (const uint32_t*)&ctr_->long_count, &ctr_->error_flags));
+        DIO_CK(launch_k(pdl(), k_csr_other_dyn<P, R>, gn, 256, 0, stream_, w_));
         launches_ += 6;
         return DIO_OK;
     }
@@ -2007,6 +2026,10 @@ class Engine final : public EngineBase {
     std::vector<uint2> chunks_host_;
     uint2* chunks_ = nullptr;
     Slot<R>* slots_[2] = {nullptr, nullptr};
+    // inside step_body_dev: its scratch zeroing is done by k_roll_counters and
+    // consecutive kernels of ours are chained by programmatic launch
+    bool world_step_ = false;
+    bool pdl() const { return world_step_ && !cfg_.profile; }
     int state_pending_ = 0;    // set_state_begin left: 1 the dynamic-set check, 2 a list rebuild
     bool lag_primed_ = false;  // the previous step's slots are this mode's
     uint32_t* chunk_n_ = nullptr;

@@ -161,6 +161,7 @@ __device__ __forceinline__ void init_body(const DevWorld<P, R>& w, uint32_t i, c
 
 template <class P, class R>
 __global__ void __launch_bounds__(256) k_init(DevWorld<P, R> w, uint32_t lo, uint32_t hi, SolveParams<R> o) {
+    pdl_enter();
     for (uint32_t i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += gridDim.x * blockDim.x)
         init_body(w, i, o);
 }

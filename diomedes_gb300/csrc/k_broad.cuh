@@ -33,6 +33,7 @@ __device__ __forceinline__ void body_aabb(const NB<R>& b, const A4<R>* hull, V3<
 
 template <class P, class R>
 __global__ void k_aabb(DevWorld<P, R> w, uint32_t lo, uint32_t hi) {
+    pdl_enter();
     for (uint32_t i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += gridDim.x * blockDim.x) {
         NB<R> b = load_nb(w, i);
         V3<R> mn, mx;

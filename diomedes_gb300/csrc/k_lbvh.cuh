@@ -41,6 +41,7 @@ __device__ __forceinline__ uint64_t d2ord(double f) {
 // grid only needs to be monotone in the centre, so FP32 bounds suffice
 template <class R>
 __global__ void k_scene_bounds(const A4<R>* mn, const A4<R>* mx, const uint32_t* scene, uint32_t n, uint32_t* bounds) {
+    pdl_enter();
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         A4<R> a = mn[i], b = mx[i];
         uint32_t ox = f2ord(float(a.x * R(0.5) + b.x * R(0.5)));
@@ -80,6 +81,7 @@ __device__ __forceinline__ uint32_t spread10(uint32_t v) {
 template <class R>
 __global__ void k_morton(const A4<R>* mn, const A4<R>* mx, const uint32_t* scene, uint32_t n, const uint32_t* bounds,
                          uint32_t scene_bits, uint32_t axis_bits, uint32_t* keys, uint32_t* vals) {
+    pdl_enter();
     const float cells = float(1u << axis_bits);
     const uint32_t top = (1u << axis_bits) - 1u;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -133,6 +135,7 @@ __device__ __forceinline__ A4<double> ldcg4(const A4<double>* p) {
 // global slots, leaves flagged with kLeafFlag (leaf = sorted position)
 static __global__ void k_karras(const uint32_t* keys, const SceneDesc* scenes, const uint32_t* scene_of_pos,
                          uint32_t n, uint2* children, uint32_t* parent) {
+    pdl_enter();
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
         const SceneDesc sc = scenes[scene_of_pos[p]];
         const uint32_t lo = sc.body_lo;
@@ -450,6 +453,7 @@ template <class R, bool WRITE>
 __global__ void __launch_bounds__(kSceneTreeThreads)
     k_scene_tree(const A4<R>* aabb_min, const A4<R>* aabb_max, A4<R>* g_leaf_min, A4<R>* g_leaf_max,
                  A4<R>* g_node_min, A4<R>* g_node_max, TreeArgs t) {
+    pdl_enter();
     extern __shared__ __align__(16) unsigned char tree_smem[];
     const uint32_t cidx = blockIdx.x;
     const uint2 chunk = t.chunks[cidx];  // scenes [x, y)
@@ -577,6 +581,7 @@ __global__ void __launch_bounds__(kSceneTreeThreads)
 // sort each body's partner list ascending; short lists in-thread, long
 // lists (> 32) by one CTA in shared memory (bitonic, up to 4096 entries)
 static __global__ void k_bounds_init(uint32_t* b, uint32_t ns) {
+    pdl_enter();
     for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x) {
         b[6 * s + 0] = b[6 * s + 1] = b[6 * s + 2] = 0xFFFFFFFFu;
         b[6 * s + 3] = b[6 * s + 4] = b[6 * s + 5] = 0u;
@@ -585,6 +590,7 @@ static __global__ void k_bounds_init(uint32_t* b, uint32_t ns) {
 
 static __global__ void k_sort_segments(const uint32_t* offsets, uint32_t n, uint32_t cap, uint32_t* pb, uint32_t* long_list,
                                 uint32_t* long_count) {
+    pdl_enter();
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         uint32_t a = offsets[i], b = offsets[i + 1];
         uint32_t len = b - a;
@@ -612,6 +618,7 @@ constexpr int kLongSort = 4096;
 
 static __global__ void __launch_bounds__(512) k_sort_long(const uint32_t* offsets, uint32_t* pb, const uint32_t* long_list,
                                                    const uint32_t* long_count, uint32_t* err) {
+    pdl_enter();
     __shared__ uint32_t s[kLongSort];
     uint32_t cnt = *long_count;
     for (uint32_t q = blockIdx.x; q < cnt; q += gridDim.x) {
@@ -648,6 +655,7 @@ static __global__ void __launch_bounds__(512) k_sort_long(const uint32_t* offset
 
 static __global__ void k_pairs_from_segments(const uint32_t* offsets, uint32_t n, const uint32_t* pb, DioPair* pairs,
                                       uint32_t cap) {
+    pdl_enter();
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         for (uint32_t k = offsets[i]; k < offsets[i + 1] && k < cap; ++k) pairs[k] = DioPair{i, pb[k]};
 }

@@ -38,6 +38,7 @@ __device__ __forceinline__ void clear_slot(Slot<R>* s) {
 // work when non-null, so the launch does not depend on a host read.
 template <class P, class R>
 __global__ void __launch_bounds__(128) k_narrow_main(DevWorld<P, R> w, const uint32_t* np_dev, uint32_t np_cap) {
+    pdl_enter();
     uint32_t np = np_dev ? min(*np_dev, np_cap) : np_cap;
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
         Slot<R>* slots = w.slots + (size_t)p * w.per_pair;
@@ -75,6 +76,7 @@ __global__ void __launch_bounds__(128) k_narrow_main(DevWorld<P, R> w, const uin
 // simplex (4 points then 4 witnesses) for EPA.
 template <class P, class R>
 __global__ void __launch_bounds__(128) k_gjk(DevWorld<P, R> w) {
+    pdl_enter();
     uint32_t nw = w.ctr->gjk_work;
     for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < nw; e += gridDim.x * blockDim.x) {
         uint32_t p = w.gjk_list[e];
@@ -140,6 +142,7 @@ constexpr uint32_t kHullStage = 64;  // vertices per hull staged in shared memor
 // expansion read shared memory.
 template <class P, class R>
 __global__ void __launch_bounds__(32 * epa_warps<R>()) k_epa(DevWorld<P, R> w) {
+    pdl_enter();
     constexpr int kEpaWarps = epa_warps<R>();
     __shared__ EpaSmem<R> smem[kEpaWarps];
     __shared__ A4<R> hull_s[kEpaWarps][2 * kHullStage];

@@ -53,10 +53,13 @@ __device__ __forceinline__ void write_row(const DevWorld<P, R>& w, uint32_t r, u
     w.ab[r] = make_uint2(a, b);
 }
 
-// Valid slots of the first `n_groups` groups of `per` slots.
+// Valid slots of the first `n_groups` groups of `per` slots; counts[n_groups]
+// is set to 0 for the exclusive scan over n_groups + 1 entries.
 template <class R>
 __global__ void k_slot_count(const Slot<R>* slots, uint32_t per, const uint32_t* n_groups_dev, uint32_t n_groups,
                              uint32_t* counts) {
+    pdl_enter();
+    if (blockIdx.x == 0 && threadIdx.x == 0) counts[n_groups] = 0u;
     uint32_t ng = n_groups_dev ? *n_groups_dev : n_groups;
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n_groups; p += gridDim.x * blockDim.x) {
         uint32_t c = 0;
@@ -70,6 +73,7 @@ __global__ void k_slot_count(const Slot<R>* slots, uint32_t per, const uint32_t*
 template <class P, class R>
 __global__ void k_slot_rows(DevWorld<P, R> w, const Slot<R>* slots, uint32_t per, const uint32_t* n_groups_dev,
                             uint32_t n_groups, const uint32_t* offsets, PrepParams<R> o) {
+    pdl_enter();
     uint32_t ng = n_groups_dev ? *n_groups_dev : n_groups;
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < ng && p < n_groups; p += gridDim.x * blockDim.x) {
         uint32_t r = offsets[p];
@@ -225,8 +229,11 @@ __global__ void k_scene_walls(DevWorld<P, R> w, const SceneDesc* scenes, uint32_
     }
 }
 
+// counts[hi - lo] is set to 0 for the exclusive scan over hi - lo + 1 entries
 template <class P, class R>
 __global__ void k_cont_count(DevWorld<P, R> w, uint32_t lo, uint32_t hi, PrepParams<R> o, uint32_t* counts) {
+    pdl_enter();
+    if (blockIdx.x == 0 && threadIdx.x == 0) counts[hi - lo] = 0u;
     for (uint32_t i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += gridDim.x * blockDim.x) {
         uint32_t c = 0;
         const SceneDesc sc = w.scenes[w.scene[i]];
@@ -235,11 +242,16 @@ __global__ void k_cont_count(DevWorld<P, R> w, uint32_t lo, uint32_t hi, PrepPar
     }
 }
 
+// zero (may be null): hi - lo + 1 per-body counters cleared on the way, for
+// the dynamic-body CSR count that follows
 template <class P, class R>
 __global__ void k_cont_rows(DevWorld<P, R> w, uint32_t lo, uint32_t hi, PrepParams<R> o, const uint32_t* offsets,
-                            const uint32_t* base_dev) {
+                            const uint32_t* base_dev, uint32_t* zero) {
+    pdl_enter();
     uint32_t base = *base_dev;
+    if (zero && blockIdx.x == 0 && threadIdx.x == 0) zero[hi - lo] = 0u;
     for (uint32_t i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += gridDim.x * blockDim.x) {
+        if (zero) zero[i - lo] = 0u;
         const SceneDesc sc = w.scenes[w.scene[i]];
         if (w.inv[i].w != R(0) && sc.has_container) container_rows(w, i, sc, o, true, base + offsets[i - lo]);
     }
@@ -370,8 +382,11 @@ __device__ __forceinline__ bool key_less(uint2 a, uint2 b) { return a.x < b.x ||
 __device__ __forceinline__ bool key_eq(uint2 a, uint2 b) { return a.x == b.x && a.y == b.y; }
 
 // roll the per-step counters: the finished step's row counts become the
-// warm-start source, the per-step counts restart at zero
-static __global__ void k_roll_counters(Counters* c) {
+// warm-start source, the per-step counts restart at zero (and up to two
+// scratch words the step's scans and sorts expect zeroed, if given)
+static __global__ void k_roll_counters(Counters* c, uint32_t* zero0, uint32_t* zero1) {
+    if (zero0) *zero0 = 0u;
+    if (zero1) *zero1 = 0u;
     c->prev_rows = c->rows;
     c->prev_pair_rows = c->pair_rows;
     c->prev_pairs = c->pairs;
@@ -387,6 +402,7 @@ static __global__ void k_roll_counters(Counters* c) {
 template <class P, class R>
 __global__ void k_warm_sections(DevWorld<P, R> w, const uint2* prev_ab, const RowDual<P, R>* prev_dual,
                                 PrepParams<R> o) {
+    pdl_enter();
     const uint32_t m = w.ctr->rows, pair_rows = w.ctr->pair_rows;
     const uint32_t prev_m = w.ctr->prev_rows, prev_pair = w.ctr->prev_pair_rows;
     for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) {
@@ -424,11 +440,13 @@ __global__ void k_warm_sections(DevWorld<P, R> w, const uint2* prev_ab, const Ro
 }
 
 // CSR of the dynamic bodies only (the primal never visits a static body):
-// counts, then an atomic scatter, then each segment sorted by row index,
+// counts, then an atomic scatter (each body's count taken down to zero),
+// then each segment sorted by row index,
 // which restores the reference's fill order (finalize_contacts, gpu.rs:
 // 286-310) without a sort over all incidences.
 template <class P, class R>
 __global__ void k_csr_count_dyn(DevWorld<P, R> w, uint32_t* counts) {
+    pdl_enter();
     const uint32_t m = w.ctr->rows;
     for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) {
         uint2 ab = w.ab[r];
@@ -437,17 +455,19 @@ __global__ void k_csr_count_dyn(DevWorld<P, R> w, uint32_t* counts) {
     }
 }
 
+// remaining: each body's incidence count (k_csr_count_dyn), consumed here
 template <class P, class R>
-__global__ void k_csr_scatter_dyn(DevWorld<P, R> w, uint32_t* cursor) {
+__global__ void k_csr_scatter_dyn(DevWorld<P, R> w, uint32_t* remaining) {
+    pdl_enter();
     const uint32_t m = w.ctr->rows;
     for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) {
         uint2 ab = w.ab[r];
         if (w.inv[ab.x].w != R(0)) {
-            uint32_t j = w.row_off[ab.x] + atomicAdd(&cursor[ab.x], 1u);
+            uint32_t j = w.row_off[ab.x] + atomicSub(&remaining[ab.x], 1u) - 1u;
             if (j < w.max_incid) w.row_idx[j] = r;
         }
         if (ab.y != kContainer && w.inv[ab.y].w != R(0)) {
-            uint32_t j = w.row_off[ab.y] + atomicAdd(&cursor[ab.y], 1u);
+            uint32_t j = w.row_off[ab.y] + atomicSub(&remaining[ab.y], 1u) - 1u;
             if (j < w.max_incid) w.row_idx[j] = r;
         }
     }
@@ -455,6 +475,7 @@ __global__ void k_csr_scatter_dyn(DevWorld<P, R> w, uint32_t* cursor) {
 
 template <class P, class R>
 __global__ void k_csr_other_dyn(DevWorld<P, R> w) {
+    pdl_enter();
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < w.n; i += gridDim.x * blockDim.x) {
         uint32_t j0 = w.row_off[i], j1 = min(w.row_off[i + 1], w.max_incid);
         for (uint32_t j = j0; j < j1; ++j) {
