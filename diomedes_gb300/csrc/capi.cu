@@ -400,6 +400,7 @@ int dio_autotune(DioCtx* ctx, const DioAvbdOptions* options, uint32_t trial_step
         if (!rc && best) *best = ctx->cfg;
         return rc;
     }
+    if (!cfg.bvh_rebuild_period) cfg.bvh_rebuild_period = 4;  // what 0 selects: report the period itself
     if ((rc = e->snapshot())) return fail(ctx, rc, e->err);
     auto trial = [&](const DioConfig& c, double* ms) -> int {
         int r = dio_ctx_configure(ctx, &c);
