@@ -16,6 +16,7 @@
 
 #include <type_traits>
 
+#include "div_rn.cuh"
 #include "engine.cuh"
 
 namespace dio {
@@ -61,7 +62,9 @@ constexpr int kMaskAxisX = (1 << 0) | (1 << 4) | (1 << 5);  // J = (s, 0, 0, 0, 
 constexpr int kMaskAxisY = (1 << 1) | (1 << 3) | (1 << 5);  // J = (0, s, 0, -s r.z, 0, s r.x)
 constexpr int kMaskAxisZ = (1 << 2) | (1 << 3) | (1 << 4);  // J = (0, 0, s, s r.y, -s r.x, 0)
 
-// solve6, avbd/src/lib.rs:107-180 (unpivoted LDL^T); solves H x = -g.
+// solve6, avbd/src/lib.rs:107-180 (unpivoted LDL^T); solves H x = -g.  Each
+// quotient by a pivot is the IEEE quotient (div_rn.cuh: one reciprocal per
+// pivot, a correction step per quotient).
 template <class R>
 __device__ __forceinline__ void solve6(const Block6<R>& B, R x[6]) {
     const R* H = B.h;
@@ -72,22 +75,27 @@ __device__ __forceinline__ void solve6(const Block6<R>& B, R x[6]) {
     R a43 = H[tri(3, 2)], a53 = H[tri(4, 2)], a63 = H[tri(5, 2)];
     R a44 = H[tri(3, 3)], a54 = H[tri(4, 3)], a64 = H[tri(5, 3)], a55 = H[tri(4, 4)], a65 = H[tri(5, 4)],
       a66 = H[tri(5, 5)];
-    R l21 = a21 / a11, l31 = a31 / a11, l41 = a41 / a11, l51 = a51 / a11, l61 = a61 / a11;
+    const Divisor<R> p1(a11);
+    R l21 = p1.div(a21), l31 = p1.div(a31), l41 = p1.div(a41), l51 = p1.div(a51), l61 = p1.div(a61);
     R d1 = a11;
     R d2 = a22 - l21 * l21 * d1;
-    R l32 = (a32 - l21 * l31 * d1) / d2;
-    R l42 = (a42 - l21 * l41 * d1) / d2;
-    R l52 = (a52 - l21 * l51 * d1) / d2;
-    R l62 = (a62 - l21 * l61 * d1) / d2;
+    const Divisor<R> p2(d2);
+    R l32 = p2.div(a32 - l21 * l31 * d1);
+    R l42 = p2.div(a42 - l21 * l41 * d1);
+    R l52 = p2.div(a52 - l21 * l51 * d1);
+    R l62 = p2.div(a62 - l21 * l61 * d1);
     R d3 = a33 - (l31 * l31 * d1 + l32 * l32 * d2);
-    R l43 = (a43 - l31 * l41 * d1 - l32 * l42 * d2) / d3;
-    R l53 = (a53 - l31 * l51 * d1 - l32 * l52 * d2) / d3;
-    R l63 = (a63 - l31 * l61 * d1 - l32 * l62 * d2) / d3;
+    const Divisor<R> p3(d3);
+    R l43 = p3.div(a43 - l31 * l41 * d1 - l32 * l42 * d2);
+    R l53 = p3.div(a53 - l31 * l51 * d1 - l32 * l52 * d2);
+    R l63 = p3.div(a63 - l31 * l61 * d1 - l32 * l62 * d2);
     R d4 = a44 - (l41 * l41 * d1 + l42 * l42 * d2 + l43 * l43 * d3);
-    R l54 = (a54 - l41 * l51 * d1 - l42 * l52 * d2 - l43 * l53 * d3) / d4;
-    R l64 = (a64 - l41 * l61 * d1 - l42 * l62 * d2 - l43 * l63 * d3) / d4;
+    const Divisor<R> p4(d4);
+    R l54 = p4.div(a54 - l41 * l51 * d1 - l42 * l52 * d2 - l43 * l53 * d3);
+    R l64 = p4.div(a64 - l41 * l61 * d1 - l42 * l62 * d2 - l43 * l63 * d3);
     R d5 = a55 - (l51 * l51 * d1 + l52 * l52 * d2 + l53 * l53 * d3 + l54 * l54 * d4);
-    R l65 = (a65 - l51 * l61 * d1 - l52 * l62 * d2 - l53 * l63 * d3 - l54 * l64 * d4) / d5;
+    const Divisor<R> p5(d5);
+    R l65 = p5.div(a65 - l51 * l61 * d1 - l52 * l62 * d2 - l53 * l63 * d3 - l54 * l64 * d4);
     R d6 = a66 - (l61 * l61 * d1 + l62 * l62 * d2 + l63 * l63 * d3 + l64 * l64 * d4 + l65 * l65 * d5);
     R b0 = -B.g[0], b1 = -B.g[1], b2 = -B.g[2], b3 = -B.g[3], b4 = -B.g[4], b5 = -B.g[5];
     R y1 = b0;
@@ -96,7 +104,7 @@ __device__ __forceinline__ void solve6(const Block6<R>& B, R x[6]) {
     R y4 = b3 - l41 * y1 - l42 * y2 - l43 * y3;
     R y5 = b4 - l51 * y1 - l52 * y2 - l53 * y3 - l54 * y4;
     R y6 = b5 - l61 * y1 - l62 * y2 - l63 * y3 - l64 * y4 - l65 * y5;
-    R z1 = y1 / d1, z2 = y2 / d2, z3 = y3 / d3, z4 = y4 / d4, z5 = y5 / d5, z6 = y6 / d6;
+    R z1 = p1.div(y1), z2 = p2.div(y2), z3 = p3.div(y3), z4 = p4.div(y4), z5 = p5.div(y5), z6 = y6 / d6;
     x[5] = z6;
     x[4] = z5 - l65 * x[5];
     x[3] = z4 - l54 * x[4] - l64 * x[5];
