@@ -310,7 +310,8 @@ __device__ __forceinline__ void primal_joint(const DevWorld<P, R>& w, const DioC
         R target = R(jt.anchor_a[3]);
         bool active = len > R(1.0e-6) && (jt.kind != DIO_CONSTRAINT_ROPE || len > target);
         if (active) {
-            V3<R> nn = divs(delta, len);
+            const Divisor<R> dl(len);  // the IEEE quotients (div_rn.cuh)
+            const V3<R> nn{dl.div(delta.x), dl.div(delta.y), dl.div(delta.z)};
             V3<R> jl = scale(nn, sign);
             V3<R> ja = cross(r_self, jl);
             stamp(B, jl, ja, stiff, stiff * (len - target));
@@ -361,7 +362,8 @@ __device__ __forceinline__ void primal_jview_p(const JView& jv, A4<P> op4, A4<P>
         R target = R(jv.self_anchor.w);
         bool active = len > R(1.0e-6) && (kind != DIO_CONSTRAINT_ROPE || len > target);
         if (active) {
-            V3<R> nn = divs(delta, len);
+            const Divisor<R> dl(len);  // the IEEE quotients (div_rn.cuh)
+            const V3<R> nn{dl.div(delta.x), dl.div(delta.y), dl.div(delta.z)};
             V3<R> jl = scale(nn, sign);
             V3<R> ja = cross(r_self, jl);
             stamp(B, jl, ja, stiff, stiff * (len - target));
