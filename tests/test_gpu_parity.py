@@ -544,6 +544,40 @@ def test_world_with_large_and_small_scenes_matches_oracle():
     assert np.array_equal(_bits(gc), _bits(ow.contacts()))
 
 
+def _overlapping_field(n, seed):
+    """n cubes and spheres (half size 0.5) on a 0.9 grid: neighbours overlap."""
+    rng = np.random.default_rng(seed)
+    side = int(np.ceil(n ** (1.0 / 3.0)))
+    items = []
+    for k in range(n):
+        x, y, z = k % side, (k // side) % side, k // (side * side)
+        p = (0.9 * x + rng.uniform(-0.05, 0.05), 0.5 + 0.9 * z, 0.9 * y + rng.uniform(-0.05, 0.05))
+        items.append(ph.cube(p, 0.5, 1.0) if k % 3 else ph.sphere(p, 0.5, 1.0))
+    b, st = ph.pack_bodies(items)
+    return scenes.Scene(f"field{n}", b, st, containers=[scenes.ground()],
+                        options=ph.avbd_options(gravity=(0, -9.81, 0), iterations=10))
+
+
+def test_scene_tree_capacity_boundaries_match_oracle():
+    """A scene of exactly the shared-memory tree's capacity (2048 bodies, one
+    CTA), one of 2049 (the global kernels) and two scenes that fill one chunk
+    exactly (1000 + 1048) step to the oracle's bits, LBVH rebuilt every 2 steps."""
+    parts = [_overlapping_field(2048, 1), _overlapping_field(2049, 2), _overlapping_field(1000, 3),
+             _overlapping_field(1048, 4)]
+    packed = scenes.pack(parts)
+    ow = O.World(packed)
+    ow.step(packed.options, 3)
+    with _world(packed, bvh_rebuild_period=2) as w:
+        w.step(packed.options, 3)
+        gb, gs = w.download()
+        gc = w.contacts()
+        st = w.stats()
+    rb, rs = ow.download()
+    assert st["error_flags"] == 0 and st["pairs"] > 10000
+    assert np.array_equal(_bits(gb), _bits(rb)) and np.array_equal(_bits(gs), _bits(rs))
+    assert np.array_equal(_bits(gc), _bits(ow.contacts()))
+
+
 @pytest.mark.parametrize("use_graph", [0, 1])
 def test_profiled_world_times_every_primal_launch(use_graph):
     sc = scenes.box_demo()
