@@ -80,3 +80,40 @@ def test_header_constants_match_the_python_mirror():
                  "DIO_ERR_NONFINITE", "DIO_ERR_STATE"):
         m = re.search(name + r"\s*=\s*(\d+)", text)
         assert m and int(m.group(1)) == getattr(abi, name), name
+
+
+def test_bad_arguments_are_rejected_before_any_device_work():
+    """Argument checks run before the library touches CUDA, so they hold on a
+    machine without a GPU: null contexts and null outputs are DIO_ERR_INVALID,
+    and the multi-world host loop rejects missing arrays (count 0 is a no-op)."""
+    L = abi.lib()
+    o = ph.avbd_options()
+    assert L.dio_step(None, ctypes.byref(o), 1) == abi.DIO_ERR_INVALID
+    assert L.dio_step_async(None, ctypes.byref(o), 1) == abi.DIO_ERR_INVALID
+    assert L.dio_world_set_state(None, None, None) == abi.DIO_ERR_INVALID
+    assert L.dio_world_download(None, None, None) == abi.DIO_ERR_INVALID
+    assert L.dio_world_download_async(None, None, None) == abi.DIO_ERR_INVALID
+    assert L.dio_ctx_synchronize(None) == abi.DIO_ERR_INVALID
+    assert L.dio_world_checkpoint(None, None, 0, None) == abi.DIO_ERR_INVALID
+    assert L.dio_world_resume(None, None, 0) == abi.DIO_ERR_INVALID
+    assert L.dio_worlds_step_host(None, 0, None, None, ctypes.byref(o), 1) == abi.DIO_OK
+    assert L.dio_worlds_step_host(None, 1, None, None, ctypes.byref(o), 1) == abi.DIO_ERR_INVALID
+    one = (ctypes.c_void_p * 1)(None)
+    assert L.dio_worlds_step_host(one, 1, one, one, ctypes.byref(o), 1) == abi.DIO_ERR_INVALID
+    assert L.dio_worlds_step_host(one, 1, one, one, None, 1) == abi.DIO_ERR_INVALID
+
+
+def test_context_creation_without_a_device_fails_loudly():
+    """No CPU fallback: without a CUDA device the context cannot be created
+    and the Python wrapper raises."""
+    from diomedes_gb300 import compute
+
+    L = abi.lib()
+    h = ctypes.c_void_p()
+    rc = L.dio_ctx_create(ctypes.byref(compute.capacity(16)), ctypes.byref(h))
+    if rc == abi.DIO_OK:  # a GPU is present: nothing to check here
+        L.dio_ctx_destroy(h)
+        pytest.skip("a CUDA device is present")
+    assert rc == abi.DIO_ERR_CUDA and not h.value
+    with pytest.raises(abi.DioError):
+        compute.World(compute.capacity(16))
