@@ -680,44 +680,47 @@ class Engine final : public EngineBase {
         if (n > cap_.max_bodies) return cap_err("too many bodies");
         if ((uint64_t)n_slots > (uint64_t)cap_.max_pairs * per_cap_) return cap_err("too many slots");
         if (n_prev > cap_.max_contacts) return cap_err("too many previous contacts");
-        if (sizeof(R) != 4) return inval("prepare_contacts needs an FP32 engine");
-        DIO_TRY(upload_bodies(bodies, n));
-        DIO_TRY(upload_state(state, n));
-        DIO_TRY(single_scene(n, container));
-        DIO_CK(cudaMemsetAsync(ctr_, 0, sizeof(Counters), stream_));
-        // previous rows into the "previous" buffer, then their sorted keys
-        int pb = 1 - cur_;
-        if (n_prev) {
-            DioContact* dprev = reinterpret_cast<DioContact*>(dstage_);
-            DIO_CK(cudaMemcpyAsync(dprev, prev, (size_t)n_prev * sizeof(DioContact), cudaMemcpyHostToDevice, stream_));
-            k_unpack_contacts<P, R><<<grid_for(n_prev, 256), 256, 0, stream_>>>(rs_[pb], rd_[pb], ab_[pb], dprev,
-                                                                                n_prev, 0xFFFFFFFFu, &ctr_->error_flags);
-            DIO_TRY(sort_keys(ab_[pb], n_prev, keys_s_[pb], ids_s_[pb]));
+        if constexpr (sizeof(R) != 4) {
+            return inval("prepare_contacts needs an FP32 engine");
+        } else {
+            DIO_TRY(upload_bodies(bodies, n));
+            DIO_TRY(upload_state(state, n));
+            DIO_TRY(single_scene(n, container));
+            DIO_CK(cudaMemsetAsync(ctr_, 0, sizeof(Counters), stream_));
+            // previous rows into the "previous" buffer, then their sorted keys
+            int pb = 1 - cur_;
+            if (n_prev) {
+                DioContact* dprev = reinterpret_cast<DioContact*>(dstage_);
+                DIO_CK(cudaMemcpyAsync(dprev, prev, (size_t)n_prev * sizeof(DioContact), cudaMemcpyHostToDevice, stream_));
+                k_unpack_contacts<P, R><<<grid_for(n_prev, 256), 256, 0, stream_>>>(rs_[pb], rd_[pb], ab_[pb], dprev,
+                                                                                    n_prev, 0xFFFFFFFFu, &ctr_->error_flags);
+                DIO_TRY(sort_keys(ab_[pb], n_prev, keys_s_[pb], ids_s_[pb]));
+            }
+            n_prev_rows_ = n_prev;
+            // slots -> device (FP32 slots are DioContactOut bytes)
+            if (n_slots)
+                DIO_CK(cudaMemcpyAsync(w_.slots, slots, (size_t)n_slots * sizeof(DioContactOut), cudaMemcpyHostToDevice,
+                                       stream_));
+            DIO_TRY(build_rows(opts_prep(*options), n_slots, 1, nullptr, n));
+            DIO_TRY(pull_counters());
+            uint32_t M = hctr_->rows;
+            *m = M;
+            DIO_TRY(finish_rows(opts_prep(*options), M, n));
+            uint32_t ninc = 0;
+            DIO_CK(cudaMemcpyAsync(&ninc, w_.row_off + n, 4, cudaMemcpyDeviceToHost, stream_));
+            DIO_CK(cudaStreamSynchronize(stream_));
+            DIO_TRY(check_flags());
+            if (M > cap || ninc > index_cap) return cap_err("output buffers smaller than the rows / CSR");
+            DioContact* dout = reinterpret_cast<DioContact*>(dstage_);
+            k_pack_contacts<P, R><<<grid_for(M, 256), 256, 0, stream_>>>(w_.rs, w_.rd, w_.ab, dout, &ctr_->rows);
+            if (M) DIO_CK(cudaMemcpyAsync(out, dout, (size_t)M * sizeof(DioContact), cudaMemcpyDeviceToHost, stream_));
+            DIO_CK(cudaMemcpyAsync(offsets, w_.row_off, ((size_t)n + 1) * 4, cudaMemcpyDeviceToHost, stream_));
+            if (ninc) DIO_CK(cudaMemcpyAsync(indices, w_.row_idx, (size_t)ninc * 4, cudaMemcpyDeviceToHost, stream_));
+            DIO_CK(cudaStreamSynchronize(stream_));
+            cur_ = 1 - cur_;
+            set_rows(cur_);
+            return DIO_OK;
         }
-        n_prev_rows_ = n_prev;
-        // slots -> device (FP32 slots are DioContactOut bytes)
-        if (n_slots)
-            DIO_CK(cudaMemcpyAsync(w_.slots, slots, (size_t)n_slots * sizeof(DioContactOut), cudaMemcpyHostToDevice,
-                                   stream_));
-        DIO_TRY(build_rows(opts_prep(*options), n_slots, 1, nullptr, n));
-        DIO_TRY(pull_counters());
-        uint32_t M = hctr_->rows;
-        *m = M;
-        DIO_TRY(finish_rows(opts_prep(*options), M, n));
-        uint32_t ninc = 0;
-        DIO_CK(cudaMemcpyAsync(&ninc, w_.row_off + n, 4, cudaMemcpyDeviceToHost, stream_));
-        DIO_CK(cudaStreamSynchronize(stream_));
-        DIO_TRY(check_flags());
-        if (M > cap || ninc > index_cap) return cap_err("output buffers smaller than the rows / CSR");
-        DioContact* dout = reinterpret_cast<DioContact*>(dstage_);
-        k_pack_contacts<P, R><<<grid_for(M, 256), 256, 0, stream_>>>(w_.rs, w_.rd, w_.ab, dout, &ctr_->rows);
-        if (M) DIO_CK(cudaMemcpyAsync(out, dout, (size_t)M * sizeof(DioContact), cudaMemcpyDeviceToHost, stream_));
-        DIO_CK(cudaMemcpyAsync(offsets, w_.row_off, ((size_t)n + 1) * 4, cudaMemcpyDeviceToHost, stream_));
-        if (ninc) DIO_CK(cudaMemcpyAsync(indices, w_.row_idx, (size_t)ninc * 4, cudaMemcpyDeviceToHost, stream_));
-        DIO_CK(cudaStreamSynchronize(stream_));
-        cur_ = 1 - cur_;
-        set_rows(cur_);
-        return DIO_OK;
     }
 
     int avbd_submit(const DioBodyState* state, const float* positions, const float* orientations, uint32_t n,
