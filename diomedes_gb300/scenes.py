@@ -40,7 +40,7 @@ class Scene:
         """Contiguous runs of whole scenes with about equal body counts, as
         separate Scenes (joints rebased; hull vertices shared).  Returns the
         Scenes and the body offset of each in this one."""
-        off = np.zeros(2, np.int64) if self.scene_offsets is None else self.scene_offsets.astype(np.int64)
+        off = np.array([0, self.n], np.int64) if self.scene_offsets is None else self.scene_offsets.astype(np.int64)
         ns = len(off) - 1
         groups = max(1, min(int(groups), ns))
         cuts = [0]

@@ -81,6 +81,9 @@ def test_scene_split_is_contiguous_complete_and_rebased():
                 assert p.constraints["a"].max() < p.n and p.constraints["b"].max() < p.n
     parts, _ = sc.split(4)
     assert max(p.n for p in parts) < 0.5 * sc.n  # balanced by bodies, not by scenes
+    one = scenes.pyramid(levels=3)  # a single scene (no offsets) stays whole
+    parts, starts = one.split(3)
+    assert len(parts) == 1 and starts == [0] and parts[0].n == one.n
 
 
 def test_two_gloo_ranks_shard_and_reduce():
