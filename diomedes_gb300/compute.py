@@ -197,6 +197,8 @@ def step_host(worlds, bodies, states, options, steps=1):
             raise ValueError(f"world {g}: arrays must hold {worlds[g].n} bodies")
         if not (bodies[g].flags.c_contiguous and states[g].flags.c_contiguous):
             raise ValueError(f"world {g}: arrays must be contiguous (updated in place)")
+        if bodies[g].dtype != abi.BODY or states[g].dtype != abi.BODY_STATE:
+            raise ValueError(f"world {g}: arrays must be abi.BODY and abi.BODY_STATE records")
     hs = (ctypes.c_void_p * n)(*[w.h for w in worlds])
     bp = (ctypes.c_void_p * n)(*[ptr(b) for b in bodies])
     sp = (ctypes.c_void_p * n)(*[ptr(s) for s in states])

@@ -117,3 +117,24 @@ def test_context_creation_without_a_device_fails_loudly():
     assert rc == abi.DIO_ERR_CUDA and not h.value
     with pytest.raises(abi.DioError):
         compute.World(compute.capacity(16))
+
+
+def test_step_host_checks_its_arrays_before_calling_the_library():
+    """compute.step_host validates every world's host arrays (count, length,
+    contiguity, record type) before anything reaches the C ABI."""
+    from diomedes_gb300 import compute
+
+    class World4:  # stands in for a world of 4 bodies; never reaches the library
+        n = 4
+        h = None
+
+    o = ph.avbd_options()
+    b, s = np.zeros(4, abi.BODY), np.zeros(4, abi.BODY_STATE)
+    with pytest.raises(ValueError):
+        compute.step_host([World4()], [b], [], o)
+    with pytest.raises(ValueError):
+        compute.step_host([World4()], [b[:3]], [s[:3]], o)
+    with pytest.raises(ValueError):
+        compute.step_host([World4()], [np.zeros(8, abi.BODY)[::2]], [s], o)
+    with pytest.raises(ValueError):
+        compute.step_host([World4()], [np.zeros(4, abi.BODY_STATE)], [s], o)
