@@ -2,6 +2,7 @@
 analytic cases that pin the restated arithmetic where the reference has no
 test (free fall, sphere overlap, resting force balance, warm start)."""
 import json
+import math
 import os
 
 import numpy as np
@@ -175,3 +176,52 @@ def test_dense_and_sort_and_sweep_pair_sets_agree():
     s, ns = O.broad(sc.bodies, sap=True)
     assert nd == ns and nd > 0
     assert np.array_equal(d, s)
+
+
+def test_spring_hangs_at_its_analytic_extension():
+    """A Hookean spring (k 1e3, rest 0.5) holding 1 kg from a static body
+    settles at rest + m g / k below it (the primal's implicit steps damp the
+    oscillation)."""
+    k, rest, m, g = 1000.0, 0.5, 1.0, 10.0
+    b, s = ph.pack_bodies([ph.sphere((0, 10, 0), 0.2, 0.0), ph.sphere((0, 10 - rest, 0), 0.2, m)])
+    cons = ph.pack_joints([ph.spring(0, 1, (0, 0, 0), (0, 0, 0), k, rest)])
+    sc = scenes.Scene("spring", b, s, constraints=cons, options=ph.avbd_options(gravity=(0, -g, 0)))
+    w = O.World(sc)
+    w.step(sc.options, 600)
+    bb, _ = w.download()
+    assert bb["position"][1, 1] == pytest.approx(10 - rest - m * g / k, abs=1e-4)
+
+
+def _box_on_slope(theta_deg, mu, steps, **opt):
+    """A unit cube resting on a container floor tilted by theta about z (the
+    box aligned with the floor); its centre before and after each run of steps."""
+    th = math.radians(theta_deg)
+    half, h = 50.0, 0.5
+    q = (0.0, 0.0, math.sin(th / 2), math.cos(th / 2))
+    up = np.array([-math.sin(th), math.cos(th), 0.0])
+    p0 = -(half - h) * up
+    b, s = ph.pack_bodies([ph.cube(tuple(p0), h, 1.0, orientation=q)])
+    sc = scenes.Scene("slope", b, s, containers=[ph.container((0, 0, 0), half, q)],
+                      options=ph.avbd_options(gravity=(0, -9.81, 0), friction=mu, **opt))
+    w = O.World(sc)
+    out = []
+    for k in steps:
+        w.step(sc.options, k)
+        out.append(w.download()[0]["position"][0, :3].astype(np.float64))
+    return p0, out
+
+
+def test_box_slides_down_a_steep_slope_at_the_coulomb_rate():
+    """40 degrees, mu 0.5 (tan 40 > mu): after 2 s the box has slid
+    g (sin - mu cos) t^2 / 2 (5.10 m), within 3 %."""
+    p0, (p,) = _box_on_slope(40.0, 0.5, [120])
+    th = math.radians(40.0)
+    expect = 0.5 * 9.81 * (math.sin(th) - 0.5 * math.cos(th)) * 2.0 ** 2
+    assert float(np.linalg.norm(p - p0)) == pytest.approx(expect, rel=0.03)
+
+
+def test_box_sticks_on_a_shallow_slope():
+    """10 degrees, mu 0.5 (tan 10 < mu), the stiff parameters of the pyramid
+    workload: after settling the box does not move (under 1 mm in 2 s)."""
+    p0, (a, b) = _box_on_slope(10.0, 0.5, [60, 120], alpha=0.95, beta_lin=1e5, penalty_min=1e4)
+    assert float(np.linalg.norm(b - a)) < 1e-3
