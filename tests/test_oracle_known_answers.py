@@ -225,3 +225,39 @@ def test_box_sticks_on_a_shallow_slope():
     workload: after settling the box does not move (under 1 mm in 2 s)."""
     p0, (a, b) = _box_on_slope(10.0, 0.5, [60, 120], alpha=0.95, beta_lin=1e5, penalty_min=1e4)
     assert float(np.linalg.norm(b - a)) < 1e-3
+
+
+def test_rope_is_free_while_slack_and_holds_at_its_length():
+    """A rope (max length 1.0, k 1e3) from a static body: while slack the body
+    follows the free-fall recurrence of the implicit step (v -= g dt, y += v
+    dt); once taut it hangs at the length plus m g / k."""
+    g, dt = 10.0, 1.0 / 60.0
+    b, s = ph.pack_bodies([ph.sphere((0, 10, 0), 0.1, 0.0), ph.sphere((0, 9.5, 0), 0.1, 1.0)])
+    cons = ph.pack_joints([ph.rope(0, 1, (0, 0, 0), (0, 0, 0), 1.0)])
+    sc = scenes.Scene("rope", b, s, constraints=cons, options=ph.avbd_options(gravity=(0, -g, 0)))
+    w = O.World(sc)
+    v, y = 0.0, 9.5
+    for _ in range(6):
+        w.step(sc.options, 1)
+        v -= g * dt
+        y += v * dt
+        assert w.download()[0]["position"][1, 1] == pytest.approx(y, abs=1e-5)
+    w.step(sc.options, 600)
+    assert w.download()[0]["position"][1, 1] == pytest.approx(10.0 - 1.0 - 1.0 * g / float(ph.DEFAULT_ROPE_STIFFNESS),
+                                                             abs=1e-4)
+
+
+def test_pendulum_keeps_its_length_and_gains_no_energy():
+    """A body on a ball socket 0.8 m from a static pivot, released level with
+    it: every sampled position stays 0.8 m (plus the joint's stretch under
+    load, k 1e3) from the pivot and never rises above the release height."""
+    b, s = ph.pack_bodies([ph.sphere((0, 10, 0), 0.1, 0.0), ph.sphere((0.8, 10, 0), 0.1, 1.0)])
+    cons = ph.pack_joints([ph.ball_socket(0, 1, (0, 0, 0), (-0.8, 0, 0))])
+    sc = scenes.Scene("pendulum", b, s, constraints=cons, options=ph.avbd_options(gravity=(0, -10.0, 0)))
+    w = O.World(sc)
+    for _ in range(20):
+        w.step(sc.options, 60)
+        p = w.download()[0]["position"][1, :3].astype(np.float64)
+        r = float(np.linalg.norm(p - np.array([0.0, 10.0, 0.0])))
+        assert 0.79 < r < 0.84
+        assert p[1] <= 10.0 + 1e-4
