@@ -261,3 +261,21 @@ def test_pendulum_keeps_its_length_and_gains_no_energy():
         r = float(np.linalg.norm(p - np.array([0.0, 10.0, 0.0])))
         assert 0.79 < r < 0.84
         assert p[1] <= 10.0 + 1e-4
+
+
+def test_gjk_epa_box_sphere_face_contact():
+    """A unit cube and a sphere (r 0.3) overlapping through a face: GJK + EPA
+    give the face normal (a -> b), depth h + r - d, and witnesses on the cube's
+    face and on the sphere's surface (EPA tolerance 1e-4)."""
+    for centre, axis in (((0, 0.7, 0), 1), ((0.7, 0, 0), 0), ((0, 0, -0.75), 2)):
+        b, _ = ph.pack_bodies([ph.cube((0, 0, 0), 0.5, 1.0), ph.sphere(centre, 0.3, 1.0)])
+        v = O.narrow(b, pair01())
+        d = abs(centre[axis])
+        sign = np.sign(centre[axis])
+        n = np.zeros(3)
+        n[axis] = sign
+        assert v["valid"][0] == 1
+        assert v["depth"][0] == pytest.approx(0.5 + 0.3 - d, abs=1e-4)
+        assert np.allclose(v["normal"][0, :3], n, atol=1e-4)
+        assert np.allclose(v["point_a"][0, :3], 0.5 * n, atol=1e-4)
+        assert np.allclose(v["point_b"][0, :3], (d - 0.3) * n, atol=1e-4)
