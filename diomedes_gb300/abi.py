@@ -36,6 +36,7 @@ CKPT_HEADER = np.dtype([("magic", "S8"), ("version", "<u4"), ("precision", "<u4"
                         ("total_bytes", "<u8")])
 PRIMAL_VARIANTS = 10  # DIO_PRIMAL_VARIANTS
 XFORM_POSE, XFORM_MAT4 = 0, 1  # DIO_XFORM_*
+DEBUG_EPA_NO_FIRST_WAIT = 1  # DIO_DEBUG_EPA_NO_FIRST_WAIT (DioConfig.debug_flags, tests only)
 
 SOLVER_JACOBI, SOLVER_COLORED = 0, 1
 PREC_F32, PREC_SPLIT, PREC_F64 = 0, 1, 2
@@ -96,7 +97,7 @@ class Config(ctypes.Structure):
     _fields_ = [("solver_mode", _u32), ("precision", _u32), ("contacts_per_pair", _u32),
                 ("use_graph", _u32), ("primal_variant", _u32), ("block_size", _u32),
                 ("batched_solver", _u32), ("profile", _u32), ("broad_phase", _u32),
-                ("bvh_rebuild_period", _u32), ("contact_lag", _u32), ("reserved", _u32 * 1)]
+                ("bvh_rebuild_period", _u32), ("contact_lag", _u32), ("debug_flags", _u32)]
 
 
 class WorldDesc(ctypes.Structure):

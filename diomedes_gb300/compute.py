@@ -25,6 +25,24 @@ def capacity(max_bodies, max_pairs=None, max_contacts=None, max_joints=0, max_sc
     return c
 
 
+def check_hull_ranges(bodies, n_hull):
+    """Host-side mirror of the library's upload check: every HULL body's
+    vertex range [pad[0], pad[0] + pad[1]) lies inside a hull-vertex pool of
+    n_hull vertices (the support queries and the EPA's bulk copies read it).
+    Raises ValueError naming the first body that does not."""
+    b = np.asarray(bodies)
+    if not len(b):
+        return
+    sh = b["shape"]
+    hull = sh["tag"] == abi.HULL
+    end = sh["pad"][:, 0].astype(np.uint64) + sh["pad"][:, 1].astype(np.uint64)
+    bad = np.flatnonzero(hull & (end > np.uint64(n_hull)))
+    if len(bad):
+        i = int(bad[0])
+        raise ValueError(f"body {i}: hull vertices [{int(sh['pad'][i, 0])}, {int(end[i])}) lie beyond the "
+                         f"{int(n_hull)}-vertex hull pool")
+
+
 class Context:
     """Owns one DioCtx (a CUDA stream plus device buffers)."""
 
@@ -251,6 +269,7 @@ class World(Context):
             keep.append(hv)
             d.n_hull_vertices = len(hv)
             d.hull_vertices = ptr(hv)
+        check_hull_ranges(bodies, d.n_hull_vertices)
         if positions_f64 is not None:
             p = np.ascontiguousarray(positions_f64, np.float64)
             keep.append(p)
@@ -324,7 +343,7 @@ class World(Context):
         path = cache_path.encode() if cache_path else None
         check(self.L.dio_autotune(self.h, ctypes.byref(options), trial_steps, path, ctypes.byref(c)), self.h,
               "autotune")
-        return {name: getattr(c, name) for name, _ in abi.Config._fields_ if name != "reserved"}
+        return {name: getattr(c, name) for name, _ in abi.Config._fields_}
 
     def reset_timers(self):
         check(self.L.dio_world_reset_timers(self.h), self.h, "reset_timers")

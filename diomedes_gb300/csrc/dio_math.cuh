@@ -3,8 +3,8 @@
 // The reference kernels use glam 0.33.3 f32 types (Vec3, Quat, Mat3) inside
 // rust-gpu shaders (engine/gpu_physics/*/src/*.rs).  These helpers restate the
 // operations the reference calls -- Hamilton product, conjugate inverse of a
-// unit quaternion, rotation v' = q v q*, normalisation as v * (1/|v|) -- with
-// a fixed left-to-right evaluation order.  The library is compiled with
+// unit quaternion, rotation q * v in glam's mul_vec3 form, normalisation as
+// v * (1/|v|) -- with a fixed left-to-right evaluation order.  The library is compiled with
 // --fmad=false, so every expression rounds exactly as written and pair sets,
 // manifold counts and solver states are reproducible bit for bit.
 #pragma once
@@ -92,12 +92,16 @@ DIO_HD Q4<R> qmul(Q4<R> a, Q4<R> b) {
 }
 template <class R>
 DIO_HD Q4<R> conj(Q4<R> q) { return {-q.x, -q.y, -q.z, q.w}; }
-// v' = q v q* for unit q: v + w t + b x t with t = 2 (b x v).
+// q * v for unit q, in the form glam 0.33's Quat::mul_vec3 evaluates it
+// (its scalar path, also what the rust-gpu shaders compile): with b = q.xyz,
+//   v (w w - b.b) + b (2 (v.b)) + (b x v) (2 w),
+// each product rounded, sums left to right.
 template <class R>
 DIO_HD V3<R> rotate(Q4<R> q, V3<R> v) {
-    V3<R> b{q.x, q.y, q.z};
-    V3<R> t = scale(cross(b, v), R(2));
-    return add(add(v, scale(t, q.w)), cross(b, t));
+    const V3<R> b{q.x, q.y, q.z};
+    const R b2 = dot(b, b);
+    const V3<R> r = add(scale(v, q.w * q.w - b2), scale(b, dot(v, b) * R(2)));
+    return add(r, scale(cross(b, v), q.w * R(2)));
 }
 template <class R>
 DIO_HD Q4<R> qnormalize(Q4<R> q) {

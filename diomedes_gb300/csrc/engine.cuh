@@ -137,6 +137,7 @@ struct DevWorld {
     uint32_t* gjk_list;
     A4<R>* simplex;   // 8 x A4 per EPA entry (4 points, 4 witnesses)
     uint32_t* epa_list;
+    uint32_t epa_wait_polls;  // budget of the EPA's first wait for its hull copies
     // rows
     RowStatic<R>* rs;
     RowDual<P, R>* rd;

@@ -520,6 +520,7 @@ class Engine final : public EngineBase {
         w_.hull = hull_;
         w_.max_pairs = PP;
         w_.per_pair = per_cap_;
+        w_.epa_wait_polls = (cfg_.debug_flags & DIO_DEBUG_EPA_NO_FIRST_WAIT) ? 0u : kEpaWaitPolls;
         w_.max_rows = M;
         w_.max_incid = 2 * M;
         w_.joints = joints_;
@@ -592,6 +593,7 @@ class Engine final : public EngineBase {
         if (cfg_.contacts_per_pair > per_cap_) cfg_.contacts_per_pair = per_cap_;
         // lagged rows need the previous step's slots in this layout
         if (cfg_.contacts_per_pair != per || !cfg_.contact_lag) lag_primed_ = false;
+        w_.epa_wait_polls = (cfg_.debug_flags & DIO_DEBUG_EPA_NO_FIRST_WAIT) ? 0u : kEpaWaitPolls;
     }
 
     // ------------------------------------------------ reference-mirror API
@@ -602,7 +604,7 @@ class Engine final : public EngineBase {
             DIO_CK(cudaMemsetAsync(ctr_, 0, sizeof(Counters), stream_));
             return DIO_OK;
         }
-        DIO_TRY(upload_bodies(bodies, n));
+        DIO_TRY(upload_bodies(bodies, n, n_hull_));
         DIO_TRY(single_scene(n, nullptr));
         DIO_CK(cudaMemsetAsync(ctr_, 0, sizeof(Counters), stream_));
         rebuild_now_ = true;
@@ -632,7 +634,7 @@ class Engine final : public EngineBase {
         if (np > cap_.max_pairs) return cap_err("too many pairs for the compute buffers");
         last_np_ = np;
         if (np == 0) return DIO_OK;
-        DIO_TRY(upload_bodies(bodies, n));
+        DIO_TRY(upload_bodies(bodies, n, n_hull_));
         api_bodies_ = n;
         DIO_TRY(single_scene(n, nullptr));
         DIO_CK(cudaMemcpyAsync(w_.pairs, pairs, (size_t)np * sizeof(DioPair), cudaMemcpyHostToDevice, stream_));
@@ -663,12 +665,16 @@ class Engine final : public EngineBase {
     }
     int set_hull(const float* xyzw, uint32_t count) override {
         if (count > cap_.max_hull_vertices) return cap_err("too many hull vertices");
-        if (count == 0) return DIO_OK;
+        if (count == 0) {
+            n_hull_ = 0;
+            return DIO_OK;
+        }
         std::vector<A4<R>> tmp(count);
         for (uint32_t i = 0; i < count; ++i)
             tmp[i] = A4<R>{R(xyzw[4 * i]), R(xyzw[4 * i + 1]), R(xyzw[4 * i + 2]), R(0)};
         DIO_CK(cudaMemcpyAsync(hull_, tmp.data(), count * sizeof(A4<R>), cudaMemcpyHostToDevice, stream_));
         DIO_CK(cudaStreamSynchronize(stream_));
+        n_hull_ = count;
         return DIO_OK;
     }
 
@@ -683,7 +689,7 @@ class Engine final : public EngineBase {
         if constexpr (sizeof(R) != 4) {
             return inval("prepare_contacts needs an FP32 engine");
         } else {
-            DIO_TRY(upload_bodies(bodies, n));
+            DIO_TRY(upload_bodies(bodies, n, n_hull_));
             DIO_TRY(upload_state(state, n));
             DIO_TRY(single_scene(n, container));
             DIO_CK(cudaMemsetAsync(ctr_, 0, sizeof(Counters), stream_));
@@ -808,10 +814,13 @@ class Engine final : public EngineBase {
         if (ns > cap_.max_scenes) return cap_err("too many scenes");
         if (d->n_hull_vertices > cap_.max_hull_vertices) return cap_err("too many hull vertices");
         if (n && (!d->bodies || !d->state)) return inval("null bodies/state");
+        if (d->n_hull_vertices && !d->hull_vertices) return inval("null hull vertices");
+        if (n && !hull_ranges_ok(d->bodies, n, d->n_hull_vertices))
+            return inval("hull vertex range beyond the hull-vertex pool");
         drop_graphs();
         lbvh_valid_ = false;
         w_.n_joints = 0;  // the world's joints are uploaded below
-        DIO_TRY(upload_bodies(d->bodies, n));
+        DIO_TRY(upload_bodies(d->bodies, n, d->n_hull_vertices));
         if (d->positions_f64 || d->orientations_f64) {
             double* dp = reinterpret_cast<double*>(dstage_);
             double* dq = dp + 3 * (size_t)n;
@@ -1086,9 +1095,19 @@ class Engine final : public EngineBase {
         }
         return DIO_OK;
     }
-    int upload_bodies(const DioGpuBody* bodies, uint32_t n) {
+    // a hull body's vertex range [first, first + count) must lie in the
+    // hull-vertex pool: the support queries and the EPA's bulk copies read it
+    static bool hull_ranges_ok(const DioGpuBody* bodies, uint32_t n, uint32_t n_hull) {
+        for (uint32_t i = 0; i < n; ++i) {
+            const DioShape& sh = bodies[i].shape;
+            if (sh.tag == DIO_SHAPE_HULL && (uint64_t)sh.pad[0] + sh.pad[1] > n_hull) return false;
+        }
+        return true;
+    }
+    int upload_bodies(const DioGpuBody* bodies, uint32_t n, uint32_t n_hull) {
         if (!n) return DIO_OK;
         if (!bodies) return inval("null bodies");
+        if (!hull_ranges_ok(bodies, n, n_hull)) return inval("hull vertex range beyond the hull-vertex pool");
         DioGpuBody* db = reinterpret_cast<DioGpuBody*>(dstage_);
         DIO_CK(cudaMemcpyAsync(db, bodies, (size_t)n * sizeof(DioGpuBody), cudaMemcpyHostToDevice, stream_));
         k_unpack_bodies<P, R><<<grid_for(n, 256), 256, 0, stream_>>>(w_, db, n);

@@ -135,6 +135,7 @@ __device__ __forceinline__ bool mbar_wait_warp(uint64_t* bar, uint32_t parity, u
 }
 
 constexpr uint32_t kHullStage = 64;  // vertices per hull staged in shared memory
+constexpr uint32_t kEpaWaitPolls = 1u << 20;  // rounds of the bounded waits for the hull copies
 
 // Stage 3: EPA, one warp per queued pair, polytope in shared memory.  Hull
 // vertex lists (both bodies, up to 64 vertices each) are staged into the
@@ -175,11 +176,18 @@ __global__ void __launch_bounds__(32 * epa_warps<R>()) k_epa(DevWorld<P, R> w) {
                     bulk_g2s(&hull_s[warp][kHullStage], w.hull + b.shape.hf, b.shape.hc * sizeof(A4<R>),
                              &mbar[warp]);
             }
-            bool done = mbar_wait_warp(&mbar[warp], parity, 1u << 20);
+            bool done = mbar_wait_warp(&mbar[warp], parity, w.epa_wait_polls);
             if (!done) {
                 if (lane == 0) atomicOr(&w.ctr->error_flags, kErrTimeout);
-                done = mbar_wait_warp(&mbar[warp], parity, 1u << 20);  // let the copies land
-                if (!done) return;                                     // warp-uniform
+                done = mbar_wait_warp(&mbar[warp], parity, kEpaWaitPolls);  // let the copies land
+                if (!done) {
+                    // the copies still have not landed: take no further pair
+                    // (the step already reports DIO_ERR_TIMEOUT) and keep
+                    // this warp, and so its CTA's shared memory, resident
+                    // for one last, longer bounded wait before exiting
+                    mbar_wait_warp(&mbar[warp], parity, 16u * kEpaWaitPolls);
+                    return;  // warp-uniform
+                }
             }
             parity ^= 1u;
             hull = &hull_s[warp][0];

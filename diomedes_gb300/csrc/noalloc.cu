@@ -15,7 +15,14 @@
 // keeps the last call's contents, so calls that overlap on the GPU (two
 // streams, two host threads) race; serialise them.  The first call on each
 // device looks up the array's device address (cudaGetSymbolAddress) with
-// that device current; make that first call before any stream capture.
+// that device current; make that first call before any stream capture.  The
+// address is cached per device together with the id of the CUDA context it
+// belongs to, and looked up again when the current context is a different
+// one (after cudaDeviceReset, say), so a stale address is never used.
+// The call is synchronous: it waits on the caller's stream twice (once to
+// validate the caller's indices before any kernel dereferences them, once at
+// the end to read the device error flags).
+#include <cuda.h>  // driver types only: the two entry points are fetched at run time
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -35,7 +42,7 @@ constexpr int kNaMaxDevices = 64;
 // scratch layout (byte offsets into the array)
 constexpr size_t kB4 = sizeof(A4<float>) * kNaMaxBodies;  // one per-body A4 array
 constexpr size_t kOffPose = 0;                            // pos[2], rot[2], init x2, inert x2, vel, ang, prev, inv
-constexpr size_t kNumBodyA4 = 14;
+constexpr size_t kNumBodyA4 = 12;
 constexpr size_t kOffFric = kOffPose + kNumBodyA4 * kB4;
 constexpr size_t kOffRs = kOffFric + sizeof(float) * kNaMaxBodies;
 constexpr size_t kOffRd = kOffRs + sizeof(RowStatic<float>) * kNaMaxContacts;
@@ -46,19 +53,65 @@ constexpr size_t kNaScratchBytes = (kOffCtr + sizeof(Counters) + 255) & ~size_t(
 
 static __device__ __align__(256) unsigned char dio_noalloc_scratch[kNaScratchBytes];
 
-void* g_scratch[kNaMaxDevices] = {};
+// per device: the array's address and the id of the context it belongs to
+struct ScratchEntry {
+    unsigned long long ctx = 0;
+    void* ptr = nullptr;
+};
+ScratchEntry g_scratch[kNaMaxDevices];
 std::mutex g_mu;
 
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+// id of the calling thread's current context (cuCtxGetCurrent + cuCtxGetId,
+// fetched from the driver through the runtime, so the library does not link
+// the driver library); false when there is none yet or the driver lacks them
+bool current_context_id(unsigned long long* id) {
+    static std::once_flag once;
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<CtxGetIdFn>(f);
+    });
+    if (!get_current || !get_id) return false;
+    CUcontext c = nullptr;
+    if (get_current(&c) != CUDA_SUCCESS || !c) return false;
+    return get_id(c, id) == CUDA_SUCCESS;
+}
+
+// The device address of the scratch array for the current device and
+// context.  Host code cannot use the array's name as a device address; the
+// address comes from cudaGetSymbolAddress with the device current.
 int scratch_ptr(unsigned char** out) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNaMaxDevices) return DIO_ERR_CUDA;
+    unsigned long long ctx = 0;
+    const bool known = current_context_id(&ctx);
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_scratch[dev]) {
-        void* p = nullptr;
-        if (cudaGetSymbolAddress(&p, dio_noalloc_scratch) != cudaSuccess || !p) return DIO_ERR_CUDA;
-        g_scratch[dev] = p;
+    ScratchEntry& e = g_scratch[dev];
+    if (known && e.ptr && e.ctx == ctx) {
+        *out = static_cast<unsigned char*>(e.ptr);
+        return DIO_OK;
     }
-    *out = static_cast<unsigned char*>(g_scratch[dev]);
+    // first call on this device, a different context, or no context current
+    // yet: look the address up (which makes the device's context current)
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, dio_noalloc_scratch) != cudaSuccess || !p) return DIO_ERR_CUDA;
+    unsigned long long now = 0;
+    if (current_context_id(&now))
+        e = ScratchEntry{now, p};
+    else
+        e = ScratchEntry{};  // without a context id nothing is cached: every call asks again
+    *out = static_cast<unsigned char*>(p);
     return DIO_OK;
 }
 
@@ -275,7 +328,12 @@ extern "C" int dio_avbd_solve_noalloc(const DioBodyState* state, const float* po
     k_recover<float, float><<<gb, 256, 0, s>>>(w, 0, n, rb, final_buf, o);
     k_na_pack<<<gb, 256, 0, s>>>(w, n, final_buf, state, out_positions, out_orientations, out_state);
     if (m) k_na_dual_out<<<grid_for(m, 256), 256, 0, s>>>(w, contacts, m);
+    // recover flags a non-finite pose or velocity, as the context-based solve
+    // reports it (dio_avbd_read)
+    if (cudaMemcpyAsync(&flags, &w.ctr->error_flags, sizeof flags, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        return DIO_ERR_CUDA;
     if (cudaGetLastError() != cudaSuccess) return DIO_ERR_CUDA;
     if (cudaStreamSynchronize(s) != cudaSuccess) return DIO_ERR_CUDA;
+    if (flags & kErrNonFinite) return DIO_ERR_NONFINITE;
     return DIO_OK;
 }

@@ -229,8 +229,15 @@ typedef struct DioConfig {
                                    step's transforms; demos/avbd_box/src/
                                    main.rs:203-207,244-249); container rows
                                    are current.  0 (default): no lag      */
-    uint32_t reserved[1];
+    uint32_t debug_flags;       /* testing only, 0 in normal use:
+                                   DIO_DEBUG_EPA_NO_FIRST_WAIT makes the
+                                   EPA's first bounded wait for its hull
+                                   copies give up at once (the step then
+                                   returns DIO_ERR_TIMEOUT; the second
+                                   wait, always at its full budget, still
+                                   lets the copies land)                  */
 } DioConfig;
+#define DIO_DEBUG_EPA_NO_FIRST_WAIT 1u
 
 /* World description for the fused device-resident step (extension of the
  * demos' per-frame loop, demos/avbd_box/src/main.rs:189-273). */
@@ -353,8 +360,13 @@ int dio_avbd_read(DioCtx* ctx, const DioAvbdResult* out);
  * contacts and 4096 joints, else DIO_ERR_CAPACITY.  Joints are scanned per
  * body as in the reference.  Calls share that array, so calls that overlap
  * on the GPU race.  The first call on each device looks up the array's
- * address; make it before any stream capture.  Synchronous: returns once
- * the solve on `cuda_stream` (NULL = default stream) has finished. */
+ * address with that device current and caches it for the current CUDA
+ * context (a new context, e.g. after cudaDeviceReset, is looked up again);
+ * make that first call before any stream capture.  Synchronous: it waits on
+ * `cuda_stream` (NULL = default stream) once to validate the indices
+ * (DIO_ERR_INVALID for a contact, CSR or joint index out of range) and once
+ * at the end; a non-finite pose or velocity after the solve returns
+ * DIO_ERR_NONFINITE, as dio_avbd_read does. */
 int dio_avbd_solve_noalloc(const DioBodyState* state, const float* positions,
                            const float* orientations, uint32_t n,
                            DioContact* contacts, uint32_t m,

@@ -17,20 +17,27 @@ DEPS = SOURCES + [os.path.join(HERE, "dio_oracle.hpp"),
                   os.path.join(HERE, "..", "include", "dio_cuda.h")]
 
 
-def build(force=False, verbose=False):
+# build variants of the oracle for tests that measure a rounding choice:
+# rotate_tq rotates vectors as v + w t + b x t (t = 2 b x v) instead of glam's
+# mul_vec3 form
+VARIANTS = {"": [], "rotate_tq": ["-DDIO_ORACLE_ROTATE_TQ"]}
+
+
+def build(force=False, verbose=False, variant=""):
     os.makedirs(OUT_DIR, exist_ok=True)
-    if not force and os.path.exists(LIB):
-        mtime = os.path.getmtime(LIB)
+    lib = LIB if not variant else os.path.join(OUT_DIR, f"liboracle_{variant}.so")
+    if not force and os.path.exists(lib):
+        mtime = os.path.getmtime(lib)
         if all(os.path.getmtime(d) <= mtime for d in DEPS):
-            return LIB
+            return lib
     cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp",
-           "-ffp-contract=off", "-fno-fast-math", "-Wall", "-Wno-unknown-pragmas",
-           "-o", LIB + ".tmp"] + SOURCES
+           "-ffp-contract=off", "-fno-fast-math", "-Wall", "-Wno-unknown-pragmas"] + VARIANTS[variant] + \
+          ["-o", lib + ".tmp"] + SOURCES
     if verbose:
         print(" ".join(cmd))
     subprocess.check_call(cmd)
-    os.replace(LIB + ".tmp", LIB)
-    return LIB
+    os.replace(lib + ".tmp", lib)
+    return lib
 
 
 if __name__ == "__main__":

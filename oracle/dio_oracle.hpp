@@ -23,9 +23,10 @@
 // Float op order follows the reference expression by expression (left to
 // right, no contraction: compile with -ffp-contract=off).  glam 0.33.3
 // (Vec3/Quat/Mat3) is a third-party dependency absent from the reference
-// tree; its operations are restated from their mathematical definitions
-// (Hamilton product, conjugate inverse of a unit quaternion, v' = q v q*,
-// normalise as v * (1/|v|)).
+// tree; its operations are restated from its published scalar forms:
+// Hamilton product with glam's term order, conjugate inverse of a unit
+// quaternion, q * v as (w w - b.b) v + 2 (v.b) b + 2 w (b x v), normalise as
+// v * (1/|v|).
 #pragma once
 
 #include <algorithm>
@@ -98,12 +99,23 @@ inline Qt<R> qmul(Qt<R> a, Qt<R> b) {
 // Inverse of a unit quaternion (the conjugate).
 template <class R>
 inline Qt<R> conj(Qt<R> q) { return {-q.x, -q.y, -q.z, q.w}; }
-// v' = q v q* for unit q, as v + w t + b x t with t = 2 (b x v).
+// q * v for unit q (glam 0.33.3 Quat::mul_vec3, the published scalar form
+// that the shader build and glam's scalar path evaluate): with b = q.xyz,
+//   v (w w - b.b) + b (2 (v.b)) + (b x v) (2 w)
+// -- every product rounded, sums left to right.  DIO_ORACLE_ROTATE_TQ
+// selects the algebraically equal v + w t + b x t, t = 2 (b x v), which the
+// tests build separately to measure how far the rotation's rounding alone
+// moves a step.
 template <class R>
 inline V3<R> rotate(Qt<R> q, V3<R> v) {
     V3<R> b{q.x, q.y, q.z};
+#ifdef DIO_ORACLE_ROTATE_TQ
     V3<R> t = cross(b, v) * R(2);
     return v + t * q.w + cross(b, t);
+#else
+    const R b2 = dot(b, b);
+    return v * (q.w * q.w - b2) + b * (dot(v, b) * R(2)) + cross(b, v) * (q.w * R(2));
+#endif
 }
 template <class R>
 inline Qt<R> qnormalize(Qt<R> q) {

@@ -4,12 +4,12 @@ tests on this path, as data.
 The reference is Rust (and rust-gpu shaders) and cannot be built or imported
 here, so its tests are read as text: every case below carries the file:line
 range it comes from and the literal fragments of that source (inputs and
-assertions) it transcribes.  Run with the reference checkout's root as the
-argument (default /root/reference) to check that each range still contains
+assertions) it transcribes.  Give the reference checkout's root as the
+argument, or in DIO_REFERENCE_ROOT, to check that each range still contains
 its fragments before the fixture is written; without the checkout the
 fixture is written from the transcription alone.
 
-    python tests/golden/make_reference_cases.py [/root/reference]
+    python tests/golden/make_reference_cases.py [REFERENCE_ROOT]
 """
 import json
 import os
@@ -103,8 +103,10 @@ def check(root):
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    checked = os.path.isdir(root)
+    # the reference checkout: the first argument or DIO_REFERENCE_ROOT; with
+    # neither, the fixture is written without checking the cited fragments
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("DIO_REFERENCE_ROOT", "")
+    checked = bool(root) and os.path.isdir(root)
     if checked:
         bad = check(root)
         if bad:

@@ -16,16 +16,17 @@ from diomedes_gb300 import abi  # noqa: E402
 
 _u32 = ctypes.c_uint32
 _vp = ctypes.c_void_p
-_L = None
+_LIBS = {}
 
 
-def lib():
-    global _L
-    if _L is None:
+def lib(variant=""):
+    """The oracle library; `variant` names a build variant of oracle/build.py
+    (the default is the reference arithmetic)."""
+    if variant not in _LIBS:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import build as oracle_build  # oracle/build.py
 
-        path = oracle_build.build()
+        path = oracle_build.build(variant=variant)
         L = ctypes.CDLL(path)
         protos = {
             "oracle_support": [_vp, _vp, _vp, _u32, _vp],
@@ -54,8 +55,8 @@ def lib():
         L.oracle_world_destroy.restype = None
         L.oracle_color_hash.argtypes = [_u32]
         L.oracle_color_hash.restype = _u32
-        _L = L
-    return _L
+        _LIBS[variant] = L
+    return _LIBS[variant]
 
 
 P = abi.ptr
@@ -146,8 +147,10 @@ def avbd_run(state, positions, orientations, contacts, constraints, offsets, ind
 class World:
     """Oracle world: same descriptor as the CUDA world."""
 
-    def __init__(self, scene, precision=0, solver_mode=0, contacts_per_pair=4, threads=1, contact_lag=0):
+    def __init__(self, scene, precision=0, solver_mode=0, contacts_per_pair=4, threads=1, contact_lag=0,
+                 variant=""):
         self._keep = []
+        self.L = lib(variant)
         d = abi.WorldDesc()
         b = np.ascontiguousarray(scene.bodies, abi.BODY)
         s = np.ascontiguousarray(scene.state, abi.BODY_STATE)
@@ -180,46 +183,46 @@ class World:
         cfg.solver_mode = solver_mode
         cfg.contacts_per_pair = contacts_per_pair
         cfg.contact_lag = contact_lag
-        self.h = lib().oracle_world_create(ctypes.byref(d), ctypes.byref(cfg), threads)
+        self.h = self.L.oracle_world_create(ctypes.byref(d), ctypes.byref(cfg), threads)
         self.n = len(b)
 
     def __del__(self):
         if getattr(self, "h", None):
-            lib().oracle_world_destroy(self.h)
+            self.L.oracle_world_destroy(self.h)
             self.h = None
 
     def step(self, options, steps=1):
-        lib().oracle_world_step(self.h, ctypes.byref(options), steps)
+        self.L.oracle_world_step(self.h, ctypes.byref(options), steps)
 
     def set_lag(self, on):
-        lib().oracle_world_set_lag(self.h, int(on))
+        self.L.oracle_world_set_lag(self.h, int(on))
 
     def download(self):
         b = np.zeros(self.n, abi.BODY)
         s = np.zeros(self.n, abi.BODY_STATE)
-        lib().oracle_world_download(self.h, P(b), P(s))
+        self.L.oracle_world_download(self.h, P(b), P(s))
         return b, s
 
     def download_f64(self):
         p = np.zeros((self.n, 3), np.float64)
         q = np.zeros((self.n, 4), np.float64)
-        lib().oracle_world_download_f64(self.h, P(p), P(q))
+        self.L.oracle_world_download_f64(self.h, P(p), P(q))
         return p, q
 
     def contacts(self):
         m = _u32()
-        lib().oracle_world_contacts(self.h, None, 0, ctypes.byref(m))
+        self.L.oracle_world_contacts(self.h, None, 0, ctypes.byref(m))
         out = np.zeros(max(1, m.value), abi.CONTACT)
-        lib().oracle_world_contacts(self.h, P(out), len(out), ctypes.byref(m))
+        self.L.oracle_world_contacts(self.h, P(out), len(out), ctypes.byref(m))
         return out[: m.value]
 
     def colors(self):
         out = np.zeros(self.n, np.uint32)
         n = _u32()
-        lib().oracle_world_colors(self.h, P(out), len(out), ctypes.byref(n))
+        self.L.oracle_world_colors(self.h, P(out), len(out), ctypes.byref(n))
         return out[: n.value]
 
     def stats(self):
         s = abi.StepStats()
-        lib().oracle_world_stats(self.h, ctypes.byref(s))
+        self.L.oracle_world_stats(self.h, ctypes.byref(s))
         return {"pairs": s.pairs, "contacts": s.contacts, "colors": s.colors, "error_flags": s.error_flags}

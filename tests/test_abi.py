@@ -138,3 +138,26 @@ def test_step_host_checks_its_arrays_before_calling_the_library():
         compute.step_host([World4()], [np.zeros(8, abi.BODY)[::2]], [s], o)
     with pytest.raises(ValueError):
         compute.step_host([World4()], [np.zeros(4, abi.BODY_STATE)], [s], o)
+
+
+def test_hull_ranges_are_checked_on_the_host():
+    """compute.check_hull_ranges mirrors the library's upload check: a HULL
+    body's vertex range must lie inside the hull-vertex pool (including a
+    first + count that wraps 32 bits)."""
+    from diomedes_gb300 import compute, scenes
+
+    sc = scenes.mixed_pile(n=60, extent=3.0)
+    nh = len(sc.hull_vertices)
+    compute.check_hull_ranges(sc.bodies, nh)
+    b = sc.bodies.copy()
+    i = int(np.flatnonzero(b["shape"]["tag"] == abi.HULL)[0])
+    b["shape"]["pad"][i, 0] = nh - 1
+    with pytest.raises(ValueError):
+        compute.check_hull_ranges(b, nh)
+    b["shape"]["pad"][i, 0] = 0xFFFFFFFF
+    with pytest.raises(ValueError):
+        compute.check_hull_ranges(b, nh)
+    b["shape"]["pad"][i, 0] = nh - b["shape"]["pad"][i, 1]  # ends exactly at the pool end
+    compute.check_hull_ranges(b, nh)
+    with pytest.raises(ValueError):
+        compute.check_hull_ranges(b, nh - 1)
