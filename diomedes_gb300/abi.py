@@ -37,6 +37,7 @@ CKPT_HEADER = np.dtype([("magic", "S8"), ("version", "<u4"), ("precision", "<u4"
 PRIMAL_VARIANTS = 10  # DIO_PRIMAL_VARIANTS
 XFORM_POSE, XFORM_MAT4 = 0, 1  # DIO_XFORM_*
 DEBUG_EPA_NO_FIRST_WAIT = 1  # DIO_DEBUG_EPA_NO_FIRST_WAIT (DioConfig.debug_flags, tests only)
+SOLVE_AUTO, SOLVE_PER_PHASE = 0, 1  # DioSolveLaunch (DioConfig.batched_solver)
 
 SOLVER_JACOBI, SOLVER_COLORED = 0, 1
 PREC_F32, PREC_SPLIT, PREC_F64 = 0, 1, 2
@@ -112,7 +113,7 @@ class StepStats(ctypes.Structure):
                 ("steps", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64), ("primal_launches", _u32),
                 ("dual_launches", _u32), ("primal_ms", ctypes.c_double), ("dual_ms", ctypes.c_double),
                 ("broad_ms", ctypes.c_double), ("narrow_ms", ctypes.c_double), ("rows_ms", ctypes.c_double),
-                ("solve_ms", ctypes.c_double)]
+                ("solve_ms", ctypes.c_double), ("chunk_launches", _u32), ("pad", _u32), ("chunk_ms", ctypes.c_double)]
 
 
 # every symbol include/dio_cuda.h declares, with its argument types

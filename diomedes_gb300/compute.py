@@ -334,7 +334,8 @@ class World(Context):
         return {"pairs": s.pairs, "contacts": s.contacts, "colors": s.colors, "error_flags": s.error_flags,
                 "steps": s.steps, "kernel_launches": s.kernel_launches, "primal_launches": s.primal_launches,
                 "dual_launches": s.dual_launches, "primal_ms": s.primal_ms, "dual_ms": s.dual_ms,
-                "broad_ms": s.broad_ms, "narrow_ms": s.narrow_ms, "rows_ms": s.rows_ms, "solve_ms": s.solve_ms}
+                "broad_ms": s.broad_ms, "narrow_ms": s.narrow_ms, "rows_ms": s.rows_ms, "solve_ms": s.solve_ms,
+                "chunk_launches": s.chunk_launches, "chunk_ms": s.chunk_ms}
 
     def autotune(self, options, trial_steps=5, cache_path=None):
         """dio_autotune: pick the fastest launch shape / LBVH rebuild period

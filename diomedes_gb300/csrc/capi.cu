@@ -350,7 +350,8 @@ std::string tune_key(DioCtx* ctx, dio::EngineBase* e) {
            std::to_string(ns) + "|p" + std::to_string(ctx->cfg.precision) + "|s" + std::to_string(ctx->cfg.solver_mode);
 }
 
-bool cache_lookup(const char* path, const std::string& key, uint32_t* variant, uint32_t* period) {
+// cache lines: key, primal variant, LBVH rebuild period, solve launch, ms
+bool cache_lookup(const char* path, const std::string& key, uint32_t* variant, uint32_t* period, uint32_t* solve) {
     if (!path) return false;
     FILE* f = std::fopen(path, "r");
     if (!f) return false;
@@ -358,10 +359,12 @@ bool cache_lookup(const char* path, const std::string& key, uint32_t* variant, u
     bool found = false;
     while (std::fgets(line, sizeof line, f)) {
         char k[400];
-        unsigned v = 0, p = 0;
-        if (std::sscanf(line, "%399s %u %u", k, &v, &p) == 3 && key == k) {
+        unsigned v = 0, p = 0, b = 0;
+        double ms = 0.0;
+        if (std::sscanf(line, "%399s %u %u %u %lf", k, &v, &p, &b, &ms) == 5 && key == k) {
             *variant = v;
             *period = p;
+            *solve = b;
             found = true;  // the last entry wins
         }
     }
@@ -392,10 +395,11 @@ int dio_autotune(DioCtx* ctx, const DioAvbdOptions* options, uint32_t trial_step
     if (trial_steps == 0) trial_steps = 5;
     const std::string key = tune_key(ctx, e);
     DioConfig cfg = ctx->cfg;
-    uint32_t v = 0, p = 0;
-    if (cache_lookup(cache_path, key, &v, &p) && v < 10) {
+    uint32_t v = 0, p = 0, b = 0;
+    if (cache_lookup(cache_path, key, &v, &p, &b) && v < DIO_PRIMAL_VARIANTS && b <= DIO_SOLVE_PER_PHASE) {
         cfg.primal_variant = v;
         cfg.bvh_rebuild_period = p;
+        cfg.batched_solver = b;
         rc = dio_ctx_configure(ctx, &cfg);
         if (!rc && best) *best = ctx->cfg;
         return rc;
@@ -410,12 +414,13 @@ int dio_autotune(DioCtx* ctx, const DioAvbdOptions* options, uint32_t trial_step
         if ((r = time_steps(ctx, e, options, 2, &warm))) return r;  // captures the graphs
         return time_steps(ctx, e, options, trial_steps, ms);
     };
-    // 1) primal launch shape at the default rebuild period
+    // 1) the solve launch: one scene-chunk launch (where the world allows
+    // it) against the per-phase launches, at the default shape and period
     double best_ms = 1e300;
     DioConfig best_cfg = cfg;
-    for (uint32_t var = 0; var < DIO_PRIMAL_VARIANTS; ++var) {
+    for (uint32_t solve : {(uint32_t)DIO_SOLVE_AUTO, (uint32_t)DIO_SOLVE_PER_PHASE}) {
         DioConfig c = cfg;
-        c.primal_variant = var;
+        c.batched_solver = solve;
         double ms = 0.0;
         if ((rc = trial(c, &ms))) return rc;
         if (ms < best_ms) {
@@ -423,7 +428,21 @@ int dio_autotune(DioCtx* ctx, const DioAvbdOptions* options, uint32_t trial_step
             best_cfg = c;
         }
     }
-    // 2) LBVH rebuild period with that shape
+    // 2) the primal launch shape, when the per-phase launches won
+    if (best_cfg.batched_solver == DIO_SOLVE_PER_PHASE) {
+        const DioConfig base = best_cfg;
+        for (uint32_t var = 0; var < DIO_PRIMAL_VARIANTS; ++var) {
+            DioConfig c = base;
+            c.primal_variant = var;
+            double ms = 0.0;
+            if ((rc = trial(c, &ms))) return rc;
+            if (ms < best_ms) {
+                best_ms = ms;
+                best_cfg = c;
+            }
+        }
+    }
+    // 3) LBVH rebuild period with that solve
     const uint32_t periods[] = {1, 2, 4, 8, 16};
     DioConfig base = best_cfg;
     for (uint32_t per : periods) {
@@ -440,8 +459,8 @@ int dio_autotune(DioCtx* ctx, const DioAvbdOptions* options, uint32_t trial_step
     if ((rc = e->restore())) return fail(ctx, rc, e->err);
     if (cache_path) {
         if (FILE* f = std::fopen(cache_path, "a")) {
-            std::fprintf(f, "%s %u %u %.4f\n", key.c_str(), best_cfg.primal_variant, best_cfg.bvh_rebuild_period,
-                         best_ms / trial_steps);
+            std::fprintf(f, "%s %u %u %u %.4f\n", key.c_str(), best_cfg.primal_variant, best_cfg.bvh_rebuild_period,
+                         best_cfg.batched_solver, best_ms / trial_steps);
             std::fclose(f);
         }
     }

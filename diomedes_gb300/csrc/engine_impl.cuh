@@ -13,6 +13,7 @@
 #include "engine_base.h"
 #include "k_avbd.cuh"
 #include "k_broad.cuh"
+#include "k_chunk.cuh"
 #include "k_color.cuh"
 #include "k_lbvh.cuh"
 #include "k_narrow_kernels.cuh"
@@ -490,6 +491,7 @@ class Engine final : public EngineBase {
         DIO_TRY(alloc(&offsets2_, (size_t)N + 2));
         DIO_TRY(alloc(&scenes_, S));
         DIO_TRY(alloc(&chunks_, S));
+        DIO_TRY(alloc(&solve_chunks_, S));
         DIO_TRY(alloc(&chunk_n_, S));
         DIO_TRY(alloc(&chunk_ovf_, S));
         // pair scratch of the shared-memory trees: scratch_k_ slots per body
@@ -540,47 +542,60 @@ class Engine final : public EngineBase {
         const int tree_bytes = (int)scene_tree_bytes<R>(scene_tree_cap<R>());
         DIO_CK(cudaFuncSetAttribute(k_scene_tree<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, tree_bytes));
         DIO_CK(cudaFuncSetAttribute(k_scene_tree<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tree_bytes));
+        DIO_CK(cudaFuncSetAttribute(k_solve_chunks<P, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)chunk_smem_bytes<P>(solve_chunk_cap<P>())));
         return DIO_OK;
     }
     // largest scene, and the chunks of consecutive scenes (each of at most
     // scene_tree_cap bodies, packed up to that many) for k_scene_tree
-    int note_scene_sizes() {
-        const uint32_t cap = scene_tree_cap<R>();
-        scene_max_ = 0;
-        chunk_max_ = 0;
-        chunks_host_.clear();
-        uint32_t open_bodies = 0;
+    // Consecutive scenes packed into chunks of at most `cap` bodies (scenes
+    // larger than cap are left out), largest chunks first: CTAs start in
+    // chunk order, so the last wave holds the short ones.  Returns the
+    // bodies of the largest chunk.
+    uint32_t pack_chunks(uint32_t cap, std::vector<uint2>& out) const {
+        out.clear();
+        uint32_t open_bodies = 0, largest = 0;
         bool open = false;
         auto close = [&](uint32_t end) {
             if (!open) return;
-            chunks_host_.back().y = end;
-            chunk_max_ = std::max(chunk_max_, open_bodies);
+            out.back().y = end;
+            largest = std::max(largest, open_bodies);
             open = false;
         };
         for (uint32_t s = 0; s < (uint32_t)scenes_host_.size(); ++s) {
             const uint32_t sz = scenes_host_[s].body_hi - scenes_host_[s].body_lo;
-            scene_max_ = std::max(scene_max_, sz);
             if (sz > cap) {
                 close(s);
                 continue;
             }
             if (open && open_bodies + sz > cap) close(s);
             if (!open) {
-                chunks_host_.push_back(make_uint2(s, s));
+                out.push_back(make_uint2(s, s));
                 open_bodies = 0;
                 open = true;
             }
             open_bodies += sz;
         }
         close((uint32_t)scenes_host_.size());
-        // largest chunks first: CTAs start in chunk order, so the last wave
-        // holds the short ones
         auto bodies_of = [&](const uint2& c) { return scenes_host_[c.y - 1].body_hi - scenes_host_[c.x].body_lo; };
-        std::stable_sort(chunks_host_.begin(), chunks_host_.end(),
+        std::stable_sort(out.begin(), out.end(),
                          [&](const uint2& a, const uint2& b) { return bodies_of(a) > bodies_of(b); });
+        return largest;
+    }
+    // largest scene; the chunks of the broad phase's shared-memory trees
+    // (scene_tree_cap<R> bodies) and of the scene-chunk solve
+    // (solve_chunk_cap<P> bodies)
+    int note_scene_sizes() {
+        scene_max_ = 0;
+        for (const SceneDesc& sd : scenes_host_) scene_max_ = std::max(scene_max_, sd.body_hi - sd.body_lo);
+        chunk_max_ = pack_chunks(scene_tree_cap<R>(), chunks_host_);
+        pack_chunks(solve_chunk_cap<P>(), solve_chunks_host_);
         if (!chunks_host_.empty())
             DIO_CK(cudaMemcpyAsync(chunks_, chunks_host_.data(), chunks_host_.size() * sizeof(uint2),
                                    cudaMemcpyHostToDevice, stream_));
+        if (!solve_chunks_host_.empty())
+            DIO_CK(cudaMemcpyAsync(solve_chunks_, solve_chunks_host_.data(),
+                                   solve_chunks_host_.size() * sizeof(uint2), cudaMemcpyHostToDevice, stream_));
         return DIO_OK;
     }
 
@@ -872,6 +887,10 @@ class Engine final : public EngineBase {
         w_.n = n;
         DIO_CK(cudaMemsetAsync(ctr_, 0, sizeof(Counters), stream_));
         DIO_TRY(upload_joints(d->constraints, d->n_constraints, n));
+        // the scene-chunk solve needs every scene in a chunk and every joint
+        // inside one scene (a chunk's shared memory holds its own bodies only)
+        chunk_world_ = n && !solve_chunks_host_.empty() && scene_max_ <= solve_chunk_cap<P>() &&
+                       joints_within_scenes(d->constraints, d->n_constraints);
         n_prev_rows_ = 0;
         steps_ = 0;
         lag_primed_ = false;
@@ -1032,6 +1051,8 @@ class Engine final : public EngineBase {
         out->narrow_ms = phase_ms_[1];
         out->rows_ms = phase_ms_[2];
         out->solve_ms = phase_ms_[3];
+        out->chunk_launches = solve_chunk_n_;
+        out->chunk_ms = solve_chunk_ms_;
         return DIO_OK;
     }
 
@@ -1173,6 +1194,33 @@ class Engine final : public EngineBase {
         scenes_host_.assign(1, x);
         DIO_TRY(note_scene_sizes());
         DIO_CK(cudaStreamSynchronize(stream_));
+        return DIO_OK;
+    }
+    // every joint's two bodies in one scene of the uploaded world
+    bool joints_within_scenes(const DioConstraint* cons, uint32_t nj) const {
+        auto scene_of = [&](uint32_t b) -> int64_t {
+            auto it = std::upper_bound(scenes_host_.begin(), scenes_host_.end(), b,
+                                       [](uint32_t v, const SceneDesc& sd) { return v < sd.body_hi; });
+            if (it == scenes_host_.end() || b < it->body_lo) return -1;
+            return it - scenes_host_.begin();
+        };
+        for (uint32_t k = 0; k < nj; ++k) {
+            const int64_t sa = scene_of(cons[k].a);
+            if (sa < 0 || sa != scene_of(cons[k].b)) return false;
+        }
+        return true;
+    }
+    // the whole solve of a world step as one launch (k_solve_chunks)
+    bool use_chunk_solve() const {
+        return chunk_world_ && cfg_.batched_solver == DIO_SOLVE_AUTO && cfg_.solver_mode == DIO_SOLVER_JACOBI;
+    }
+    int solve_chunks(const SolveParams<R>& o) {
+        const uint32_t cap = solve_chunk_cap<P>();
+        cudaEvent_t e0 = span_begin();
+        DIO_CK(launch_k(pdl(), k_solve_chunks<P, R>, (int)solve_chunks_host_.size(), kChunkThreads,
+                        chunk_smem_bytes<P>(cap), stream_, w_, (const uint2*)solve_chunks_, scenes_, cap, o));
+        span_end(e0, 6);
+        ++launches_;
         return DIO_OK;
     }
     int upload_joints(const DioConstraint* cons, uint32_t nj, uint32_t n) {
@@ -1489,6 +1537,9 @@ class Engine final : public EngineBase {
             } else if (s.kind == 1) {
                 dual_ms_ += ms;
                 ++dual_n_;
+            } else if (s.kind == 6) {
+                solve_chunk_ms_ += ms;
+                ++solve_chunk_n_;
             } else {
                 phase_ms_[s.kind - 2] += ms;
             }
@@ -1743,8 +1794,8 @@ class Engine final : public EngineBase {
    public:
     int reset_timers() override {
         collect_spans();
-        primal_ms_ = dual_ms_ = 0.0;
-        primal_n_ = dual_n_ = 0;
+        primal_ms_ = dual_ms_ = solve_chunk_ms_ = 0.0;
+        primal_n_ = dual_n_ = solve_chunk_n_ = 0;
         for (double& x : phase_ms_) x = 0.0;
         launches_ = 0;
         return DIO_OK;
@@ -1790,7 +1841,10 @@ class Engine final : public EngineBase {
         span_end(e, 4);
         SolveParams<R> so = solve_params(opt.dt, opt.gravity, opt.alpha, opt.beta_lin, opt.penalty_max, opt.iterations);
         e = span_begin();
-        DIO_TRY(solve(so, n, 0, &ctr_->rows));
+        if (use_chunk_solve())
+            DIO_TRY(solve_chunks(so));
+        else
+            DIO_TRY(solve(so, n, 0, &ctr_->rows));
         span_end(e, 5);
         return DIO_OK;
     }
@@ -2043,9 +2097,12 @@ class Engine final : public EngineBase {
     uint32_t *counts_ = nullptr, *offsets_ = nullptr, *counts2_ = nullptr, *offsets2_ = nullptr;
     SceneDesc* scenes_ = nullptr;
     std::vector<SceneDesc> scenes_host_;
+    bool chunk_world_ = false;  // every scene in a solve chunk, joints inside scenes
     uint32_t scene_max_ = 0;  // bodies in the largest scene
     uint32_t chunk_max_ = 0;  // bodies in the largest scene chunk
     std::vector<uint2> chunks_host_;
+    std::vector<uint2> solve_chunks_host_;  // chunks of the scene-chunk solve
+    uint2* solve_chunks_ = nullptr;
     uint2* chunks_ = nullptr;
     Slot<R>* slots_[2] = {nullptr, nullptr};
     // inside step_body_dev: its scratch zeroing is done by k_roll_counters and
@@ -2092,7 +2149,8 @@ class Engine final : public EngineBase {
     uint32_t *lb_pb_ = nullptr, *lb_long_ = nullptr, *lb_long_count_ = nullptr;
     double primal_ms_ = 0.0, dual_ms_ = 0.0;
     double phase_ms_[4] = {0.0, 0.0, 0.0, 0.0};  // broad, narrow, rows, solve
-    uint32_t primal_n_ = 0, dual_n_ = 0;
+    uint32_t primal_n_ = 0, dual_n_ = 0, solve_chunk_n_ = 0;
+    double solve_chunk_ms_ = 0.0;
     uint64_t launches_ = 0;
 };
 

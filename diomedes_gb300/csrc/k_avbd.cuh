@@ -177,6 +177,7 @@ __global__ void __launch_bounds__(256) k_init(DevWorld<P, R> w, uint32_t lo, uin
 // Where the primal reads another body's snapshot / step-start pose: global
 // memory, or a shared-memory tile of consecutive bodies with a global
 // fallback.  Both return the same values.
+// `store` writes a body's new pose (the primal's output buffer).
 template <class P, class R>
 struct GlobalFetch {
     const DevWorld<P, R>& w;
@@ -185,6 +186,10 @@ struct GlobalFetch {
     __device__ __forceinline__ A4<P> rot(uint32_t j) const { return w.rot[rd][j]; }
     __device__ __forceinline__ A4<P> ipos(uint32_t j) const { return w.init_pos[j]; }
     __device__ __forceinline__ A4<P> irot(uint32_t j) const { return w.init_rot[j]; }
+    __device__ __forceinline__ void store(uint32_t i, A4<P> p, A4<P> q) const {
+        w.pos[1 - rd][i] = p;
+        w.rot[1 - rd][i] = q;
+    }
 };
 
 template <class P, class R, int T>
@@ -200,6 +205,32 @@ struct TileFetch {
     __device__ __forceinline__ A4<P> rot(uint32_t j) const { return j - lo < (uint32_t)T ? sq[j - lo] : w.rot[rd][j]; }
     __device__ __forceinline__ A4<P> ipos(uint32_t j) const { return j - lo < (uint32_t)T ? si[j - lo] : w.init_pos[j]; }
     __device__ __forceinline__ A4<P> irot(uint32_t j) const { return j - lo < (uint32_t)T ? sr[j - lo] : w.init_rot[j]; }
+    __device__ __forceinline__ void store(uint32_t i, A4<P> p, A4<P> q) const {
+        w.pos[1 - rd][i] = p;
+        w.rot[1 - rd][i] = q;
+    }
+};
+
+// Poses of one scene chunk held in shared memory: bodies [lo, lo + count)
+// at index j - lo.  Every body a chunk's rows and joints touch lies in the
+// chunk (rows and joints never cross scenes).
+template <class P>
+struct SmemFetch {
+    const A4<P>* sp;  // snapshot (read) buffer
+    const A4<P>* sq;
+    const A4<P>* si;  // step-start pose
+    const A4<P>* sr;
+    A4<P>* wp;        // the primal's output buffer
+    A4<P>* wq;
+    uint32_t lo;
+    __device__ __forceinline__ A4<P> pos(uint32_t j) const { return sp[j - lo]; }
+    __device__ __forceinline__ A4<P> rot(uint32_t j) const { return sq[j - lo]; }
+    __device__ __forceinline__ A4<P> ipos(uint32_t j) const { return si[j - lo]; }
+    __device__ __forceinline__ A4<P> irot(uint32_t j) const { return sr[j - lo]; }
+    __device__ __forceinline__ void store(uint32_t i, A4<P> p, A4<P> q) const {
+        wp[i - lo] = p;
+        wq[i - lo] = q;
+    }
 };
 
 // Clamped row forces shared by avbd_primal and avbd_dual (avbd/src/lib.rs:
@@ -377,10 +408,10 @@ __device__ __forceinline__ void primal_jview_f(const JView& jv, const F& fetch, 
     primal_jview_p<P, R>(jv, fetch.pos(jv.other), fetch.rot(jv.other), sp, sq, sqr, B);
 }
 
-// avbd_primal for one body: reads buffer rd (through `fetch`), writes wr.
-// [k0, k1) is the body's joint-view range.
+// avbd_primal for one body: reads the snapshot through `fetch` and stores
+// the new pose through it.  [k0, k1) is the body's joint-view range.
 template <class P, class R, class F>
-__device__ __forceinline__ void primal_body_f(const DevWorld<P, R>& w, uint32_t i, uint32_t k0, uint32_t k1, int wr,
+__device__ __forceinline__ void primal_body_f(const DevWorld<P, R>& w, uint32_t i, uint32_t k0, uint32_t k1,
                                               const SolveParams<R>& o, const F& fetch) {
     const A4<R> inv = w.inv[i];
     if (inv.w == R(0)) return;
@@ -432,18 +463,17 @@ __device__ __forceinline__ void primal_body_f(const DevWorld<P, R>& w, uint32_t 
     }
     R dx[6];
     solve6(B, dx);
-    w.pos[wr][i] = pack(add(sp, cast3<P>(V3<R>{dx[0], dx[1], dx[2]})));
+    const A4<P> np = pack(add(sp, cast3<P>(V3<R>{dx[0], dx[1], dx[2]})));
     if constexpr (std::is_same<P, R>::value)
-        w.rot[wr][i] = packq(quat_step(sq, V3<P>{dx[3], dx[4], dx[5]}));
+        fetch.store(i, np, packq(quat_step(sq, V3<P>{dx[3], dx[4], dx[5]})));
     else
-        w.rot[wr][i] = packq(quat_step_split<P, R>(sq, V3<R>{dx[3], dx[4], dx[5]}));
+        fetch.store(i, np, packq(quat_step_split<P, R>(sq, V3<R>{dx[3], dx[4], dx[5]})));
 }
 
 template <class P, class R>
-__device__ __forceinline__ void primal_body(const DevWorld<P, R>& w, uint32_t i, int rd, int wr,
-                                            const SolveParams<R>& o) {
+__device__ __forceinline__ void primal_body(const DevWorld<P, R>& w, uint32_t i, int rd, const SolveParams<R>& o) {
     const uint32_t k0 = w.n_joints ? w.joint_off[i] : 0u, k1 = w.n_joints ? w.joint_off[i + 1] : 0u;
-    primal_body_f(w, i, k0, k1, wr, o, GlobalFetch<P, R>{w, rd});
+    primal_body_f(w, i, k0, k1, o, GlobalFetch<P, R>{w, rd});
 }
 
 // Tile variant: the CTA's T consecutive bodies stage their snapshot and
@@ -465,7 +495,7 @@ __global__ void __launch_bounds__(T, MINB) k_primal_tile(DevWorld<P, R> w, int r
     __syncthreads();
     if (i < w.n) {
         const uint32_t k0 = w.n_joints ? w.joint_off[i] : 0u, k1 = w.n_joints ? w.joint_off[i + 1] : 0u;
-        primal_body_f(w, i, k0, k1, wr, o, TileFetch<P, R, T>{w, rd, lo, s_pos, s_rot, s_ipos, s_irot});
+        primal_body_f(w, i, k0, k1, o, TileFetch<P, R, T>{w, rd, lo, s_pos, s_rot, s_ipos, s_irot});
     }
 }
 
@@ -477,7 +507,7 @@ template <class P, class R, int BLOCK, int MINB>
 __global__ void __launch_bounds__(BLOCK, MINB) k_primal(DevWorld<P, R> w, int rd, int wr, SolveParams<R> o) {
     pdl_enter();
     for (uint32_t t = blockIdx.x * BLOCK + threadIdx.x; t < w.n_dyn; t += gridDim.x * BLOCK)
-        primal_body(w, w.dyn_list[t], rd, wr, o);
+        primal_body(w, w.dyn_list[t], rd, o);
 }
 
 // variants: 0-5 k_primal over the dynamic-body list with {threads per CTA,
@@ -525,29 +555,47 @@ inline void launch_primal(int variant, bool pdl, const DevWorld<P, R>& w, int rd
     }
 }
 
+// Buffer 0 read and written in place (the coloured Gauss-Seidel sweeps).
+template <class P, class R>
+struct InPlaceFetch {
+    const DevWorld<P, R>& w;
+    __device__ __forceinline__ A4<P> pos(uint32_t j) const { return w.pos[0][j]; }
+    __device__ __forceinline__ A4<P> rot(uint32_t j) const { return w.rot[0][j]; }
+    __device__ __forceinline__ A4<P> ipos(uint32_t j) const { return w.init_pos[j]; }
+    __device__ __forceinline__ A4<P> irot(uint32_t j) const { return w.init_rot[j]; }
+    __device__ __forceinline__ void store(uint32_t i, A4<P> p, A4<P> q) const {
+        w.pos[0][i] = p;
+        w.rot[0][i] = q;
+    }
+};
+
 // Coloured Gauss-Seidel sweep: bodies color_order[c0 .. c1) in place.
 template <class P, class R>
 __global__ void __launch_bounds__(128) k_primal_color(DevWorld<P, R> w, uint32_t c0, uint32_t c1, SolveParams<R> o) {
-    for (uint32_t t = c0 + blockIdx.x * blockDim.x + threadIdx.x; t < c1; t += gridDim.x * blockDim.x)
-        primal_body(w, w.color_order[t], 0, 0, o);
+    for (uint32_t t = c0 + blockIdx.x * blockDim.x + threadIdx.x; t < c1; t += gridDim.x * blockDim.x) {
+        const uint32_t i = w.color_order[t];
+        const uint32_t k0 = w.n_joints ? w.joint_off[i] : 0u, k1 = w.n_joints ? w.joint_off[i + 1] : 0u;
+        primal_body_f(w, i, k0, k1, o, InPlaceFetch<P, R>{w});
+    }
 }
 
-// avbd_dual, avbd/src/lib.rs:565-663, for one row; `rd` holds the new state.
-template <class P, class R>
-__device__ __forceinline__ void dual_row(const DevWorld<P, R>& w, uint32_t c, int rd, const SolveParams<R>& o) {
+// avbd_dual, avbd/src/lib.rs:565-663, for one row; `fetch` reads the new state.
+template <class P, class R, class F>
+__device__ __forceinline__ void dual_row_f(const DevWorld<P, R>& w, uint32_t c, const F& fetch,
+                                           const SolveParams<R>& o) {
     const uint2 ab = w.ab[c];
     const RowStatic<R> rs = w.rs[c];
     RowDual<P, R> du = w.rd[c];
-    A4<P> pa4 = w.pos[rd][ab.x];
-    A4<P> qa4 = w.rot[rd][ab.x];
-    V3<R> dal = cast3<R>(sub(xyz(pa4), xyz(w.init_pos[ab.x])));
-    V3<R> daa = ang_diff(castq<R>(quat(qa4)), castq<R>(quat(w.init_rot[ab.x])));
+    A4<P> pa4 = fetch.pos(ab.x);
+    A4<P> qa4 = fetch.rot(ab.x);
+    V3<R> dal = cast3<R>(sub(xyz(pa4), xyz(fetch.ipos(ab.x))));
+    V3<R> daa = ang_diff(castq<R>(quat(qa4)), castq<R>(quat(fetch.irot(ab.x))));
     V3<R> dbl{R(0), R(0), R(0)}, dba{R(0), R(0), R(0)}, rbw{R(0), R(0), R(0)};
     if (ab.y != kContainer) {
-        A4<P> pb4 = w.pos[rd][ab.y];
-        A4<P> qb4 = w.rot[rd][ab.y];
-        dbl = cast3<R>(sub(xyz(pb4), xyz(w.init_pos[ab.y])));
-        dba = ang_diff(castq<R>(quat(qb4)), castq<R>(quat(w.init_rot[ab.y])));
+        A4<P> pb4 = fetch.pos(ab.y);
+        A4<P> qb4 = fetch.rot(ab.y);
+        dbl = cast3<R>(sub(xyz(pb4), xyz(fetch.ipos(ab.y))));
+        dba = ang_diff(castq<R>(quat(qb4)), castq<R>(quat(fetch.irot(ab.y))));
         rbw = rotate(castq<R>(quat(qb4)), xyz(rs.rb));
     }
     V3<R> raw = rotate(castq<R>(quat(qa4)), xyz(rs.ra));
@@ -569,6 +617,10 @@ __device__ __forceinline__ void dual_row(const DevWorld<P, R>& w, uint32_t c, in
     }
     w.rd[c] = du;
 }
+template <class P, class R>
+__device__ __forceinline__ void dual_row(const DevWorld<P, R>& w, uint32_t c, int rd, const SolveParams<R>& o) {
+    dual_row_f(w, c, GlobalFetch<P, R>{w, rd}, o);
+}
 
 template <class P, class R>
 __global__ void __launch_bounds__(256) k_dual(DevWorld<P, R> w, uint32_t lo, uint32_t hi, const uint32_t* dyn_hi,
@@ -581,22 +633,23 @@ __global__ void __launch_bounds__(256) k_dual(DevWorld<P, R> w, uint32_t lo, uin
 
 // avbd_recover, avbd/src/lib.rs:667-699; also leaves the final pose in
 // buffer 0 when it lives in buffer 1.
-template <class P, class R>
-__device__ __forceinline__ void recover_body(const DevWorld<P, R>& w, uint32_t i, int rb, const SolveParams<R>& o) {
+template <class P, class R, class F>
+__device__ __forceinline__ void recover_body_f(const DevWorld<P, R>& w, uint32_t i, const F& fetch,
+                                               const SolveParams<R>& o) {
     if (w.inv[i].w == R(0)) return;
-    A4<P> p4 = w.pos[rb][i];
-    A4<P> q4 = w.rot[rb][i];
+    A4<P> p4 = fetch.pos(i);
+    A4<P> q4 = fetch.rot(i);
     P dt = P(o.dt);
     A4<P> v = w.vel[i];
     w.prev_vel[i] = v;
-    const Q4<P> rel = qmul(quat(q4), conj(quat(w.init_rot[i])));
+    const Q4<P> rel = qmul(quat(q4), conj(quat(fetch.irot(i))));
     V3<P> nv, na;
     if constexpr (std::is_same<P, R>::value) {
-        nv = divs(sub(xyz(p4), xyz(w.init_pos[i])), dt);
+        nv = divs(sub(xyz(p4), xyz(fetch.ipos(i))), dt);
         na = divs(V3<P>{P(2) * rel.x, P(2) * rel.y, P(2) * rel.z}, dt);
     } else {  // split mode: one division, then products (within an ulp of P)
         const P inv_dt = P(1) / dt;
-        nv = scale(sub(xyz(p4), xyz(w.init_pos[i])), inv_dt);
+        nv = scale(sub(xyz(p4), xyz(fetch.ipos(i))), inv_dt);
         na = scale(V3<P>{P(2) * rel.x, P(2) * rel.y, P(2) * rel.z}, inv_dt);
     }
     w.vel[i] = pack(nv);
@@ -606,6 +659,10 @@ __device__ __forceinline__ void recover_body(const DevWorld<P, R>& w, uint32_t i
     if (w.ctr && !(finite_(nv.x) && finite_(nv.y) && finite_(nv.z) && finite_(na.x) && finite_(na.y) &&
                    finite_(na.z) && finite_(q4.w)))
         atomicOr(&w.ctr->error_flags, kErrNonFinite);
+}
+template <class P, class R>
+__device__ __forceinline__ void recover_body(const DevWorld<P, R>& w, uint32_t i, int rb, const SolveParams<R>& o) {
+    recover_body_f(w, i, GlobalFetch<P, R>{w, rb}, o);
 }
 
 template <class P, class R>

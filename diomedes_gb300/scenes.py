@@ -68,6 +68,31 @@ class Scene:
             starts.append(lo)
         return out, starts
 
+    def select(self, indices):
+        """The scenes `indices` (in that order) as one packed Scene: bodies,
+        containers and joints of each, joints rebased (hull vertices shared)."""
+        off = np.array([0, self.n], np.int64) if self.scene_offsets is None else self.scene_offsets.astype(np.int64)
+        idx = [int(i) for i in indices]
+        c = self.constraints
+        cs = np.searchsorted(off, c["a"].astype(np.int64), side="right") - 1 if len(c) else np.zeros(0, np.int64)
+        bodies, states, cons, offs, conts = [], [], [], [0], []
+        for s in idx:
+            lo, hi = int(off[s]), int(off[s + 1])
+            bodies.append(self.bodies[lo:hi])
+            states.append(self.state[lo:hi])
+            j = c[cs == s].copy()
+            j["a"] = (j["a"].astype(np.int64) - lo + offs[-1]).astype(j["a"].dtype)
+            j["b"] = (j["b"].astype(np.int64) - lo + offs[-1]).astype(j["b"].dtype)
+            cons.append(j)
+            offs.append(offs[-1] + hi - lo)
+            if self.containers is not None:
+                conts.append(self.containers[s] if self.scene_offsets is not None else self.containers[0])
+        return Scene(f"{self.name}[{len(idx)} scenes]", np.concatenate(bodies) if bodies else self.bodies[:0].copy(),
+                     np.concatenate(states) if states else self.state[:0].copy(),
+                     constraints=np.concatenate(cons) if cons else c[:0].copy(),
+                     scene_offsets=np.array(offs, np.uint32), containers=conts if self.containers is not None else None,
+                     hull_vertices=self.hull_vertices, options=self.options, steps=self.steps)
+
     def upload_kwargs(self):
         return dict(constraints=self.constraints, scene_offsets=self.scene_offsets, containers=self.containers,
                     hull_vertices=self.hull_vertices, positions_f64=self.positions_f64)

@@ -218,7 +218,16 @@ typedef struct DioConfig {
                                    (launch shape, body tiles; every variant
                                    computes the same bits; autotuned)     */
     uint32_t block_size;        /* reserved (0)                           */
-    uint32_t batched_solver;    /* 1: one CTA-per-scene persistent solve  */
+    uint32_t batched_solver;    /* DioSolveLaunch: DIO_SOLVE_AUTO (0) runs
+                                   a world step's whole solve (init, the
+                                   iterations, recover) as one launch, a
+                                   CTA per chunk of whole scenes with the
+                                   poses in shared memory, when every
+                                   scene fits a chunk (2048 bodies, 1024
+                                   with FP64 poses) and no joint crosses
+                                   scenes; DIO_SOLVE_PER_PHASE (1) always
+                                   launches init / primal / dual / recover
+                                   kernels.  Both give identical results. */
     uint32_t profile;           /* time primal / dual launches with events */
     uint32_t broad_phase;       /* 0: LBVH (default), 1: dense sweep        */
     uint32_t bvh_rebuild_period; /* LBVH topology rebuilt every N steps and
@@ -238,6 +247,7 @@ typedef struct DioConfig {
                                    lets the copies land)                  */
 } DioConfig;
 #define DIO_DEBUG_EPA_NO_FIRST_WAIT 1u
+typedef enum DioSolveLaunch { DIO_SOLVE_AUTO = 0, DIO_SOLVE_PER_PHASE = 1 } DioSolveLaunch;
 
 /* World description for the fused device-resident step (extension of the
  * demos' per-frame loop, demos/avbd_box/src/main.rs:189-273). */
@@ -271,6 +281,9 @@ typedef struct DioStepStats {
     double narrow_ms;         /* summed narrow-phase time                  */
     double rows_ms;           /* summed row build + warm start + CSR time  */
     double solve_ms;          /* summed init .. recover time               */
+    uint32_t chunk_launches;  /* scene-chunk solve launches timed          */
+    uint32_t pad;
+    double chunk_ms;          /* summed scene-chunk solve kernel time      */
 } DioStepStats;
 
 typedef struct DioCtx DioCtx;
@@ -453,8 +466,10 @@ int dio_world_checkpoint(DioCtx* ctx, void* buffer, size_t capacity, size_t* siz
  * rows restored, so stepping continues bit for bit as the checkpointed world
  * would have.  A damaged or foreign image returns DIO_ERR_INVALID. */
 int dio_world_resume(DioCtx* ctx, const void* buffer, size_t size);
-/* Autotuner (extension): times the primal launch-shape variants and the
- * LBVH rebuild period on the uploaded world (trial_steps timed steps per
+/* Autotuner (extension): times the solve launch (one scene-chunk launch
+ * against init / primal / dual / recover per phase), the primal launch-shape
+ * variants (when the per-phase launches win) and the LBVH rebuild period on
+ * the uploaded world (trial_steps timed steps per
  * candidate, starting from a device snapshot that is restored afterwards,
  * so the world's state is unchanged), applies the fastest configuration and
  * returns it in `best`.  With `cache_path` set, a tuned configuration for

@@ -262,23 +262,44 @@ inline void broad_dense(const std::vector<V3<R>>& mn, const std::vector<V3<R>>& 
             if (overlap(mn[i], mx[i], mn[j], mx[j])) out.push_back({i, j});
 }
 
-// Same pair set by sort-and-sweep on x (a faster CPU broad phase used by
-// the CPU baseline); the closed-interval test is identical, so the set is
-// identical to broad_dense, and sorting restores the canonical order.
+// Same pair set by sort-and-sweep (a faster CPU broad phase used by the CPU
+// baseline) along the axis on which the scene's boxes spread widest (a wall
+// standing in the y-z plane would make a sweep on x quadratic); the
+// closed-interval test is identical, so the set is identical to broad_dense
+// for any axis, and sorting restores the canonical order.
+template <class R>
+inline R axis_of(const V3<R>& v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
 template <class R>
 inline void broad_sap(const std::vector<V3<R>>& mn, const std::vector<V3<R>>& mx, uint32_t lo,
                       uint32_t hi, std::vector<std::pair<uint32_t, uint32_t>>& out) {
+    if (hi <= lo) return;
+    int ax = 0;
+    R best = R(-1);
+    for (int k = 0; k < 3; ++k) {
+        R a = axis_of(mn[lo], k), b = a;
+        for (uint32_t i = lo + 1; i < hi; ++i) {
+            const R v = axis_of(mn[i], k);
+            a = v < a ? v : a;
+            b = v > b ? v : b;
+        }
+        if (b - a > best) {
+            best = b - a;
+            ax = k;
+        }
+    }
     std::vector<uint32_t> order;
     for (uint32_t i = lo; i < hi; ++i) order.push_back(i);
     std::sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
-        return mn[a].x < mn[b].x || (mn[a].x == mn[b].x && a < b);
+        const R ka = axis_of(mn[a], ax), kb = axis_of(mn[b], ax);
+        return ka < kb || (ka == kb && a < b);
     });
     size_t start = out.size();
     for (size_t s = 0; s < order.size(); ++s) {
         uint32_t i = order[s];
+        const R end = axis_of(mx[i], ax);
         for (size_t t = s + 1; t < order.size(); ++t) {
             uint32_t j = order[t];
-            if (!(mn[j].x <= mx[i].x)) break;
+            if (!(axis_of(mn[j], ax) <= end)) break;
             if (overlap(mn[i], mx[i], mn[j], mx[j])) out.push_back({std::min(i, j), std::max(i, j)});
         }
     }

@@ -123,14 +123,19 @@ def _world(sc, **cfg):
     return w
 
 
-@pytest.mark.parametrize("steps,use_graph", [(1, 1), (60, 1), (60, 0)])
-def test_world_steps_match_oracle(steps, use_graph):
+@pytest.mark.parametrize("steps,use_graph,batched_solver", [(1, 1, abi.SOLVE_AUTO), (60, 1, abi.SOLVE_AUTO),
+                                                            (60, 0, abi.SOLVE_AUTO), (1, 1, abi.SOLVE_PER_PHASE),
+                                                            (60, 1, abi.SOLVE_PER_PHASE)])
+def test_world_steps_match_oracle(steps, use_graph, batched_solver):
+    """SOLVE_AUTO runs each step's solve as one scene-chunk launch (every
+    scene here fits a chunk), SOLVE_PER_PHASE as init / primal / dual /
+    recover launches: both equal the oracle bit for bit."""
     for sc in small_scenes():
         ow = O.World(sc)
         ow.step(sc.options, steps)
         rb, rs = ow.download()
         rc = ow.contacts()
-        with _world(sc, use_graph=use_graph) as w:
+        with _world(sc, use_graph=use_graph, batched_solver=batched_solver) as w:
             for _ in range(steps):  # one dio_step per step: graph replay per call
                 w.step(sc.options, 1)
             gb, gs = w.download()
