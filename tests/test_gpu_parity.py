@@ -585,16 +585,25 @@ def test_scene_tree_capacity_boundaries_match_oracle():
 
 @pytest.mark.parametrize("use_graph", [0, 1])
 def test_profiled_world_times_every_primal_launch(use_graph):
+    """With event timers on, every primal launch of the per-phase solve is
+    timed, and every scene-chunk solve launch of the one-launch solve."""
     sc = scenes.box_demo()
-    with _world(sc, use_graph=use_graph, profile=1) as w:
+    with _world(sc, use_graph=use_graph, profile=1, batched_solver=abi.SOLVE_PER_PHASE) as w:
         w.step(sc.options, 3)
         w.reset_timers()
         w.step(sc.options, 4)
         st = w.stats()
     iters = sc.options.iterations
-    assert st["primal_launches"] == 4 * iters
+    assert st["primal_launches"] == 4 * iters and st["chunk_launches"] == 0
     assert st["primal_ms"] > 0 and st["solve_ms"] >= st["primal_ms"]
     assert st["kernel_launches"] > 4 * 2 * iters
+    with _world(sc, use_graph=use_graph, profile=1) as w:
+        w.step(sc.options, 3)
+        w.reset_timers()
+        w.step(sc.options, 4)
+        st = w.stats()
+    assert st["chunk_launches"] == 4 and st["primal_launches"] == 0
+    assert st["chunk_ms"] > 0 and st["solve_ms"] >= st["chunk_ms"]
 
 
 def test_nonfinite_state_is_reported():
