@@ -170,6 +170,9 @@ int dio_ctx_configure(DioCtx* ctx, const DioConfig* config) {
     if (config->precision > DIO_PREC_F64) return fail(ctx, DIO_ERR_INVALID, "unknown precision");
     if (config->contacts_per_pair != 4 && config->contacts_per_pair != 8)
         return fail(ctx, DIO_ERR_INVALID, "contacts_per_pair must be 4 or 8");
+    if (config->block_size != 0 && config->block_size != 640)
+        return fail(ctx, DIO_ERR_INVALID, "block_size must be 0 (512 threads) or 640");
+    if (config->batched_solver > DIO_SOLVE_PER_PHASE) return fail(ctx, DIO_ERR_INVALID, "unknown solve launch");
     bool realloc = config->contacts_per_pair > ctx->cfg.contacts_per_pair;
     ctx->cfg = *config;
     if (realloc) {
@@ -350,8 +353,10 @@ std::string tune_key(DioCtx* ctx, dio::EngineBase* e) {
            std::to_string(ns) + "|p" + std::to_string(ctx->cfg.precision) + "|s" + std::to_string(ctx->cfg.solver_mode);
 }
 
-// cache lines: key, primal variant, LBVH rebuild period, solve launch, ms
-bool cache_lookup(const char* path, const std::string& key, uint32_t* variant, uint32_t* period, uint32_t* solve) {
+// cache lines: key, primal variant, LBVH rebuild period, solve launch,
+// chunk-solve CTA size, ms
+bool cache_lookup(const char* path, const std::string& key, uint32_t* variant, uint32_t* period, uint32_t* solve,
+                  uint32_t* block) {
     if (!path) return false;
     FILE* f = std::fopen(path, "r");
     if (!f) return false;
@@ -359,12 +364,13 @@ bool cache_lookup(const char* path, const std::string& key, uint32_t* variant, u
     bool found = false;
     while (std::fgets(line, sizeof line, f)) {
         char k[400];
-        unsigned v = 0, p = 0, b = 0;
+        unsigned v = 0, p = 0, b = 0, t = 0;
         double ms = 0.0;
-        if (std::sscanf(line, "%399s %u %u %u %lf", k, &v, &p, &b, &ms) == 5 && key == k) {
+        if (std::sscanf(line, "%399s %u %u %u %u %lf", k, &v, &p, &b, &t, &ms) == 6 && key == k) {
             *variant = v;
             *period = p;
             *solve = b;
+            *block = t;
             found = true;  // the last entry wins
         }
     }
@@ -395,11 +401,12 @@ int dio_autotune(DioCtx* ctx, const DioAvbdOptions* options, uint32_t trial_step
     if (trial_steps == 0) trial_steps = 5;
     const std::string key = tune_key(ctx, e);
     DioConfig cfg = ctx->cfg;
-    uint32_t v = 0, p = 0, b = 0;
-    if (cache_lookup(cache_path, key, &v, &p, &b) && v < DIO_PRIMAL_VARIANTS && b <= DIO_SOLVE_PER_PHASE) {
+    uint32_t v = 0, p = 0, b = 0, t = 0;
+    if (cache_lookup(cache_path, key, &v, &p, &b, &t) && v < DIO_PRIMAL_VARIANTS && b <= DIO_SOLVE_PER_PHASE) {
         cfg.primal_variant = v;
         cfg.bvh_rebuild_period = p;
         cfg.batched_solver = b;
+        cfg.block_size = t;
         rc = dio_ctx_configure(ctx, &cfg);
         if (!rc && best) *best = ctx->cfg;
         return rc;
@@ -428,8 +435,18 @@ int dio_autotune(DioCtx* ctx, const DioAvbdOptions* options, uint32_t trial_step
             best_cfg = c;
         }
     }
-    // 2) the primal launch shape, when the per-phase launches won
-    if (best_cfg.batched_solver == DIO_SOLVE_PER_PHASE) {
+    // 2) the scene-chunk solve's CTA size when it won, else the primal
+    // launch shape
+    if (best_cfg.batched_solver == DIO_SOLVE_AUTO) {
+        DioConfig c = best_cfg;
+        c.block_size = 640;
+        double ms = 0.0;
+        if ((rc = trial(c, &ms))) return rc;
+        if (ms < best_ms) {
+            best_ms = ms;
+            best_cfg = c;
+        }
+    } else {
         const DioConfig base = best_cfg;
         for (uint32_t var = 0; var < DIO_PRIMAL_VARIANTS; ++var) {
             DioConfig c = base;
@@ -459,8 +476,9 @@ int dio_autotune(DioCtx* ctx, const DioAvbdOptions* options, uint32_t trial_step
     if ((rc = e->restore())) return fail(ctx, rc, e->err);
     if (cache_path) {
         if (FILE* f = std::fopen(cache_path, "a")) {
-            std::fprintf(f, "%s %u %u %u %.4f\n", key.c_str(), best_cfg.primal_variant, best_cfg.bvh_rebuild_period,
-                         best_cfg.batched_solver, best_ms / trial_steps);
+            std::fprintf(f, "%s %u %u %u %u %.4f\n", key.c_str(), best_cfg.primal_variant,
+                         best_cfg.bvh_rebuild_period, best_cfg.batched_solver, best_cfg.block_size,
+                         best_ms / trial_steps);
             std::fclose(f);
         }
     }

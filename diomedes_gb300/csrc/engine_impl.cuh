@@ -320,8 +320,11 @@ static __global__ void k_dyn_fill(const uint32_t* flags, const uint32_t* pos, ui
 // incidences (three rows each) first, then distance joints, then the shape.
 // Bodies with one signature run the same code path, so sorting the list by
 // it keeps warps convergent; the Jacobi primal does not depend on the order.
+// With `scene_chunk` set the key leads with the body's solve chunk, so each
+// chunk's dynamic bodies form one signature-ordered run of the list.
 template <class P, class R>
-__global__ void k_dyn_keys(DevWorld<P, R> w, const uint32_t* list, uint32_t nd, uint32_t* keys) {
+__global__ void k_dyn_keys(DevWorld<P, R> w, const uint32_t* list, uint32_t nd, const uint32_t* scene_chunk,
+                           uint32_t* keys) {
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nd; t += gridDim.x * blockDim.x) {
         const uint32_t i = list[t];
         uint32_t nb = 0, nl = 0;
@@ -335,7 +338,20 @@ __global__ void k_dyn_keys(DevWorld<P, R> w, const uint32_t* list, uint32_t nd, 
         nb = nb > 3u ? 3u : nb;
         nl = nl > 3u ? 3u : nl;
         const uint32_t tag = w.shape[i].tag > 7u ? 7u : w.shape[i].tag;
-        keys[t] = ((3u - nb) << 5) | ((3u - nl) << 3) | tag;
+        const uint32_t chunk = scene_chunk ? scene_chunk[w.scene[i]] : 0u;
+        keys[t] = (chunk << 7) | ((3u - nb) << 5) | ((3u - nl) << 3) | tag;
+    }
+}
+
+// [first, last) of each solve chunk's run in the chunk-ordered dynamic-body
+// list (runs start zeroed: a chunk without dynamic bodies keeps (0, 0))
+template <class P, class R>
+__global__ void k_chunk_dyn_runs(DevWorld<P, R> w, const uint32_t* list, uint32_t nd, const uint32_t* scene_chunk,
+                                 uint2* runs) {
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nd; t += gridDim.x * blockDim.x) {
+        const uint32_t c = scene_chunk[w.scene[list[t]]];
+        if (t == 0 || scene_chunk[w.scene[list[t - 1]]] != c) runs[c].x = t;
+        if (t + 1 == nd || scene_chunk[w.scene[list[t + 1]]] != c) runs[c].y = t + 1;
     }
 }
 
@@ -492,6 +508,8 @@ class Engine final : public EngineBase {
         DIO_TRY(alloc(&scenes_, S));
         DIO_TRY(alloc(&chunks_, S));
         DIO_TRY(alloc(&solve_chunks_, S));
+        DIO_TRY(alloc(&chunk_dyn_, S));
+        DIO_TRY(alloc(&scene_chunk_, S));
         DIO_TRY(alloc(&chunk_n_, S));
         DIO_TRY(alloc(&chunk_ovf_, S));
         // pair scratch of the shared-memory trees: scratch_k_ slots per body
@@ -542,7 +560,10 @@ class Engine final : public EngineBase {
         const int tree_bytes = (int)scene_tree_bytes<R>(scene_tree_cap<R>());
         DIO_CK(cudaFuncSetAttribute(k_scene_tree<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, tree_bytes));
         DIO_CK(cudaFuncSetAttribute(k_scene_tree<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tree_bytes));
-        DIO_CK(cudaFuncSetAttribute(k_solve_chunks<P, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        DIO_CK(cudaFuncSetAttribute(k_solve_chunks<P, R, kChunkThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)chunk_smem_bytes<P>(solve_chunk_cap<P>())));
+        DIO_CK(cudaFuncSetAttribute(k_solve_chunks<P, R, kChunkThreadsWide>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)chunk_smem_bytes<P>(solve_chunk_cap<P>())));
         return DIO_OK;
     }
@@ -582,6 +603,51 @@ class Engine final : public EngineBase {
                          [&](const uint2& a, const uint2& b) { return bodies_of(a) > bodies_of(b); });
         return largest;
     }
+    // Chunks of the scene-chunk solve.  It runs one CTA per chunk and one CTA
+    // per SM, so it takes about (waves) x (largest chunk): for k = 1, 2, ...
+    // waves the smallest chunk size that packs every scene into at most k x
+    // SMs chunks (greedy over consecutive scenes) is found by bisection, and
+    // the k with the smallest k x size wins.  Returns the largest chunk's
+    // bodies (0: some scene exceeds solve_chunk_cap).
+    uint32_t pack_solve_chunks() {
+        const uint32_t cap = solve_chunk_cap<P>();
+        uint32_t largest = 0;
+        for (const SceneDesc& sd : scenes_host_) largest = std::max(largest, sd.body_hi - sd.body_lo);
+        solve_chunks_host_.clear();
+        if (scenes_host_.empty() || largest == 0 || largest > cap) return 0;
+        auto count_at = [&](uint32_t m) {
+            uint64_t count = 0, open = 0;
+            for (const SceneDesc& sd : scenes_host_) {
+                const uint32_t sz = sd.body_hi - sd.body_lo;
+                if (!count || open + sz > m) {
+                    ++count;
+                    open = 0;
+                }
+                open += sz;
+            }
+            return count;
+        };
+        const uint64_t sm = (uint64_t)std::max(1, sms_);
+        uint64_t best_cost = ~0ull;
+        uint32_t best_m = cap;
+        for (uint64_t k = 1; k <= 64; ++k) {
+            if (count_at(cap) > k * sm) continue;
+            uint32_t lo = largest, hi = cap;  // the smallest size with at most k x SMs chunks
+            while (lo < hi) {
+                const uint32_t mid = lo + (hi - lo) / 2;
+                if (count_at(mid) <= k * sm)
+                    hi = mid;
+                else
+                    lo = mid + 1;
+            }
+            if (k * lo < best_cost) {
+                best_cost = k * lo;
+                best_m = lo;
+            }
+            if (lo == largest || k * sm >= scenes_host_.size()) break;  // more waves cannot help
+        }
+        return pack_chunks(best_m, solve_chunks_host_);
+    }
     // largest scene; the chunks of the broad phase's shared-memory trees
     // (scene_tree_cap<R> bodies) and of the scene-chunk solve
     // (solve_chunk_cap<P> bodies)
@@ -589,7 +655,16 @@ class Engine final : public EngineBase {
         scene_max_ = 0;
         for (const SceneDesc& sd : scenes_host_) scene_max_ = std::max(scene_max_, sd.body_hi - sd.body_lo);
         chunk_max_ = pack_chunks(scene_tree_cap<R>(), chunks_host_);
-        pack_chunks(solve_chunk_cap<P>(), solve_chunks_host_);
+        solve_chunk_max_ = pack_solve_chunks();
+        // solve chunk of every scene (when every scene has one)
+        chunked_scenes_ = !solve_chunks_host_.empty() && scene_max_ <= solve_chunk_cap<P>();
+        if (chunked_scenes_) {
+            std::vector<uint32_t> sch(scenes_host_.size(), 0u);
+            for (uint32_t c = 0; c < (uint32_t)solve_chunks_host_.size(); ++c)
+                for (uint32_t sc = solve_chunks_host_[c].x; sc < solve_chunks_host_[c].y; ++sc) sch[sc] = c;
+            DIO_CK(cudaMemcpyAsync(scene_chunk_, sch.data(), sch.size() * 4, cudaMemcpyHostToDevice, stream_));
+            DIO_CK(cudaStreamSynchronize(stream_));  // sch is a host temporary
+        }
         if (!chunks_host_.empty())
             DIO_CK(cudaMemcpyAsync(chunks_, chunks_host_.data(), chunks_host_.size() * sizeof(uint2),
                                    cudaMemcpyHostToDevice, stream_));
@@ -889,7 +964,7 @@ class Engine final : public EngineBase {
         DIO_TRY(upload_joints(d->constraints, d->n_constraints, n));
         // the scene-chunk solve needs every scene in a chunk and every joint
         // inside one scene (a chunk's shared memory holds its own bodies only)
-        chunk_world_ = n && !solve_chunks_host_.empty() && scene_max_ <= solve_chunk_cap<P>() &&
+        chunk_world_ = n && chunked_scenes_ &&
                        joints_within_scenes(d->constraints, d->n_constraints);
         n_prev_rows_ = 0;
         steps_ = 0;
@@ -1164,12 +1239,19 @@ class Engine final : public EngineBase {
     // index order is kept inside a signature
     int order_dyn_list() {
         const uint32_t nd = w_.n_dyn;
+        const uint32_t nc = (uint32_t)solve_chunks_host_.size();
+        if (nc) DIO_CK(cudaMemsetAsync(chunk_dyn_, 0, nc * sizeof(uint2), stream_));
         if (!nd) return DIO_OK;
-        k_dyn_keys<P, R><<<grid_for(nd, 256), 256, 0, stream_>>>(w_, dyn_list_, nd, counts2_);
+        // in chunk order when every scene has a solve chunk (the scene-chunk
+        // solve walks its chunk's run), else by signature alone
+        const uint32_t* sch = chunked_scenes_ ? scene_chunk_ : nullptr;
+        k_dyn_keys<P, R><<<grid_for(nd, 256), 256, 0, stream_>>>(w_, dyn_list_, nd, sch, counts2_);
         size_t tb = cub_bytes_;
-        DIO_CK(cub::DeviceRadixSort::SortPairs(cub_tmp_, tb, counts2_, offsets2_, dyn_list_, dyn_tmp_, (int)nd, 0, 8,
-                                               stream_));
+        const int end_bit = 7 + (sch ? (int)bits_for(nc) : 0);
+        DIO_CK(cub::DeviceRadixSort::SortPairs(cub_tmp_, tb, counts2_, offsets2_, dyn_list_, dyn_tmp_, (int)nd, 0,
+                                               end_bit, stream_));
         DIO_CK(cudaMemcpyAsync(dyn_list_, dyn_tmp_, (size_t)nd * 4, cudaMemcpyDeviceToDevice, stream_));
+        if (sch) k_chunk_dyn_runs<P, R><<<grid_for(nd, 256), 256, 0, stream_>>>(w_, dyn_list_, nd, sch, chunk_dyn_);
         return DIO_OK;
     }
     int single_scene(uint32_t n, const DioContainer* c) {
@@ -1215,10 +1297,16 @@ class Engine final : public EngineBase {
         return chunk_world_ && cfg_.batched_solver == DIO_SOLVE_AUTO && cfg_.solver_mode == DIO_SOLVER_JACOBI;
     }
     int solve_chunks(const SolveParams<R>& o) {
-        const uint32_t cap = solve_chunk_cap<P>();
+        const uint32_t cap = solve_chunk_max_;  // shared memory sized to the largest chunk
         cudaEvent_t e0 = span_begin();
-        DIO_CK(launch_k(pdl(), k_solve_chunks<P, R>, (int)solve_chunks_host_.size(), kChunkThreads,
-                        chunk_smem_bytes<P>(cap), stream_, w_, (const uint2*)solve_chunks_, scenes_, cap, o));
+        const int grid = (int)solve_chunks_host_.size();
+        const size_t smem = chunk_smem_bytes<P>(cap);
+        if (cfg_.block_size == (uint32_t)kChunkThreadsWide)
+            DIO_CK(launch_k(pdl(), k_solve_chunks<P, R, kChunkThreadsWide>, grid, kChunkThreadsWide, smem, stream_, w_,
+                            (const uint2*)solve_chunks_, (const uint2*)chunk_dyn_, scenes_, cap, o));
+        else
+            DIO_CK(launch_k(pdl(), k_solve_chunks<P, R, kChunkThreads>, grid, kChunkThreads, smem, stream_, w_,
+                            (const uint2*)solve_chunks_, (const uint2*)chunk_dyn_, scenes_, cap, o));
         span_end(e0, 6);
         ++launches_;
         return DIO_OK;
@@ -2103,6 +2191,10 @@ class Engine final : public EngineBase {
     std::vector<uint2> chunks_host_;
     std::vector<uint2> solve_chunks_host_;  // chunks of the scene-chunk solve
     uint2* solve_chunks_ = nullptr;
+    uint2* chunk_dyn_ = nullptr;        // each solve chunk's run of the dynamic-body list
+    uint32_t* scene_chunk_ = nullptr;   // solve chunk of every scene
+    bool chunked_scenes_ = false;       // every scene has a solve chunk
+    uint32_t solve_chunk_max_ = 0;      // bodies of the largest solve chunk
     uint2* chunks_ = nullptr;
     Slot<R>* slots_[2] = {nullptr, nullptr};
     // inside step_body_dev: its scratch zeroing is done by k_roll_counters and

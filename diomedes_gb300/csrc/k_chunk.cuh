@@ -8,21 +8,28 @@
 // scene -- so a chunk of whole scenes can run its whole schedule alone: its
 // snapshot / new poses (both Jacobi parities) and step-start poses live in
 // shared memory, the phases are separated by __syncthreads, and only the
-// rows, joint views and per-body constants stream from L2 / HBM.  Each phase
+// rows, joint views and per-body constants stream from L1 / L2 / HBM.  Each phase
 // evaluates exactly the expressions of the per-phase kernels (the same
 // device functions, reading shared instead of global memory), so the result
 // is bit-identical to init, 10 x (primal, dual), recover launched one by one.
 //
 // Shared memory per body: pos[2], rot[2], init pos, init rot = 6 x A4<P>
 // (96 B at FP32, 192 B at FP64 poses); a chunk holds at most
-// solve_chunk_cap<P>() bodies (2048 / 1024), one CTA per SM.
+// solve_chunk_cap<P>() bodies (2048 / 1024), one CTA per SM.  The host packs
+// scenes into chunks so that the chunks fill whole waves of the GPU's SMs.
+// (Measured and dropped: 64 B per body with the step-start poses read from
+// global memory, which let one wave of 152 chunks of up to 3391 bodies hold
+// the bench batch, ran the solve 0.48 -> 0.59 ms: the step-start reads of
+// contact rows and the smaller L1 cost more than the wave saved.)
 #pragma once
 
 #include "k_avbd.cuh"
 
 namespace dio {
 
+// threads per CTA: 512 (128 registers, no spill) or 640 (96 registers)
 constexpr int kChunkThreads = 512;
+constexpr int kChunkThreadsWide = 640;
 
 template <class P>
 __host__ __device__ constexpr size_t chunk_smem_bytes(uint32_t cap) {
@@ -57,14 +64,17 @@ __device__ __forceinline__ uint32_t warp_lower_bound(const uint2* ab, uint32_t s
     return lo + __popc(__ballot_sync(0xFFFFFFFFu, less));
 }
 
-// One CTA per chunk (chunks[c] = scene range [x, y), bodies contiguous).
-// `cap` is the shared-memory capacity in bodies.  Rows of the chunk: its
+// One CTA per chunk (chunks[c] = scene range [x, y), bodies contiguous;
+// dyn_runs[c] = the chunk's run of the dynamic-body list, ordered by work
+// signature so a warp's bodies take the same code path).
+// `cap` is the shared-memory capacity in bodies (the largest chunk).  Rows of the chunk: its
 // pair rows are one range of the pair-row section (pairs sorted by body a,
 // scenes contiguous) and its container rows one range of the container
 // section (dynamic bodies in index order).
-template <class P, class R>
-__global__ void __launch_bounds__(kChunkThreads, 1)
-    k_solve_chunks(DevWorld<P, R> w, const uint2* chunks, const SceneDesc* scenes, uint32_t cap, SolveParams<R> o) {
+template <class P, class R, int T>
+__global__ void __launch_bounds__(T, 1)
+    k_solve_chunks(DevWorld<P, R> w, const uint2* chunks, const uint2* dyn_runs, const SceneDesc* scenes, uint32_t cap,
+                   SolveParams<R> o) {
     extern __shared__ __align__(16) unsigned char chunk_smem[];
     __shared__ uint32_t s_rows[4];
     pdl_enter();
@@ -75,6 +85,7 @@ __global__ void __launch_bounds__(kChunkThreads, 1)
     A4<P>* const s_ipos = s_pos + 4 * cap;
     A4<P>* const s_irot = s_pos + 5 * cap;
     const uint2 ch = chunks[blockIdx.x];
+    const uint2 dr = dyn_runs[blockIdx.x];  // the chunk's dynamic bodies: w.dyn_list[dr.x, dr.y)
     const uint32_t lo = scenes[ch.x].body_lo, hi = scenes[ch.y - 1].body_hi;
     const uint32_t tid = threadIdx.x, nt = blockDim.x;
 
@@ -105,7 +116,8 @@ __global__ void __launch_bounds__(kChunkThreads, 1)
     for (uint32_t k = 0; k < o.iterations; ++k) {
         const uint32_t rd = (k & 1u) * cap, wr = cap - rd;
         const SmemFetch<P> f{s_pos + rd, s_rot + rd, s_ipos, s_irot, s_pos + wr, s_rot + wr, lo};
-        for (uint32_t i = lo + tid; i < hi; i += nt) {
+        for (uint32_t t = dr.x + tid; t < dr.y; t += nt) {
+            const uint32_t i = w.dyn_list[t];
             const uint32_t k0 = w.n_joints ? w.joint_off[i] : 0u, k1 = w.n_joints ? w.joint_off[i + 1] : 0u;
             primal_body_f(w, i, k0, k1, o, f);
         }

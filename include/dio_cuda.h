@@ -217,7 +217,8 @@ typedef struct DioConfig {
     uint32_t primal_variant;    /* primal kernel variant, 0 .. DIO_PRIMAL_VARIANTS-1
                                    (launch shape, body tiles; every variant
                                    computes the same bits; autotuned)     */
-    uint32_t block_size;        /* reserved (0)                           */
+    uint32_t block_size;        /* threads per CTA of the scene-chunk
+                                   solve: 0 (512) or 640 (autotuned)      */
     uint32_t batched_solver;    /* DioSolveLaunch: DIO_SOLVE_AUTO (0) runs
                                    a world step's whole solve (init, the
                                    iterations, recover) as one launch, a
