@@ -1,9 +1,18 @@
 """Benchmark: body-steps/s of the full rigid-body step on GB300.
 
-Workload (default): 1024 independent joint + contact scenes (body counts
-log-uniform in [16, 2048], rope / ball-socket / spring chains and loose boxes
-on the ground), dt 1/60, 10 AVBD iterations, packed into one device world
-and stepped by dio_step (broad -> narrow -> rows + warm start -> solve).
+Workloads (--config), seeded synthetic scenes of the stated sizes:
+  batched  (default) 1024 independent joint + contact scenes (body counts
+           log-uniform in [16, 2048]; rope / ball-socket / spring chains and
+           0-200 loose boxes on the ground), dt 1/60, 10 AVBD iterations,
+           packed into one device world
+  pyramid  10-level pyramid of 55 unit cubes, dt 1/60, 10 iterations, up to
+           8 contacts per pair
+  field    32 x 32 x 8 cube field dropped on the ground, dt 1/60, 10 iterations
+  pile     50,000 mixed convex bodies (boxes, 42-vertex hulls, tetrahedra),
+           dt 1/120, 12 iterations
+  wall     400 x 500-brick wall at x = 1e5 m and 1000 spheres, dt 1/120,
+           15 iterations, FP32/FP64 split precision
+Each step is dio_step: broad -> narrow -> rows + warm start -> solve.
 
 One JSON line on rank 0:
   value      body-steps/s with the world resident in HBM (CUDA events on the
@@ -13,12 +22,22 @@ One JSON line on rank 0:
              reads poses + state back (dio_world_download); timed with the
              batch as one world and as several worlds on several streams
              (dio_worlds_step_host), the faster reported
+  per_phase  the same K steps with the solve launched per phase (init,
+             primal / dual per iteration, recover) instead of one scene-chunk
+             launch, and the primal kernel's roofline
   plain      the one-scene-per-launch path (one context per scene) on a
              sample of scenes, for the batched-vs-plain ratio
-  roofline   the primal kernel: algorithmic bytes per launch / event time
-  cpu_baseline  the CPU oracle (OpenMP over bodies / rows) on a sample
---impl reference times the CPU restatement of the reference path (the
-reference is Rust + Vulkan; neither toolchain nor a Vulkan device exists here).
+  roofline   the dominant solve kernel: algorithmic bytes per launch / event
+             time
+  fp64_error position / angle error of the FP32 and split worlds against an
+             all-FP64 world after --error-steps steps, per content class,
+             beside the chaos floor (FP64 from positions nudged by one FP32
+             ulp against FP64)
+  cpu_baseline  the CPU oracle (OpenMP over bodies / rows) on the same
+             workload
+--impl reference times the CPU restatement of the reference path on the
+same workload (the reference is Rust + Vulkan; neither toolchain nor a
+Vulkan device exists here).
 """
 import argparse
 import json
@@ -36,6 +55,20 @@ sys.path.insert(0, ROOT)
 
 METRIC = "body-steps/s at 10 iters, batched vs plain on 1 GB300; max pos err vs FP64 (m)"
 
+# workload -> (description, precision, contacts per pair, pairs / rows per body of the capacity)
+CONFIGS = {
+    "batched": ("batched {scenes} scenes (rope / ball-socket / spring chains + loose boxes), dt 1/60, "
+                "10 iterations", "f32", 4, (2, 4)),
+    "pyramid": ("10-level pyramid of 55 unit cubes on the ground, dt 1/60, 10 iterations, up to 8 contacts "
+                "per pair", "f32", 8, (64, 200)),
+    "field": ("32 x 32 x 8 cube field (side 0.5 m, random orientations) dropped on the ground, dt 1/60, "
+              "10 iterations", "f32", 4, (24, 24)),
+    "pile": ("mixed convex pile of 50,000 bodies (40% boxes, 40% 42-vertex hulls, 20% tetrahedra), dt 1/120, "
+             "12 iterations", "f32", 4, (4, 8)),
+    "wall": ("wall throw: 400 x 500 bricks at x = 1e5 m + 1000 spheres at 30 m/s, dt 1/120, 15 iterations, "
+             "FP32 Hessian / FP64 poses", "split", 4, (3, 8)),
+}
+
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -43,21 +76,30 @@ def parse():
     ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="batched", choices=sorted(CONFIGS))
     ap.add_argument("--scenes", type=int, default=1024)
+    ap.add_argument("--strong", action="store_true",
+                    help="N > 1: shard one batch across the ranks (strong scaling) instead of a batch per rank")
     ap.add_argument("--plain-scenes", type=int, default=128)
+    ap.add_argument("--error-steps", type=int, default=600,
+                    help="steps of the FP32 / split / FP64 error study (capped by the workload's own step count)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--e2e-worlds", type=int, default=4,
                     help="e2e: the batch as this many worlds on as many streams (dio_worlds_step_host)")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-f64", action="store_true")
+    ap.add_argument("--no-per-phase", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="keep the default configuration (profiling runs)")
+    ap.add_argument("--per-phase", action="store_true",
+                    help="time the per-phase solve launches as the headline (profiling the primal kernel)")
     ap.add_argument("--save-state", default=None, metavar="PATH",
                     help="after the timed region, write the world as a checkpoint image")
     ap.add_argument("--load-state", default=None, metavar="PATH",
                     help="resume the world from a checkpoint image before the warm-up (profiling a late step)")
-    ap.add_argument("--precision", default="f32", choices=["f32", "split"],
-                    help="arithmetic of the timed world (split: FP64 poses / lambda, FP32 Hessian)")
+    ap.add_argument("--precision", default=None, choices=["f32", "split"],
+                    help="arithmetic of the timed world (split: FP64 poses / lambda, FP32 Hessian); "
+                         "default: the workload's own")
     return ap.parse_args()
 
 
@@ -126,13 +168,33 @@ def measured_hbm_peak():
         return 6800.0, "fallback"
 
 
-def world_capacity(sc):
+def make_workload(args, rank, world):
+    """The rank's scenes and the scaling mode.  batched: a batch of
+    args.scenes scenes per rank (weak scaling: rank r steps sub-batch r of
+    the N-batch workload), or with --strong one batch sharded across the
+    ranks by cost (dio_dist.shard_scenes).  Single-scene workloads run one
+    replica per rank."""
+    from diomedes_gb300 import dist as dio_dist
+    from diomedes_gb300 import scenes
+
+    if args.config == "batched":
+        if args.strong and world > 1:
+            full = scenes.batched(n_scenes=args.scenes)
+            mine = dio_dist.shard_scenes(dio_dist.scene_costs(full.scene_offsets, full.constraints), world)[rank]
+            return full.select(mine), "strong"
+        return scenes.batched(n_scenes=args.scenes, seed=4 + 1000 * rank), "weak"
+    make = {"pyramid": lambda: scenes.pyramid(levels=10), "field": lambda: scenes.cube_field(nx=32, nz=32, ny=8),
+            "pile": lambda: scenes.mixed_pile(n=50000), "wall": lambda: scenes.wall_throw(cols=400, rows=500)}
+    return make[args.config](), "weak"
+
+
+def world_capacity(sc, per_body=(2, 4)):
     from diomedes_gb300 import compute
 
-    # the joint scenes carry ~0.6 rows and ~0.01 pairs per body; 2 pairs and
-    # 4 rows per body leave a wide margin (overflow is reported, not dropped)
+    # overflow is reported (DIO_ERR_CAPACITY), never dropped; the batched
+    # scenes carry ~0.6 rows and ~0.01 pairs per body
     n = sc.n
-    return compute.capacity(n, max_pairs=max(1024, 2 * n), max_contacts=max(4096, 4 * n),
+    return compute.capacity(n, max_pairs=max(1024, per_body[0] * n), max_contacts=max(4096, per_body[1] * n),
                             max_joints=max(1, len(sc.constraints)), max_scenes=sc.n_scenes,
                             max_hull_vertices=max(1, 0 if sc.hull_vertices is None else len(sc.hull_vertices)))
 
@@ -143,6 +205,23 @@ def primal_bytes(n_dyn, m, j_inc):
     pose), per contact row 108 B + two 4-byte CSR entries, per joint
     incidence 44 B + 4 B."""
     return 132 * n_dyn + (108 + 8) * m + 48 * j_inc
+
+
+def chunk_solve_bytes(n, m, j_inc):
+    """Compulsory bytes of one scene-chunk solve launch (the whole step's
+    init, iterations and recover; every array element read or written once):
+    per body 152 B (pose, velocities, inverse mass / moment and the two CSR
+    offsets read; pose and velocities written), per contact row 148 B (row
+    payload, friction and bodies read, lambda / penalty written, two CSR
+    entries of 8 B), per joint incidence 48 B."""
+    return 152 * n + 148 * m + 48 * j_inc
+
+
+def iteration_bytes(n_dyn, m, j_inc):
+    """The per-iteration compulsory model of a per-phase solve, which re-reads
+    every pose and row each iteration: 188 N + 248 M + 52 J (J joints, two
+    incidences each)."""
+    return 188 * n_dyn + 248 * m + 26 * j_inc
 
 
 # DRAM traffic of one k_primal launch over its algorithmic bytes, from one ncu
@@ -163,12 +242,13 @@ def primal_gather_bytes(n_dyn, pair_rows, cont_rows, j_inc):
     return 132 * n_dyn + incid * (108 + 8) + 2 * pair_rows * 64 + j_inc * (48 + 32)
 
 
-def run_cpu(sc, steps, warmup, threads, budget_s=20.0):
-    """CPU oracle (f32) on a scene: body-steps/s."""
+def run_cpu(sc, steps, warmup, threads, budget_s=20.0, contacts_per_pair=4):
+    """CPU oracle (f32) on a scene: body-steps/s over the steps after
+    `warmup` untimed ones (stops early at the time budget)."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_lib as O
 
-    w = O.World(sc, threads=threads)
+    w = O.World(sc, threads=threads, contacts_per_pair=contacts_per_pair)
     w.step(sc.options, warmup)
     t0 = time.perf_counter()
     done = 0
@@ -181,37 +261,120 @@ def run_cpu(sc, steps, warmup, threads, budget_s=20.0):
     return sc.n * done / dt, done, dt
 
 
-def sample_scenes(scenes_mod, sc, count):
-    """The first `count` scenes of a packed batch as their own world."""
-    off = sc.scene_offsets
-    count = min(count, len(off) - 1)
-    hi = int(off[count])
-    cons = sc.constraints[(sc.constraints["a"] < hi)]
-    return scenes_mod.Scene(f"{sc.name}[:{count}]", sc.bodies[:hi].copy(), sc.state[:hi].copy(), constraints=cons,
-                            scene_offsets=off[: count + 1].copy(), containers=sc.containers[:count],
-                            options=sc.options, steps=sc.steps)
+def workload_config(args, sc, scaling, world):
+    desc = CONFIGS[args.config][0].format(scenes=sc.n_scenes)
+    return {"workload": desc, "bodies_per_gpu": sc.n, "scenes_per_gpu": sc.n_scenes, "joints": len(sc.constraints),
+            "l2": "working set > L2 (129 MB)" if sc.n > 100_000 else "working set within L2 (129 MB)",
+            "parallelism": f"scene-sharded x{world} ({scaling})" if args.config == "batched"
+            else f"replicas x{world}"}
 
 
-def reference_arm(args, rank):
-    from diomedes_gb300 import scenes
-
+def reference_arm(args, rank, world):
+    """The reference's path on the host cores: the CPU restatement (the
+    reference itself is Rust + Vulkan), on this arm's workload, W untimed
+    steps then up to K timed steps within a time budget."""
     if rank != 0:
         return
-    sc = scenes.batched(n_scenes=args.scenes)
-    sample = sample_scenes(scenes, sc, 64)
+    sc, scaling = make_workload(args, 0, 1)
     threads = os.cpu_count() or 1
-    v, done, dt = run_cpu(sample, max(1, args.steps), max(1, min(args.warmup, 3)), threads, budget_s=60.0)
+    v, done, dt = run_cpu(sc, max(1, args.steps), max(0, args.warmup), threads, budget_s=90.0,
+                          contacts_per_pair=CONFIGS[args.config][2])
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "body-steps/s", "n_gpus": args.gpus,
         "steps": done, "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(1, done), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"batched {args.scenes} scenes (joints + contacts), 10 iterations",
-                   "sample": f"first 64 scenes, {sample.n} bodies"},
+        "scaling": scaling, "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": workload_config(args, sc, scaling, world),
         "cpu_baseline": {"value": v, "unit": "body-steps/s", "cores": threads, "kind": "port",
-                         "sample": f"first 64 of {args.scenes} scenes ({sample.n} bodies), {done} steps"},
+                         "sample": f"the whole workload ({sc.n} bodies), {done} steps after {args.warmup} "
+                                   "untimed ones"},
         "e2e": {"value": v, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def body_classes(sc):
+    """Dynamic bodies grouped by content: for joint scenes by the kind of
+    joint they hang on (rope, ball-socket, spring, rod) or loose; otherwise
+    by shape."""
+    from diomedes_gb300 import abi
+
+    dyn = sc.state["inv_mass"] != 0
+    cls = {}
+    if len(sc.constraints):
+        kinds = {0: "spring", 1: "rod", 2: "ball_socket", 3: "rope"}
+        tag = np.full(sc.n, -1, np.int64)
+        for k in kinds:
+            c = sc.constraints[sc.constraints["kind"] == k]
+            tag[c["a"]] = k
+            tag[c["b"]] = k
+        for k, name in kinds.items():
+            idx = np.flatnonzero(dyn & (tag == k))
+            if len(idx):
+                cls[name] = idx
+        loose = np.flatnonzero(dyn & (tag < 0))
+        if len(loose):
+            cls["loose_box"] = loose
+    else:
+        shapes = {abi.SPHERE: "sphere", abi.CUBE: "cube", abi.TETRAHEDRON: "tetrahedron", abi.BOX: "box",
+                  abi.HULL: "hull"}
+        for t, name in shapes.items():
+            idx = np.flatnonzero(dyn & (sc.bodies["shape"]["tag"] == t))
+            if len(idx):
+                cls[name] = idx
+    cls["all"] = np.flatnonzero(dyn)
+    return cls
+
+
+def error_study(sc, o, steps, cap, cpp, tuned):
+    """FP32, split and all-FP64 worlds stepped `steps` from the same initial
+    state, plus the chaos floor: an FP64 world whose dynamic bodies' initial
+    positions are nudged by one FP32 ulp.  Max / median position error (m)
+    and max angle error (rad) per content class against the FP64 world."""
+    from diomedes_gb300 import compute
+
+    pos0 = sc.positions_f64 if sc.positions_f64 is not None else sc.bodies["position"][:, :3].astype(np.float64)
+    dyn = sc.state["inv_mass"] != 0
+    nudged = pos0.copy()
+    nudged[dyn] = pos0[dyn] + np.spacing(pos0[dyn].astype(np.float32)).astype(np.float64)
+
+    def run(precision, positions_f64=None):
+        kw = sc.upload_kwargs()
+        if positions_f64 is not None:
+            kw["positions_f64"] = positions_f64
+        w = compute.World(cap, precision=precision, contacts_per_pair=cpp, **tuned)
+        w.upload(sc.bodies, sc.state, **kw)
+        w.step(o, steps)
+        p, q = w.download_f64()
+        w.close()
+        return p, q
+
+    p64, q64 = run(2)
+    runs = {"fp32": run(0), "split": run(1), "chaos_floor": run(2, nudged)}
+
+    def ang(q):
+        c = np.abs((q * q64).sum(axis=1))
+        return 2.0 * np.arccos(np.clip(c, 0.0, 1.0))
+
+    out = {"steps": steps, "classes": {}}
+    for name, idx in body_classes(sc).items():
+        row = {"bodies": int(len(idx))}
+        for k, (p, q) in runs.items():
+            e = np.abs(p[idx] - p64[idx]).max(axis=1)
+            row[k] = {"max_pos_err_m": float(e.max()), "median_pos_err_m": float(np.median(e)),
+                      "max_angle_err_rad": float(ang(q)[idx].max())}
+        out["classes"][name] = row
+    allc = out["classes"]["all"]
+    out["max_pos_err_m"] = allc["split"]["max_pos_err_m"]
+    out["median_pos_err_m"] = allc["split"]["median_pos_err_m"]
+    out["fp32_max_pos_err_m"] = allc["fp32"]["max_pos_err_m"]
+    out["chaos_floor_max_pos_err_m"] = allc["chaos_floor"]["max_pos_err_m"]
+    return out
+
+
+def tuned_config(w):
+    c = w.configure()
+    return {"primal_variant": c.primal_variant, "bvh_rebuild_period": c.bvh_rebuild_period,
+            "batched_solver": c.batched_solver, "block_size": c.block_size}
 
 
 def main():
@@ -220,7 +383,7 @@ def main():
         args.no_f64 = True  # the FP64 comparison steps from the initial state
     rank, world, local = dist_info()
     if args.impl == "reference":
-        return reference_arm(args, rank)
+        return reference_arm(args, rank, world)
 
     import torch
 
@@ -231,23 +394,26 @@ def main():
 
         dist.init_process_group("nccl")
 
-    from diomedes_gb300 import compute, scenes
+    from diomedes_gb300 import abi, compute
+    from diomedes_gb300 import dist as dio_dist
 
-    sc = scenes.batched(n_scenes=args.scenes, seed=4 + 1000 * rank)
+    sc, scaling = make_workload(args, rank, world)
+    _, default_prec, cpp, per_body = CONFIGS[args.config]
+    prec = 1 if (args.precision or default_prec) == "split" else 0
+    cap = world_capacity(sc, per_body)
     stream = torch.cuda.current_stream()
-    prec = 1 if args.precision == "split" else 0
-    w = compute.World(world_capacity(sc), profile=0, precision=prec)
+    w = compute.World(cap, profile=0, precision=prec, contacts_per_pair=cpp)
     w.set_stream(stream.cuda_stream)
     w.upload(sc.bodies, sc.state, **sc.upload_kwargs())
     if args.load_state:
         with open(args.load_state, "rb") as f:
             w.resume(f.read())
     o = sc.options
-    if args.no_tune:
-        c = w.configure()
-        tuned = {"primal_variant": c.primal_variant, "bvh_rebuild_period": c.bvh_rebuild_period}
-    else:
-        tuned = w.autotune(o, trial_steps=4)  # launch shape + LBVH rebuild period; state restored
+    if not args.no_tune:
+        w.autotune(o, trial_steps=4)  # solve launch, CTA size / launch shape, LBVH rebuild period; state restored
+    if args.per_phase:
+        w.configure(batched_solver=abi.SOLVE_PER_PHASE)
+    tuned = tuned_config(w)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     # the clock sampler starts with the warm-up so that its 50 ms samples
     # cover the (sub-second) timed region
@@ -269,13 +435,11 @@ def main():
     if args.save_state:
         with open(args.save_state, "wb") as f:
             f.write(w.checkpoint())
-    b32_after, _ = w.download()  # for the FP64 comparison below
-    p_after, q_after = w.download_f64() if prec else (None, None)
-    rows_after = w.contacts()
+    state_after = w.checkpoint()  # the passes below start from the state the timed steps reached
 
     # a second pass of the same K steps with the per-phase / per-launch event
     # timers on (they add an event pair per span, so the headline pass above
-    # runs without them): phase split and the primal's launch duration
+    # runs without them): phase split and the solve kernel's launch duration
     w.configure(profile=1)
     w.step(o, 3)
     torch.cuda.synchronize()
@@ -288,28 +452,78 @@ def main():
     stp = w.stats()
     ms_profiled = q0.elapsed_time(q1)
     w.configure(profile=0)
-    from diomedes_gb300 import dist as dio_dist
 
     # max time over ranks, body-steps summed over ranks (each rank owns its scenes)
     ms_max, body_steps = dio_dist.frame(dist, ms, sc.n * args.steps, device="cuda")
     n_dyn = int((sc.state["inv_mass"] != 0).sum())
-    total_bodies = sc.n * world
     value = body_steps / (ms_max / 1e3)
-
-    # roofline of the primal kernel (event-timed on the launching stream)
     peak, peak_kind = measured_hbm_peak()
-    prim_ms = stp["primal_ms"] / max(1, stp["primal_launches"])
     j_inc = 2 * len(sc.constraints)
-    pb = primal_bytes(n_dyn, stp["contacts"], j_inc)
-    achieved = pb / (prim_ms / 1e3) / 1e9 if prim_ms > 0 else None
     rows_now = w.contacts()
     cont_rows = int((rows_now["b"] == 0xFFFFFFFF).sum())
-    pg = primal_gather_bytes(n_dyn, len(rows_now) - cont_rows, cont_rows, j_inc)
+    m_now = int(stp["contacts"])
+
+    def primal_roofline(s):
+        prim_ms = s["primal_ms"] / max(1, s["primal_launches"])
+        pb = primal_bytes(n_dyn, s["contacts"], j_inc)
+        pg = primal_gather_bytes(n_dyn, len(rows_now) - cont_rows, cont_rows, j_inc)
+        ach = pb / (prim_ms / 1e3) / 1e9 if prim_ms > 0 else None
+        return {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak if ach else None,
+                "traffic": PRIMAL_TRAFFIC_RATIO * pb,
+                "traffic_source": "ncu DRAM bytes of one launch at the timed state (step 310), scaled by "
+                                  "algorithmic bytes",
+                "kernel": "k_primal", "bytes_per_launch": pb, "avg_launch_ms": prim_ms, "peak_kind": peak_kind,
+                "gather_bytes_per_launch": pg,
+                "achieved_gather": pg / (prim_ms / 1e3) / 1e9 if prim_ms > 0 else None}
+
+    if stp["chunk_launches"]:
+        chunk_ms = stp["chunk_ms"] / stp["chunk_launches"]
+        cb = chunk_solve_bytes(sc.n, m_now, j_inc)
+        ach = cb / (chunk_ms / 1e3) / 1e9
+        it_b = iteration_bytes(n_dyn, m_now, j_inc) * int(o.iterations)
+        roofline = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                    "traffic": None, "kernel": "k_solve_chunks", "bytes_per_launch": cb, "avg_launch_ms": chunk_ms,
+                    "peak_kind": peak_kind,
+                    "limiter": "SM issue, not HBM: poses stay in shared memory across the iterations, rows and "
+                               "joint views are re-read from L1 / L2",
+                    "per_phase_equivalent_bytes": it_b,
+                    "per_phase_equivalent_GBs": it_b / (chunk_ms / 1e3) / 1e9}
+    else:
+        roofline = primal_roofline(stp)
+
+    # the same K steps from the same state with the solve launched per
+    # phase (init, primal / dual per iteration, recover): the primal
+    # kernel's roofline and the gain of the one-launch solve
+    per_phase = None
+    if stp["chunk_launches"] and not args.no_per_phase:
+        w.resume(state_after)
+        w.configure(batched_solver=abi.SOLVE_PER_PHASE)
+        w.step(o, 3)
+        torch.cuda.synchronize()
+        r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        r0.record(stream)
+        w.step(o, args.steps)
+        r1.record(stream)
+        torch.cuda.synchronize()
+        pp_ms = r0.elapsed_time(r1)
+        w.configure(profile=1)
+        w.step(o, 3)
+        torch.cuda.synchronize()
+        w.reset_timers()
+        w.step(o, args.steps)
+        torch.cuda.synchronize()
+        spp = w.stats()
+        w.configure(profile=0, batched_solver=tuned["batched_solver"])
+        per_phase = {"value": sc.n * args.steps / (pp_ms / 1e3), "ms_per_step": pp_ms / args.steps,
+                     "roofline": primal_roofline(spp),
+                     "phase_ms_per_step": {k: spp[f"{k}_ms"] / args.steps
+                                           for k in ("broad", "narrow", "rows", "solve", "primal", "dual")}}
 
     # end to end through the public API with host buffers: the demos'
     # per-frame loop (upload poses + state, step, read them back)
     e2e = None
     if not args.no_e2e:
+        w.resume(state_after)
         # the caller's host arrays: page-locked (cudaHostAlloc through torch)
         hb = torch.empty(sc.n * sc.bodies.dtype.itemsize, dtype=torch.uint8,
                          pin_memory=True).numpy().view(sc.bodies.dtype)
@@ -325,48 +539,46 @@ def main():
             w.step(o, 1)
             w.download_into(hb, hs)
         t1 = time.perf_counter()
-        single = total_bodies * k2 / (t1 - t0)
+        single = sc.n * k2 / (t1 - t0)
         # (2) the same batch as G worlds (contiguous runs of whole scenes) on
         # G streams, stepped by dio_worlds_step_host: one world's host copies
         # overlap the other worlds' steps
-        parts, starts = sc.split(args.e2e_worlds)
-        worlds, streams, vb, vs = [], [], [], []
-        for p, lo in zip(parts, starts):
-            wg = compute.World(world_capacity(p), profile=0, precision=prec)
-            streams.append(torch.cuda.Stream())
-            wg.set_stream(streams[-1].cuda_stream)
-            wg.upload(p.bodies, p.state, **p.upload_kwargs())
-            wg.configure(primal_variant=tuned["primal_variant"], bvh_rebuild_period=tuned["bvh_rebuild_period"])
-            worlds.append(wg)
-            vb.append(hb[lo:lo + p.n])
-            vs.append(hs[lo:lo + p.n])
-        compute.step_host(worlds, vb, vs, o, args.warmup)  # from the state reached above
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        compute.step_host(worlds, vb, vs, o, k2)
-        t1 = time.perf_counter()
-        piped = total_bodies * k2 / (t1 - t0)
-        for wg in worlds:
-            wg.close()
-        e2e = {"value": max(piped, single), "unit": "body-steps/s",
+        piped, parts = 0.0, [sc]
+        if sc.n_scenes > 1:
+            parts, starts = sc.split(args.e2e_worlds)
+            worlds, streams, vb, vs = [], [], [], []
+            for p, lo in zip(parts, starts):
+                wg = compute.World(world_capacity(p, per_body), profile=0, precision=prec, contacts_per_pair=cpp)
+                streams.append(torch.cuda.Stream())
+                wg.set_stream(streams[-1].cuda_stream)
+                wg.upload(p.bodies, p.state, **p.upload_kwargs())
+                wg.configure(**tuned)
+                worlds.append(wg)
+                vb.append(hb[lo:lo + p.n])
+                vs.append(hs[lo:lo + p.n])
+            compute.step_host(worlds, vb, vs, o, args.warmup)  # from the state reached above
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            compute.step_host(worlds, vb, vs, o, k2)
+            t1 = time.perf_counter()
+            piped = sc.n * k2 / (t1 - t0)
+            for wg in worlds:
+                wg.close()
+        t_ms = 1e3 * sc.n * k2 / max(piped, single)  # this rank's time for its share
+        t_max, units = dio_dist.frame(dist, t_ms, sc.n * k2, device="cuda")
+        e2e = {"value": units / (t_max / 1e3), "unit": "body-steps/s",
                "h2d_bytes_per_step": int(hb.nbytes + hs.nbytes), "d2h_bytes_per_step": int(hb.nbytes + hs.nbytes),
                "steps": k2, "worlds": len(parts) if piped >= single else 1,
                "one_world": single, "worlds_on_streams": {"worlds": len(parts), "value": piped}}
 
     # plain path: one context per scene, stepped one scene at a time
     plain = None
-    if not args.no_plain and rank == 0:
+    if not args.no_plain and rank == 0 and sc.n_scenes > 1:
         idx = np.linspace(0, sc.n_scenes - 1, min(args.plain_scenes, sc.n_scenes)).astype(int)
         worlds, nb = [], 0
         for s in idx:
-            lo, hi = int(sc.scene_offsets[s]), int(sc.scene_offsets[s + 1])
-            cmask = (sc.constraints["a"] >= lo) & (sc.constraints["a"] < hi)
-            cons = sc.constraints[cmask].copy()
-            cons["a"] -= lo
-            cons["b"] -= lo
-            one = scenes.Scene("one", sc.bodies[lo:hi], sc.state[lo:hi], constraints=cons,
-                               containers=[sc.containers[s]], options=o)
-            pw = compute.World(world_capacity(one))
+            one = sc.select([s])
+            pw = compute.World(world_capacity(one, per_body), contacts_per_pair=cpp)
             pw.set_stream(stream.cuda_stream)
             pw.upload(one.bodies, one.state, **one.upload_kwargs())
             worlds.append(pw)
@@ -388,42 +600,16 @@ def main():
         for pw in worlds:
             pw.close()
 
-    # max position error vs the all-FP64 world after the same steps
+    # errors against the all-FP64 world at the workload's horizon, with the
+    # split path's throughput on the same batch beside the FP32 one
     f64 = None
     if not args.no_f64 and rank == 0:
-        b32 = b32_after
-        steps_done = args.warmup + args.steps
-        wf = compute.World(world_capacity(sc), precision=2)
-        wf.upload(sc.bodies, sc.state, **sc.upload_kwargs())
-        wf.step(o, steps_done)
-        p64, q64 = wf.download_f64()
-        rows64 = wf.contacts()
-        wf.close()
-
-        def pos_err(p):
-            return np.abs(p - p64).max(axis=1)
-
-        def ang_err(q):  # rotation angle between the two orientations
-            c = np.abs((q.astype(np.float64) * q64).sum(axis=1))
-            return 2.0 * np.arccos(np.clip(c, 0.0, 1.0))
-
-        def max_pen(rows):  # deepest row of the last step: depth = margin - c0.x
-            return float((o.margin - rows["c0"][:, 0]).max()) if len(rows) else 0.0
-
-        err = pos_err(p_after if prec else b32["position"][:, :3].astype(np.float64))
-        aerr = ang_err(q_after if prec else b32["orientation"])
-        f64 = {"max_pos_err_m": float(err.max()), "median_pos_err_m": float(np.median(err)),
-               "max_angle_err_rad": float(aerr.max()), "median_angle_err_rad": float(np.median(aerr)),
-               "max_penetration_m": max_pen(rows_after), "max_penetration_m_fp64": max_pen(rows64),
-               "steps": steps_done}
-        if not prec:  # the timed world is FP32: time the split path beside it
-            # the split-precision path on the same batch (FP64 poses / inertial
-            # terms / lambda, FP32 Hessian, LDL^T and detection): throughput and
-            # its own error against the FP64 world
-            ws = compute.World(world_capacity(sc), precision=1)
+        steps_err = max(1, min(args.error_steps, int(sc.steps)))
+        f64 = error_study(sc, o, steps_err, cap, cpp, tuned)
+        if not prec:
+            ws = compute.World(cap, precision=1, contacts_per_pair=cpp, **tuned)
             ws.set_stream(stream.cuda_stream)
             ws.upload(sc.bodies, sc.state, **sc.upload_kwargs())
-            ws.configure(primal_variant=tuned["primal_variant"], bvh_rebuild_period=tuned["bvh_rebuild_period"])
             ws.step(o, args.warmup)
             torch.cuda.synchronize()
             s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -431,54 +617,38 @@ def main():
             ws.step(o, args.steps)
             s1.record(stream)
             torch.cuda.synchronize()
-            ps, qs = ws.download_f64()
-            rows_s = ws.contacts()
             ws.close()
-            es, ea = pos_err(ps), ang_err(qs)
-            f64["split"] = {"value": sc.n * args.steps / (s0.elapsed_time(s1) / 1e3), "unit": "body-steps/s",
-                            "batched_over_plain": (sc.n * args.steps / (s0.elapsed_time(s1) / 1e3)) / plain["value"]
-                            if plain else None,
-                            "max_pos_err_m": float(es.max()), "median_pos_err_m": float(np.median(es)),
-                            "max_angle_err_rad": float(ea.max()), "max_penetration_m": max_pen(rows_s)}
+            sv = sc.n * args.steps / (s0.elapsed_time(s1) / 1e3)
+            f64["split_throughput"] = {"value": sv, "unit": "body-steps/s",
+                                       "batched_over_plain": sv / plain["value"] if plain else None}
 
     cpu = None
     if not args.no_cpu and rank == 0:
-        sample = sample_scenes(scenes, sc, 32)
         threads = os.cpu_count() or 1
-        v, done, dt = run_cpu(sample, 5, 1, threads, budget_s=20.0)
-        v1, done1, _ = run_cpu(sample, 3, 1, 1, budget_s=10.0)
+        ks = max(1, min(args.steps, 20))
+        wu = min(args.warmup, 5)
+        v, done, dt = run_cpu(sc, ks, wu, threads, budget_s=25.0, contacts_per_pair=cpp)
+        v1, done1, _ = run_cpu(sc, 2, 0, 1, budget_s=10.0, contacts_per_pair=cpp)
         cpu = {"value": v, "unit": "body-steps/s", "cores": threads, "kind": "port",
-               "sample": f"first 32 of {sc.n_scenes} scenes ({sample.n} bodies), {done} steps after 1 warm-up",
+               "sample": f"the whole workload ({sc.n} bodies): {done} steps after {wu} untimed ones, from the "
+                         "initial state",
                "single_thread": {"value": v1, "cores": 1, "steps": done1}}
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64/f32 split" if prec else "f32",
-            "data": "synthetic",
-            "config": {"workload": f"batched {sc.n_scenes} scenes (rope / ball-socket / spring chains + loose "
-                                   f"boxes), {sc.n} bodies per GPU, dt 1/60, 10 iterations",
-                       "bodies_per_gpu": sc.n, "contacts_last_step": st["contacts"],
-                       "pairs_last_step": st["pairs"], "joints": len(sc.constraints),
-                       "l2": "working set > L2 (129 MB): poses, rows and CSR re-read every iteration",
-                       "parallelism": f"scene-sharded x{world}",
-                       "tuned": {"primal_variant": tuned["primal_variant"],
-                                 "bvh_rebuild_period": tuned["bvh_rebuild_period"]}},
-            "e2e": e2e, "plain": plain, "fp64_error": f64,
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak if achieved else None,
-                         "traffic": PRIMAL_TRAFFIC_RATIO * pb,
-                         "traffic_source": "ncu DRAM bytes of one launch at the timed state (step 310), scaled by algorithmic bytes",
-                         "kernel": "k_primal", "bytes_per_launch": pb, "avg_launch_ms": prim_ms,
-                         "peak_kind": peak_kind,
-                         "gather_bytes_per_launch": pg,
-                         "achieved_gather": pg / (prim_ms / 1e3) / 1e9 if prim_ms > 0 else None},
+            "scaling": scaling, "vs_baseline": None, "dtype": "f64/f32 split" if prec else "f32",
+            "data": "synthetic", "config": workload_config(args, sc, scaling, world),
+            "run": {"contacts_last_step": st["contacts"], "pairs_last_step": st["pairs"], "tuned": tuned,
+                    "contacts_per_pair": cpp},
+            "e2e": e2e, "per_phase": per_phase, "plain": plain, "fp64_error": f64,
+            "roofline": roofline,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "gpu_launches": st["kernel_launches"],
             "phase_ms_per_step": {k: stp[f"{k}_ms"] / args.steps
-                                  for k in ("broad", "narrow", "rows", "solve", "primal", "dual")},
+                                  for k in ("broad", "narrow", "rows", "solve", "primal", "dual", "chunk")},
             "profiled_ms_per_step": ms_profiled / args.steps,
         }
         print(json.dumps(line), flush=True)
