@@ -91,6 +91,8 @@ def parse():
     ap.add_argument("--no-f64", action="store_true")
     ap.add_argument("--no-per-phase", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="keep the default configuration (profiling runs)")
+    ap.add_argument("--block-size", type=int, default=None, choices=[0, 640],
+                    help="threads per CTA of the scene-chunk solve (0: 512); default: the autotuner's choice")
     ap.add_argument("--per-phase", action="store_true",
                     help="time the per-phase solve launches as the headline (profiling the primal kernel)")
     ap.add_argument("--save-state", default=None, metavar="PATH",
@@ -413,6 +415,8 @@ def main():
         w.autotune(o, trial_steps=4)  # solve launch, CTA size / launch shape, LBVH rebuild period; state restored
     if args.per_phase:
         w.configure(batched_solver=abi.SOLVE_PER_PHASE)
+    if args.block_size is not None:
+        w.configure(block_size=args.block_size)
     tuned = tuned_config(w)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     # the clock sampler starts with the warm-up so that its 50 ms samples
