@@ -269,10 +269,9 @@ __device__ __forceinline__ void row_forces(const RowDual<P, R>& du, R mu, R c0, 
 
 // One contact row seen from body i (avbd/src/lib.rs:321-418).
 template <class P, class R, class F>
-__device__ __forceinline__ void primal_row_f(const DevWorld<P, R>& w, uint32_t r, uint32_t oth, const F& fetch,
-                                             Q4<R> sqr, V3<R> dqsl, V3<R> dqsa, R k_alpha, Block6<R>& B) {
-    const RowStatic<R> rs = w.rs[r];
-    const RowDual<P, R> du = w.rd[r];
+__device__ __forceinline__ void primal_row_core(const RowStatic<R>& rs, const RowDual<P, R>& du, uint32_t oth,
+                                                const F& fetch, Q4<R> sqr, V3<R> dqsl, V3<R> dqsa, R k_alpha,
+                                                Block6<R>& B) {
     const bool container = oth == kContainer;
     const bool is_a = container || !(oth & kIsB);
     const uint32_t other = oth & ~kIsB;
@@ -304,6 +303,20 @@ __device__ __forceinline__ void primal_row_f(const DevWorld<P, R>& w, uint32_t r
     stamp(B, r1, j1, du.penalty.y, R(f1));
     stamp(B, r2, j2, du.penalty.z, R(f2));
 }
+template <class P, class R, class F>
+__device__ __forceinline__ void primal_row_f(const DevWorld<P, R>& w, uint32_t r, uint32_t oth, const F& fetch,
+                                             Q4<R> sqr, V3<R> dqsl, V3<R> dqsa, R k_alpha, Block6<R>& B) {
+    primal_row_core<P, R>(w.rs[r], w.rd[r], oth, fetch, sqr, dqsl, dqsa, k_alpha, B);
+}
+// The rows of a body read from the world's current row duals.
+struct RowsFromWorld {
+    template <class P, class R, class F>
+    __device__ __forceinline__ void operator()(const DevWorld<P, R>& w, uint32_t i, uint32_t r, uint32_t oth,
+                                               const F& fetch, Q4<R> sqr, V3<R> dqsl, V3<R> dqsa, R k_alpha,
+                                               Block6<R>& B) const {
+        primal_row_f(w, r, oth, fetch, sqr, dqsl, dqsa, k_alpha, B);
+    }
+};
 
 template <class P, class R>
 __device__ __forceinline__ void primal_row(const DevWorld<P, R>& w, uint32_t r, uint32_t oth, int rd, Q4<R> sqr,
@@ -410,9 +423,9 @@ __device__ __forceinline__ void primal_jview_f(const JView& jv, const F& fetch, 
 
 // avbd_primal for one body: reads the snapshot through `fetch` and stores
 // the new pose through it.  [k0, k1) is the body's joint-view range.
-template <class P, class R, class F>
+template <class P, class R, class F, class Rows = RowsFromWorld>
 __device__ __forceinline__ void primal_body_f(const DevWorld<P, R>& w, uint32_t i, uint32_t k0, uint32_t k1,
-                                              const SolveParams<R>& o, const F& fetch) {
+                                              const SolveParams<R>& o, const F& fetch, const Rows& rows = Rows()) {
     const A4<R> inv = w.inv[i];
     if (inv.w == R(0)) return;
     const V3<P> sp = xyz(fetch.pos(i));
@@ -454,8 +467,7 @@ __device__ __forceinline__ void primal_body_f(const DevWorld<P, R>& w, uint32_t 
         const V3<R> dqsl = cast3<R>(sub(sp, xyz(fetch.ipos(i))));
         const V3<R> dqsa = ang_diff(sqr, castq<R>(quat(fetch.irot(i))));
         const R k_alpha = R(1) - o.alpha;
-        for (uint32_t j = j0; j < j1; ++j)
-            primal_row_f(w, w.row_idx[j], w.row_oth[j], fetch, sqr, dqsl, dqsa, k_alpha, B);
+        for (uint32_t j = j0; j < j1; ++j) rows(w, i, w.row_idx[j], w.row_oth[j], fetch, sqr, dqsl, dqsa, k_alpha, B);
     }
     for (uint32_t k = k0; k < k1; ++k) {
         const JView jv = w.jview[k];
@@ -579,23 +591,18 @@ __global__ void __launch_bounds__(128) k_primal_color(DevWorld<P, R> w, uint32_t
     }
 }
 
-// avbd_dual, avbd/src/lib.rs:565-663, for one row; `fetch` reads the new state.
-template <class P, class R, class F>
-__device__ __forceinline__ void dual_row_f(const DevWorld<P, R>& w, uint32_t c, const F& fetch,
-                                           const SolveParams<R>& o) {
-    const uint2 ab = w.ab[c];
-    const RowStatic<R> rs = w.rs[c];
-    RowDual<P, R> du = w.rd[c];
-    A4<P> pa4 = fetch.pos(ab.x);
-    A4<P> qa4 = fetch.rot(ab.x);
-    V3<R> dal = cast3<R>(sub(xyz(pa4), xyz(fetch.ipos(ab.x))));
-    V3<R> daa = ang_diff(castq<R>(quat(qa4)), castq<R>(quat(fetch.irot(ab.x))));
+// avbd_dual, avbd/src/lib.rs:565-663: the row's dual update from its bodies' new poses (a, and b unless the
+// row is against a container) and step-start poses.
+template <class P, class R>
+__device__ __forceinline__ RowDual<P, R> dual_update(const RowStatic<R>& rs, RowDual<P, R> du, A4<P> pa4, A4<P> qa4,
+                                                     A4<P> ia_p, A4<P> ia_q, bool has_b, A4<P> pb4, A4<P> qb4,
+                                                     A4<P> ib_p, A4<P> ib_q, const SolveParams<R>& o) {
+    V3<R> dal = cast3<R>(sub(xyz(pa4), xyz(ia_p)));
+    V3<R> daa = ang_diff(castq<R>(quat(qa4)), castq<R>(quat(ia_q)));
     V3<R> dbl{R(0), R(0), R(0)}, dba{R(0), R(0), R(0)}, rbw{R(0), R(0), R(0)};
-    if (ab.y != kContainer) {
-        A4<P> pb4 = fetch.pos(ab.y);
-        A4<P> qb4 = fetch.rot(ab.y);
-        dbl = cast3<R>(sub(xyz(pb4), xyz(fetch.ipos(ab.y))));
-        dba = ang_diff(castq<R>(quat(qb4)), castq<R>(quat(fetch.irot(ab.y))));
+    if (has_b) {
+        dbl = cast3<R>(sub(xyz(pb4), xyz(ib_p)));
+        dba = ang_diff(castq<R>(quat(qb4)), castq<R>(quat(ib_q)));
         rbw = rotate(castq<R>(quat(qb4)), xyz(rs.rb));
     }
     V3<R> raw = rotate(castq<R>(quat(qa4)), xyz(rs.ra));
@@ -615,7 +622,23 @@ __device__ __forceinline__ void dual_row_f(const DevWorld<P, R>& w, uint32_t c, 
         du.penalty.y = fmin_(du.penalty.y + o.beta_lin * dabs(c1), o.penalty_max);
         du.penalty.z = fmin_(du.penalty.z + o.beta_lin * dabs(c2), o.penalty_max);
     }
-    w.rd[c] = du;
+    return du;
+}
+// avbd_dual, avbd/src/lib.rs:565-663, for row c of `rd`: new duals into
+// `out`; `fetch` reads the new state.
+template <class P, class R, class F>
+__device__ __forceinline__ void dual_row_io(const DevWorld<P, R>& w, uint32_t c, const F& fetch,
+                                            const RowDual<P, R>* rd, RowDual<P, R>* out, const SolveParams<R>& o) {
+    const uint2 ab = w.ab[c];
+    const bool has_b = ab.y != kContainer;
+    const uint32_t b = has_b ? ab.y : ab.x;
+    out[c] = dual_update<P, R>(w.rs[c], rd[c], fetch.pos(ab.x), fetch.rot(ab.x), fetch.ipos(ab.x),
+                               fetch.irot(ab.x), has_b, fetch.pos(b), fetch.rot(b), fetch.ipos(b), fetch.irot(b), o);
+}
+template <class P, class R, class F>
+__device__ __forceinline__ void dual_row_f(const DevWorld<P, R>& w, uint32_t c, const F& fetch,
+                                           const SolveParams<R>& o) {
+    dual_row_io(w, c, fetch, w.rd, w.rd, o);
 }
 template <class P, class R>
 __device__ __forceinline__ void dual_row(const DevWorld<P, R>& w, uint32_t c, int rd, const SolveParams<R>& o) {

@@ -20,7 +20,12 @@
 // (Measured and dropped: 64 B per body with the step-start poses read from
 // global memory, which let one wave of 152 chunks of up to 3391 bodies hold
 // the bench batch, ran the solve 0.48 -> 0.59 ms: the step-start reads of
-// contact rows and the smaller L1 cost more than the wave saved.)
+// contact rows and the smaller L1 cost more than the wave saved.  Also
+// measured and dropped: forming each row's dual inside the next iteration's
+// primal -- bit-identical, one barrier per iteration instead of two, duals
+// of pair rows formed by both endpoints, a second dual buffer -- which ran
+// 0.48 -> 0.59 ms (640 threads) and 0.50 -> 0.54 ms (512): the extra work
+// and spills in the primal cost more than the barrier saved.)
 #pragma once
 
 #include "k_avbd.cuh"
