@@ -64,9 +64,9 @@ CONFIGS = {
     "field": ("32 x 32 x 8 cube field (side 0.5 m, random orientations) dropped on the ground, dt 1/60, "
               "10 iterations", "f32", 4, (24, 24)),
     "pile": ("mixed convex pile of 50,000 bodies (40% boxes, 40% 42-vertex hulls, 20% tetrahedra), dt 1/120, "
-             "12 iterations", "f32", 4, (4, 8)),
+             "12 iterations", "f32", 4, (16, 32)),
     "wall": ("wall throw: 400 x 500 bricks at x = 1e5 m + 1000 spheres at 30 m/s, dt 1/120, 15 iterations, "
-             "FP32 Hessian / FP64 poses", "split", 4, (3, 8)),
+             "FP32 Hessian / FP64 poses", "split", 4, (8, 16)),
 }
 
 
@@ -339,25 +339,49 @@ def error_study(sc, o, steps, cap, cpp, tuned):
     nudged = pos0.copy()
     nudged[dyn] = pos0[dyn] + np.spacing(pos0[dyn].astype(np.float32)).astype(np.float64)
 
-    def run(precision, positions_f64=None):
+    from diomedes_gb300 import abi
+
+    def run(precision, positions_f64=None, horizon=None):
+        """Step to `horizon` (or as far as the capacity lets the world go, in
+        blocks of 25 steps, when horizon is None); returns the poses and the
+        steps done."""
         kw = sc.upload_kwargs()
         if positions_f64 is not None:
             kw["positions_f64"] = positions_f64
         w = compute.World(cap, precision=precision, contacts_per_pair=cpp, **tuned)
         w.upload(sc.bodies, sc.state, **kw)
-        w.step(o, steps)
-        p, q = w.download_f64()
+        done, last = 0, None
+        target = steps if horizon is None else horizon
+        while done < target:
+            k = min(25, target - done)
+            try:
+                w.step(o, k)
+            except abi.DioError as e:
+                if e.status != abi.DIO_ERR_CAPACITY or horizon is not None:
+                    raise
+                break
+            done += k
+            last = w.download_f64()
         w.close()
-        return p, q
+        return last, done
 
-    p64, q64 = run(2)
-    runs = {"fp32": run(0), "split": run(1), "chaos_floor": run(2, nudged)}
+    worlds = {"fp64": (2, None), "fp32": (0, None), "split": (1, None), "chaos_floor": (2, nudged)}
+    got = {name: run(prec, pos) for name, (prec, pos) in worlds.items()}
+    horizon = min(done for _, done in got.values())
+    for name, (prec, pos) in worlds.items():  # worlds that went further: again, to the common horizon
+        if got[name][1] != horizon:
+            got[name] = run(prec, pos, horizon)
+    p64, q64 = got["fp64"][0]
+    runs = {k: got[k][0] for k in ("fp32", "split", "chaos_floor")}
 
     def ang(q):
         c = np.abs((q * q64).sum(axis=1))
         return 2.0 * np.arccos(np.clip(c, 0.0, 1.0))
 
-    out = {"steps": steps, "classes": {}}
+    out = {"steps": horizon, "classes": {}}
+    if horizon < steps:
+        out["horizon_note"] = (f"a world outgrew its pair / row capacity after {horizon} of {steps} steps "
+                               "(the stack compresses and candidate pairs multiply); errors at that step")
     for name, idx in body_classes(sc).items():
         row = {"bodies": int(len(idx))}
         for k, (p, q) in runs.items():

@@ -1179,7 +1179,11 @@ class Engine final : public EngineBase {
         if (!f) return DIO_OK;
         DIO_CK(cudaMemsetAsync(&ctr_->error_flags, 0, 4, stream_));
         if (f & kErrBadIndex) return inval("body / row index out of range");
-        if (f & (kErrPairOverflow | kErrRowOverflow | kErrIndexOverflow)) return cap_err("device capacity exceeded");
+        if (f & kErrPairOverflow) return cap_err("device capacity exceeded: more candidate pairs than max_pairs");
+        if (f & kErrRowOverflow) return cap_err("device capacity exceeded: more contact rows than max_contacts");
+        if (f & kErrIndexOverflow)
+            return cap_err("device capacity exceeded: a traversal stack, a tree's pair scratch or a per-body "
+                           "segment sort ran out of room");
         if (f & (kErrEpaFaces | kErrEpaHorizon)) return cap_err("EPA polytope exceeded its shared-memory capacity");
         if (f & kErrTimeout) {
             err = "device wait timed out";
