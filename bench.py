@@ -368,6 +368,8 @@ def error_study(sc, o, steps, cap, cpp, tuned):
     worlds = {"fp64": (2, None), "fp32": (0, None), "split": (1, None), "chaos_floor": (2, nudged)}
     got = {name: run(prec, pos) for name, (prec, pos) in worlds.items()}
     horizon = min(done for _, done in got.values())
+    if horizon == 0:
+        return {"steps": 0, "horizon_note": "a world outgrew its pair / row capacity within the first 25 steps"}
     for name, (prec, pos) in worlds.items():  # worlds that went further: again, to the common horizon
         if got[name][1] != horizon:
             got[name] = run(prec, pos, horizon)
