@@ -357,7 +357,7 @@ def error_study(sc, o, steps, cap, cpp, tuned):
             try:
                 w.step(o, k)
             except abi.DioError as e:
-                if e.status != abi.DIO_ERR_CAPACITY or horizon is not None:
+                if e.status not in (abi.DIO_ERR_CAPACITY, abi.DIO_ERR_NONFINITE) or horizon is not None:
                     raise
                 break
             done += k
@@ -369,7 +369,7 @@ def error_study(sc, o, steps, cap, cpp, tuned):
     got = {name: run(prec, pos) for name, (prec, pos) in worlds.items()}
     horizon = min(done for _, done in got.values())
     if horizon == 0:
-        return {"steps": 0, "horizon_note": "a world outgrew its pair / row capacity within the first 25 steps"}
+        return {"steps": 0, "horizon_note": "a world outgrew its capacity or went non-finite within 25 steps"}
     for name, (prec, pos) in worlds.items():  # worlds that went further: again, to the common horizon
         if got[name][1] != horizon:
             got[name] = run(prec, pos, horizon)
@@ -382,8 +382,8 @@ def error_study(sc, o, steps, cap, cpp, tuned):
 
     out = {"steps": horizon, "classes": {}}
     if horizon < steps:
-        out["horizon_note"] = (f"a world outgrew its pair / row capacity after {horizon} of {steps} steps "
-                               "(the stack compresses and candidate pairs multiply); errors at that step")
+        out["horizon_note"] = (f"a world outgrew its pair / row capacity or went non-finite after {horizon} of "
+                               f"{steps} steps (the stack compresses, candidate pairs multiply); errors at that step")
     for name, idx in body_classes(sc).items():
         row = {"bodies": int(len(idx))}
         for k, (p, q) in runs.items():
