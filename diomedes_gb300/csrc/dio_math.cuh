@@ -120,15 +120,24 @@ DIO_HD Q4<R> quat_step(Q4<R> q, V3<R> d) {
 // quat_step of the split mode: the increment (d, 0) * q / 2 is formed in R
 // from the rounded quaternion and added to the P quaternion; 1/|q| is seeded
 // in R (correctly rounded sqrt and division) and refined by one Newton step
-// in P (relative error ~1e-14; the quaternion is renormalised every step).
+// in P (relative error ~1e-14; the quaternion is renormalised every step),
+// or taken in P when |u|^2 lies outside [1e-30, 1e30].
 template <class P, class R>
 DIO_HD Q4<P> quat_step_split(Q4<P> q, V3<R> d) {
     Q4<R> s = qmul(Q4<R>{d.x, d.y, d.z, R(0)}, castq<R>(q));
     s = {s.x * R(0.5), s.y * R(0.5), s.z * R(0.5), s.w * R(0.5)};
     const Q4<P> u{q.x + P(s.x), q.y + P(s.y), q.z + P(s.z), q.w + P(s.w)};
     const P n = u.x * u.x + u.y * u.y + u.z * u.z + u.w * u.w;
-    P r = P(R(1) / dsqrt(R(n)));
-    r = r * (P(1.5) - P(0.5) * n * r * r);
+    // an R seed only where n and its root stay well inside R's range; a
+    // quaternion blown up by a huge increment (|u|^2 beyond R) is normalised
+    // in P (an R seed would overflow to a zero quaternion, then NaN)
+    P r;
+    if (n > P(1.0e-30) && n < P(1.0e30)) {
+        r = P(R(1) / dsqrt(R(n)));
+        r = r * (P(1.5) - P(0.5) * n * r * r);
+    } else {
+        r = P(1) / dsqrt(n);
+    }
     return {u.x * r, u.y * r, u.z * r, u.w * r};
 }
 // ang_diff, engine/gpu_physics/avbd/src/lib.rs:96-99
