@@ -561,6 +561,10 @@ __device__ bool epa_warp(EpaSmem<R>& S, const NB<R>& a, const NB<R>& b, const A4
         __syncwarp();
     }
     for (int it = 0; it < 64; ++it) {
+        // no face of nonzero area (a flat or collapsed simplex): no contact,
+        // where the reference would emit its zero default face (a zero normal
+        // at zero depth, whose tangents are NaN)
+        if (nf == 0) return false;  // warp-uniform
         // closest face: first minimum in index order (strict <)
         uint32_t mi = 0;
         {

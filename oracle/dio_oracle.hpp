@@ -835,6 +835,11 @@ inline bool epa(const NBody<R>& a, const NBody<R>& b, const Simplex<R>& s, const
     static thread_local std::vector<uint32_t> visible;
     static thread_local std::vector<std::pair<uint32_t, uint32_t>> horizon;
     for (int it = 0; it < 64; ++it) {
+        // no face of nonzero area (a flat or collapsed simplex): no contact.
+        // The reference would take its zero default face here and emit a
+        // zero normal at zero depth (epa.rs:44-66,102-123), whose tangents
+        // are NaN -- a deliberate difference.
+        if (poly.nf == 0) return false;
         uint32_t mi = 0;
         R md = poly.f[0].distance;
         for (uint32_t i = 1; i < poly.nf; ++i)
