@@ -565,6 +565,12 @@ class Engine final : public EngineBase {
         DIO_CK(cudaFuncSetAttribute(k_solve_chunks<P, R, kChunkThreadsWide>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)chunk_smem_bytes<P>(solve_chunk_cap<P>())));
+        DIO_CK(cudaFuncSetAttribute(k_solve_chunks_colored<P, R, kChunkThreads>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)chunk_colored_smem_bytes<P>(solve_chunk_cap<P>())));
+        DIO_CK(cudaFuncSetAttribute(k_solve_chunks_colored<P, R, kChunkThreadsWide>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)chunk_colored_smem_bytes<P>(solve_chunk_cap<P>())));
         return DIO_OK;
     }
     // largest scene, and the chunks of consecutive scenes (each of at most
@@ -994,7 +1000,7 @@ class Engine final : public EngineBase {
             lag_primed_ = false;
         }
         for (uint32_t k = 0; k < steps; ++k) {
-            if (cfg_.solver_mode == DIO_SOLVER_COLORED)
+            if (cfg_.solver_mode == DIO_SOLVER_COLORED && !use_chunk_solve())
                 DIO_TRY(step_once_colored(*options));
             else if (cfg_.use_graph)
                 DIO_TRY(step_graph(*options));
@@ -1185,6 +1191,7 @@ class Engine final : public EngineBase {
             return cap_err("device capacity exceeded: a traversal stack, a tree's pair scratch or a per-body "
                            "segment sort ran out of room");
         if (f & (kErrEpaFaces | kErrEpaHorizon)) return cap_err("EPA polytope exceeded its shared-memory capacity");
+        if (f & kErrColorOverflow) return cap_err("colouring needed more than 256 colours or did not converge");
         if (f & kErrTimeout) {
             err = "device wait timed out";
             return DIO_ERR_TIMEOUT;
@@ -1297,15 +1304,27 @@ class Engine final : public EngineBase {
         return true;
     }
     // the whole solve of a world step as one launch (k_solve_chunks)
-    bool use_chunk_solve() const {
-        return chunk_world_ && cfg_.batched_solver == DIO_SOLVE_AUTO && cfg_.solver_mode == DIO_SOLVER_JACOBI;
-    }
+    bool use_chunk_solve() const { return chunk_world_ && cfg_.batched_solver == DIO_SOLVE_AUTO; }
     int solve_chunks(const SolveParams<R>& o) {
         const uint32_t cap = solve_chunk_max_;  // shared memory sized to the largest chunk
         cudaEvent_t e0 = span_begin();
         const int grid = (int)solve_chunks_host_.size();
+        const bool wide = cfg_.block_size == (uint32_t)kChunkThreadsWide;
+        if (cfg_.solver_mode == DIO_SOLVER_COLORED) {
+            // the coloured Gauss-Seidel schedule, colouring included
+            const size_t cs = chunk_colored_smem_bytes<P>(cap);
+            if (wide)
+                DIO_CK(launch_k(pdl(), k_solve_chunks_colored<P, R, kChunkThreadsWide>, grid, kChunkThreadsWide, cs,
+                                stream_, w_, (const uint2*)solve_chunks_, (const uint2*)chunk_dyn_, scenes_, cap, o));
+            else
+                DIO_CK(launch_k(pdl(), k_solve_chunks_colored<P, R, kChunkThreads>, grid, kChunkThreads, cs,
+                                stream_, w_, (const uint2*)solve_chunks_, (const uint2*)chunk_dyn_, scenes_, cap, o));
+            span_end(e0, 6);
+            ++launches_;
+            return DIO_OK;
+        }
         const size_t smem = chunk_smem_bytes<P>(cap);
-        if (cfg_.block_size == (uint32_t)kChunkThreadsWide)
+        if (wide)
             DIO_CK(launch_k(pdl(), k_solve_chunks<P, R, kChunkThreadsWide>, grid, kChunkThreadsWide, smem, stream_, w_,
                             (const uint2*)solve_chunks_, (const uint2*)chunk_dyn_, scenes_, cap, o));
         else

@@ -29,6 +29,7 @@
 #pragma once
 
 #include "k_avbd.cuh"
+#include "k_color.cuh"
 
 namespace dio {
 
@@ -141,6 +142,158 @@ __global__ void __launch_bounds__(T, 1)
         recover_body_f(w, i, fr, o);
         w.pos[0][i] = s_pos[final_buf * cap + i - lo];
         w.rot[0][i] = s_rot[final_buf * cap + i - lo];
+    }
+}
+
+// ---------------------------------------------------------------------
+// The coloured Gauss-Seidel schedule as one launch per step: each chunk
+// colours its own dynamic bodies (the Jones-Plassmann rounds of k_color.cuh
+// -- priority hash(index), ties by index, smallest colour free among the
+// coloured neighbours -- with the colours in shared memory and a barrier
+// between a round's selection and its assignment), sorts them by colour,
+// then runs init, per iteration one in-place primal sweep per colour
+// (barrier after each) and the dual, and recover.  One pose buffer (the
+// sweeps are in place): 4 x A4<P> per body plus colour, order and selection
+// arrays.  The colouring of a disconnected graph is the union of its
+// components' colourings, so per-chunk rounds give the colours of the
+// whole-world rounds; results equal the host-driven coloured step bit for
+// bit.
+
+template <class P>
+__host__ __device__ constexpr size_t chunk_colored_smem_bytes(uint32_t cap) {
+    return (size_t)4 * cap * sizeof(A4<P>) + (size_t)cap * (4 + 4 + 4) + (size_t)2 * (kMaxColors + 1) * 4;
+}
+
+constexpr uint32_t kChunkColorRounds = 4096;  // Jones-Plassmann rounds before giving up
+
+template <class P, class R, int T>
+__global__ void __launch_bounds__(T, 1)
+    k_solve_chunks_colored(DevWorld<P, R> w, const uint2* chunks, const uint2* dyn_runs, const SceneDesc* scenes,
+                           uint32_t cap, SolveParams<R> o) {
+    extern __shared__ __align__(16) unsigned char chunk_smem[];
+    __shared__ uint32_t s_rows[4];
+    __shared__ uint32_t s_colored, s_ncolors;
+    pdl_enter();
+    A4<P>* const s_pos = reinterpret_cast<A4<P>*>(chunk_smem);
+    A4<P>* const s_rot = s_pos + cap;
+    A4<P>* const s_ipos = s_pos + 2 * cap;
+    A4<P>* const s_irot = s_pos + 3 * cap;
+    uint32_t* const s_color = reinterpret_cast<uint32_t*>(s_pos + 4 * cap);
+    uint32_t* const s_order = s_color + cap;
+    uint32_t* const s_sel = s_order + cap;
+    uint32_t* const s_cstart = s_sel + cap;          // kMaxColors + 1
+    uint32_t* const s_cursor = s_cstart + kMaxColors + 1;
+    const uint2 ch = chunks[blockIdx.x];
+    const uint2 dr = dyn_runs[blockIdx.x];
+    const uint32_t lo = scenes[ch.x].body_lo, hi = scenes[ch.y - 1].body_hi;
+    const uint32_t tid = threadIdx.x, nt = blockDim.x;
+    const uint32_t warp = tid >> 5;
+    if (warp < 4) {
+        const uint32_t m = w.ctr->rows;
+        const uint32_t split = min(w.ctr->pair_rows, m);
+        const uint32_t s0 = warp < 2 ? 0u : split, s1 = warp < 2 ? split : m;
+        const uint32_t r = warp_lower_bound(w.ab, s0, s1, (warp & 1) ? hi : lo);
+        if ((tid & 31) == 0) s_rows[warp] = r;
+    }
+    if (tid == 0) {
+        s_colored = 0;
+        s_ncolors = 0;
+    }
+    for (uint32_t c = tid; c <= kMaxColors; c += nt) {
+        s_cstart[c] = 0;
+        s_cursor[c] = 0;
+    }
+    // init (the in-place schedule reads and writes buffer 0) and colours reset
+    for (uint32_t i = lo + tid; i < hi; i += nt) {
+        init_body(w, i, o);
+        s_pos[i - lo] = w.pos[0][i];
+        s_rot[i - lo] = w.rot[0][i];
+        s_ipos[i - lo] = w.init_pos[i];
+        s_irot[i - lo] = w.init_rot[i];
+        s_color[i - lo] = kNoColor;
+    }
+    __syncthreads();
+    // Jones-Plassmann rounds over the chunk's dynamic bodies
+    const uint32_t ndyn = dr.y - dr.x;
+    uint32_t rounds = 0;
+    while (s_colored < ndyn) {
+        if (++rounds > kChunkColorRounds) {
+            if (tid == 0) atomicOr(&w.ctr->error_flags, kErrColorOverflow);
+            break;
+        }
+        for (uint32_t t = dr.x + tid; t < dr.y; t += nt) {
+            const uint32_t v = w.dyn_list[t];
+            bool sel = false;
+            if (s_color[v - lo] == kNoColor) {
+                sel = true;
+                for_each_neighbour(w, v, [&](uint32_t u) {
+                    if (sel && s_color[u - lo] == kNoColor && !color_beats(v, u)) sel = false;
+                });
+            }
+            s_sel[v - lo] = sel ? 1u : 0u;
+        }
+        __syncthreads();
+        for (uint32_t t = dr.x + tid; t < dr.y; t += nt) {
+            const uint32_t v = w.dyn_list[t];
+            if (!s_sel[v - lo]) continue;
+            unsigned long long used[kMaxColors / 64] = {0ull, 0ull, 0ull, 0ull};
+            for_each_neighbour(w, v, [&](uint32_t u) {
+                const uint32_t c = s_color[u - lo];
+                if (c < kMaxColors) used[c >> 6] |= 1ull << (c & 63);
+            });
+            uint32_t c = kMaxColors;
+            for (uint32_t q = 0; q < kMaxColors / 64; ++q)
+                if (~used[q]) {
+                    c = q * 64 + (__ffsll(~used[q]) - 1);
+                    break;
+                }
+            if (c >= kMaxColors) {
+                atomicOr(&w.ctr->error_flags, kErrColorOverflow);
+                c = kMaxColors - 1;
+            }
+            s_color[v - lo] = c;
+            atomicAdd(&s_colored, 1u);
+            atomicMax(&s_ncolors, c + 1);
+        }
+        __syncthreads();
+    }
+    const uint32_t ncolors = s_ncolors;
+    // colours out, and the chunk's dynamic bodies sorted by colour
+    for (uint32_t i = lo + tid; i < hi; i += nt) w.color[i] = s_color[i - lo];
+    if (tid == 0) atomicMax(&w.ctr->colors, ncolors);
+    for (uint32_t t = dr.x + tid; t < dr.y; t += nt) {
+        const uint32_t c = s_color[w.dyn_list[t] - lo];
+        if (c < kMaxColors) atomicAdd(&s_cstart[c + 1], 1u);
+    }
+    __syncthreads();
+    if (tid == 0)
+        for (uint32_t c = 0; c < ncolors; ++c) s_cstart[c + 1] += s_cstart[c];
+    __syncthreads();
+    for (uint32_t t = dr.x + tid; t < dr.y; t += nt) {
+        const uint32_t v = w.dyn_list[t];
+        const uint32_t c = s_color[v - lo];
+        if (c < kMaxColors) s_order[s_cstart[c] + atomicAdd(&s_cursor[c], 1u)] = v;
+    }
+    __syncthreads();
+    const uint32_t p0 = s_rows[0], p1 = s_rows[1], c0 = s_rows[2], c1 = s_rows[3];
+    const uint32_t np = p1 - p0, nrows = np + (c1 - c0);
+    const SmemFetch<P> f{s_pos, s_rot, s_ipos, s_irot, s_pos, s_rot, lo};  // in place
+    for (uint32_t k = 0; k < o.iterations; ++k) {
+        for (uint32_t c = 0; c < ncolors; ++c) {
+            for (uint32_t t = s_cstart[c] + tid; t < s_cstart[c + 1]; t += nt) {
+                const uint32_t i = s_order[t];
+                const uint32_t k0 = w.n_joints ? w.joint_off[i] : 0u, k1 = w.n_joints ? w.joint_off[i + 1] : 0u;
+                primal_body_f(w, i, k0, k1, o, f);
+            }
+            __syncthreads();
+        }
+        for (uint32_t t = tid; t < nrows; t += nt) dual_row_f(w, t < np ? p0 + t : c0 + (t - np), f, o);
+        __syncthreads();
+    }
+    for (uint32_t i = lo + tid; i < hi; i += nt) {
+        recover_body_f(w, i, f, o);
+        w.pos[0][i] = s_pos[i - lo];
+        w.rot[0][i] = s_rot[i - lo];
     }
 }
 

@@ -397,6 +397,7 @@ static __global__ void k_roll_counters(Counters* c, uint32_t* zero0, uint32_t* z
     c->gjk_work = 0;
     c->epa_work = 0;
     c->long_count = 0;
+    c->colors = 0;
 }
 
 template <class P, class R>
