@@ -550,33 +550,34 @@ def main():
                                            for k in ("broad", "narrow", "rows", "solve", "primal", "dual")}}
 
     # end to end through the public API with host buffers: the demos'
-    # per-frame loop (upload poses + state, step, read them back)
+    # per-frame loop (upload poses + velocities, step, read them back), with
+    # the 64-byte motion records (shapes, masses and joints stay on the
+    # device); the same loop with the full body + state records beside it
     e2e = None
     if not args.no_e2e:
         w.resume(state_after)
-        # the caller's host arrays: page-locked (cudaHostAlloc through torch)
-        hb = torch.empty(sc.n * sc.bodies.dtype.itemsize, dtype=torch.uint8,
-                         pin_memory=True).numpy().view(sc.bodies.dtype)
-        hs = torch.empty(sc.n * sc.state.dtype.itemsize, dtype=torch.uint8,
-                         pin_memory=True).numpy().view(sc.state.dtype)
-        w.download_into(hb, hs)
+
+        def pinned(dtype, count):  # the caller's page-locked host array (cudaHostAlloc through torch)
+            return torch.empty(count * dtype.itemsize, dtype=torch.uint8, pin_memory=True).numpy().view(dtype)
+
+        hm = pinned(abi.MOTION, sc.n)
+        w.download_motion_into(hm)
         k2 = max(3, args.steps // 2)
-        # (1) the batch as one world: set_state, dio_step, download in series
+        # (1) the batch as one world: set_motion, dio_step, download_motion in series
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(k2):
-            w.set_state(hb, hs)
+            w.set_motion(hm)
             w.step(o, 1)
-            w.download_into(hb, hs)
+            w.download_motion_into(hm)
         t1 = time.perf_counter()
         single = sc.n * k2 / (t1 - t0)
         # (2) the same batch as G worlds (contiguous runs of whole scenes) on
-        # G streams, stepped by dio_worlds_step_host: one world's host copies
-        # overlap the other worlds' steps
-        piped, parts = 0.0, [sc]
+        # G streams: one world's host copies overlap the other worlds' steps
+        piped, piped_full, parts = 0.0, 0.0, [sc]
         if sc.n_scenes > 1:
             parts, starts = sc.split(args.e2e_worlds)
-            worlds, streams, vb, vs = [], [], [], []
+            worlds, streams = [], []
             for p, lo in zip(parts, starts):
                 wg = compute.World(world_capacity(p, per_body), profile=0, precision=prec, contacts_per_pair=cpp)
                 streams.append(torch.cuda.Stream())
@@ -584,22 +585,36 @@ def main():
                 wg.upload(p.bodies, p.state, **p.upload_kwargs())
                 wg.configure(**tuned)
                 worlds.append(wg)
-                vb.append(hb[lo:lo + p.n])
-                vs.append(hs[lo:lo + p.n])
-            compute.step_host(worlds, vb, vs, o, args.warmup)  # from the state reached above
+            vm = [hm[lo:lo + p.n] for p, lo in zip(parts, starts)]
+            compute.step_motion_host(worlds, vm, o, args.warmup)  # from the state reached above
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            compute.step_motion_host(worlds, vm, o, k2)
+            t1 = time.perf_counter()
+            piped = sc.n * k2 / (t1 - t0)
+            # (3) the full GpuBody + GpuAvbdBodyState records (192 B per body each way)
+            hb, hs = pinned(sc.bodies.dtype, sc.n), pinned(sc.state.dtype, sc.n)
+            worlds[0].download_into(hb[:parts[0].n], hs[:parts[0].n])
+            for wg, p, lo in zip(worlds[1:], parts[1:], starts[1:]):
+                wg.download_into(hb[lo:lo + p.n], hs[lo:lo + p.n])
+            vb = [hb[lo:lo + p.n] for p, lo in zip(parts, starts)]
+            vs = [hs[lo:lo + p.n] for p, lo in zip(parts, starts)]
+            compute.step_host(worlds, vb, vs, o, 2)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             compute.step_host(worlds, vb, vs, o, k2)
             t1 = time.perf_counter()
-            piped = sc.n * k2 / (t1 - t0)
+            piped_full = sc.n * k2 / (t1 - t0)
             for wg in worlds:
                 wg.close()
         t_ms = 1e3 * sc.n * k2 / max(piped, single)  # this rank's time for its share
         t_max, units = dio_dist.frame(dist, t_ms, sc.n * k2, device="cuda")
         e2e = {"value": units / (t_max / 1e3), "unit": "body-steps/s",
-               "h2d_bytes_per_step": int(hb.nbytes + hs.nbytes), "d2h_bytes_per_step": int(hb.nbytes + hs.nbytes),
-               "steps": k2, "worlds": len(parts) if piped >= single else 1,
-               "one_world": single, "worlds_on_streams": {"worlds": len(parts), "value": piped}}
+               "h2d_bytes_per_step": int(hm.nbytes), "d2h_bytes_per_step": int(hm.nbytes),
+               "records": "DioBodyMotion, 64 B per body each way", "steps": k2,
+               "worlds": len(parts) if piped >= single else 1, "one_world": single,
+               "worlds_on_streams": {"worlds": len(parts), "value": piped},
+               "full_records_worlds_on_streams": {"value": piped_full, "bytes_per_step_each_way": 192 * sc.n}}
 
     # plain path: one context per scene, stepped one scene at a time
     plain = None

@@ -45,6 +45,9 @@ PREC_F32, PREC_SPLIT, PREC_F64 = 0, 1, 2
 # ------------------------------------------------------------ record dtypes
 SHAPE = np.dtype([("tag", "<u4"), ("pad", "<u4", 3), ("corners", "<f4", (4, 4))])
 BODY = np.dtype([("position", "<f4", 4), ("orientation", "<f4", 4), ("shape", SHAPE)])
+# DioBodyMotion: the per-frame pose and velocities of a body (64 B)
+MOTION = np.dtype([("position", "<f4", 3), ("orientation", "<f4", 4), ("velocity", "<f4", 3),
+                   ("angular_velocity", "<f4", 3), ("prev_velocity", "<f4", 3)])
 PAIR = np.dtype([("a", "<u4"), ("b", "<u4")])
 CONTACT_OUT = np.dtype([("valid", "<u4"), ("a", "<u4"), ("b", "<u4"), ("pad", "<u4"),
                         ("normal", "<f4", 4), ("depth", "<f4"), ("pad2", "<f4", 3),
@@ -156,6 +159,11 @@ _PROTOS = {
     "dio_world_download_async": [_P, _vp, _vp],
     "dio_worlds_step_host": [ctypes.POINTER(_P), _u32, ctypes.POINTER(_vp), ctypes.POINTER(_vp),
                              ctypes.POINTER(AvbdOptions), _u32],
+    "dio_world_set_motion": [_P, _vp],
+    "dio_world_download_motion": [_P, _vp],
+    "dio_world_download_motion_async": [_P, _vp],
+    "dio_worlds_step_motion_host": [ctypes.POINTER(_P), _u32, ctypes.POINTER(_vp), ctypes.POINTER(AvbdOptions),
+                                    _u32],
     "dio_world_checkpoint": [_P, _vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)],
     "dio_world_resume": [_P, _vp, ctypes.c_size_t],
     "dio_autotune": [_P, ctypes.POINTER(AvbdOptions), _u32, ctypes.c_char_p, ctypes.POINTER(Config)],

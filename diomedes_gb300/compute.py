@@ -202,6 +202,26 @@ class AvbdCompute(Context):
         return out[: m.value].copy(), offsets, indices[: offsets[-1]].copy()
 
 
+def step_motion_host(worlds, motions, options, steps=1):
+    """dio_worlds_step_motion_host: the per-frame loop with motion records
+    (abi.MOTION) over a batch held as several worlds (one per stream);
+    motions[g] is world g's host array (page-locked for overlapped copies),
+    updated in place; returns after every world has finished."""
+    n = len(worlds)
+    if len(motions) != n:
+        raise ValueError("one motion array per world")
+    for g in range(n):
+        m = motions[g]
+        if len(m) != worlds[g].n or m.dtype != abi.MOTION or not m.flags.c_contiguous:
+            raise ValueError(f"world {g}: motion must be {worlds[g].n} contiguous abi.MOTION records")
+    hs = (ctypes.c_void_p * n)(*[w.h for w in worlds])
+    ms = (ctypes.c_void_p * n)(*[ptr(m) for m in motions])
+    rc = abi.lib().dio_worlds_step_motion_host(hs, n, ms, ctypes.byref(options), steps)
+    if rc != abi.DIO_OK:
+        failed = next((w.h for w in worlds if abi.lib().dio_ctx_last_error(w.h)), None)
+        check(rc, failed, "dio_worlds_step_motion_host")
+
+
 def step_host(worlds, bodies, states, options, steps=1):
     """dio_worlds_step_host: the per-frame upload / step / read-back loop over
     a batch held as several worlds (one per stream).  bodies[g] / states[g]
@@ -299,6 +319,23 @@ class World(Context):
         b = None if bodies is None else np.ascontiguousarray(bodies, abi.BODY)
         s = None if state is None else np.ascontiguousarray(state, abi.BODY_STATE)
         check(self.L.dio_world_set_state(self.h, ptr(b), ptr(s)), self.h, "set_state")
+
+    def set_motion(self, motion):
+        """dio_world_set_motion: poses and velocities (abi.MOTION records)."""
+        m = np.ascontiguousarray(motion, abi.MOTION)
+        if len(m) != self.n:
+            raise ValueError(f"motion records must hold {self.n} bodies")
+        check(self.L.dio_world_set_motion(self.h, ptr(m)), self.h, "set_motion")
+
+    def download_motion_into(self, motion):
+        if len(motion) != self.n or motion.dtype != abi.MOTION or not motion.flags.c_contiguous:
+            raise ValueError(f"motion records must be {self.n} contiguous abi.MOTION records")
+        check(self.L.dio_world_download_motion(self.h, ptr(motion)), self.h, "download_motion")
+
+    def download_motion(self):
+        m = np.zeros(self.n, abi.MOTION)
+        self.download_motion_into(m)
+        return m
 
     def download_into(self, bodies, state):
         check(self.L.dio_world_download(self.h, ptr(bodies), ptr(state)), self.h, "download")

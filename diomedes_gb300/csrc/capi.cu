@@ -306,6 +306,41 @@ int dio_worlds_step_host(DioCtx* const* ctxs, uint32_t count, DioGpuBody* const*
     }
     return rc;
 }
+int dio_world_set_motion(DioCtx* ctx, const DioBodyMotion* motion) {
+    if (!motion) return fail(ctx, DIO_ERR_INVALID, "null motion records");
+    return with_world(ctx, false, [&](dio::EngineBase* e) { return e->set_motion(motion); });
+}
+int dio_world_download_motion_async(DioCtx* ctx, DioBodyMotion* motion) {
+    if (!motion) return fail(ctx, DIO_ERR_INVALID, "null motion records");
+    return with_world(ctx, false, [&](dio::EngineBase* e) { return e->download_motion_async(motion); });
+}
+int dio_world_download_motion(DioCtx* ctx, DioBodyMotion* motion) {
+    int rc = dio_world_download_motion_async(ctx, motion);
+    if (rc) return rc;
+    return dio_ctx_synchronize(ctx);
+}
+int dio_worlds_step_motion_host(DioCtx* const* ctxs, uint32_t count, DioBodyMotion* const* motions,
+                                const DioAvbdOptions* options, uint32_t steps) {
+    if (!count) return DIO_OK;
+    if (!ctxs || !motions || !options) return DIO_ERR_INVALID;
+    for (uint32_t g = 0; g < count; ++g)
+        if (!ctxs[g] || !motions[g]) return DIO_ERR_INVALID;
+    int rc = DIO_OK;
+    // each world's chain (upload, step, read-back) is stream-ordered; the
+    // worlds' chains are queued in turn, so one world's copies run beside
+    // another world's step, and nothing waits on the host inside a step
+    for (uint32_t k = 0; k < steps && !rc; ++k)
+        for (uint32_t g = 0; g < count && !rc; ++g) {
+            rc = dio_world_set_motion(ctxs[g], motions[g]);
+            if (!rc) rc = dio_step_async(ctxs[g], options, 1);
+            if (!rc) rc = dio_world_download_motion_async(ctxs[g], motions[g]);
+        }
+    for (uint32_t g = 0; g < count; ++g) {
+        int s = dio_ctx_synchronize(ctxs[g]);
+        if (!rc) rc = s;
+    }
+    return rc;
+}
 int dio_world_download_f64(DioCtx* ctx, double* positions, double* orientations) {
     return with_world(ctx, false, [&](dio::EngineBase* e) { return e->download_f64(positions, orientations); });
 }

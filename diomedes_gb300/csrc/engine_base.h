@@ -44,6 +44,10 @@ struct EngineBase {
     // rebuilds the dynamic-body list if the set changed
     virtual int set_state_begin(const DioGpuBody* bodies, const DioBodyState* state) = 0;
     virtual int set_state_end() = 0;
+    // per-frame pose and velocity records (DioBodyMotion): upload, and the
+    // enqueued read-back
+    virtual int set_motion(const DioBodyMotion* motion) = 0;
+    virtual int download_motion_async(DioBodyMotion* motion) = 0;
     virtual int download(DioGpuBody* bodies, DioBodyState* state) = 0;
     virtual int download_f64(double* positions, double* orientations) = 0;
     virtual int contacts(DioContact* out, uint32_t cap, uint32_t* m) = 0;

@@ -92,6 +92,33 @@ __global__ void k_unpack_pose_f64(DevWorld<P, R> w, const double* pos3, const do
     }
 }
 
+// DioBodyMotion records in / out (pose and velocities)
+template <class P, class R>
+__global__ void k_unpack_motion(DevWorld<P, R> w, const DioBodyMotion* m, uint32_t n) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const DioBodyMotion r = m[i];
+        w.pos[0][i] = A4<P>{P(r.position[0]), P(r.position[1]), P(r.position[2]), P(0)};
+        w.rot[0][i] = A4<P>{P(r.orientation[0]), P(r.orientation[1]), P(r.orientation[2]), P(r.orientation[3])};
+        w.vel[i] = A4<P>{P(r.velocity[0]), P(r.velocity[1]), P(r.velocity[2]), P(0)};
+        w.ang[i] = A4<P>{P(r.angular_velocity[0]), P(r.angular_velocity[1]), P(r.angular_velocity[2]), P(0)};
+        w.prev_vel[i] = A4<P>{P(r.prev_velocity[0]), P(r.prev_velocity[1]), P(r.prev_velocity[2]), P(0)};
+    }
+}
+template <class P, class R>
+__global__ void k_pack_motion(DevWorld<P, R> w, DioBodyMotion* m, uint32_t n) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const A4<P> p = w.pos[0][i], q = w.rot[0][i], v = w.vel[i], a = w.ang[i], pv = w.prev_vel[i];
+        DioBodyMotion r;
+        r.position[0] = float(p.x), r.position[1] = float(p.y), r.position[2] = float(p.z);
+        r.orientation[0] = float(q.x), r.orientation[1] = float(q.y), r.orientation[2] = float(q.z);
+        r.orientation[3] = float(q.w);
+        r.velocity[0] = float(v.x), r.velocity[1] = float(v.y), r.velocity[2] = float(v.z);
+        r.angular_velocity[0] = float(a.x), r.angular_velocity[1] = float(a.y), r.angular_velocity[2] = float(a.z);
+        r.prev_velocity[0] = float(pv.x), r.prev_velocity[1] = float(pv.y), r.prev_velocity[2] = float(pv.z);
+        m[i] = r;
+    }
+}
+
 template <class P, class R>
 __global__ void k_unpack_state(DevWorld<P, R> w, const DioBodyState* st, uint32_t n) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -1051,6 +1078,32 @@ class Engine final : public EngineBase {
             if (!hctr_->dyn_changed) return DIO_OK;
         }
         if (pending) return build_dyn_list(w_.n);
+        return DIO_OK;
+    }
+
+    int set_motion(const DioBodyMotion* motion) override {
+        if (!world_ready_) return state_err("no world uploaded");
+        if (!motion) return inval("null motion records");
+        const uint32_t n = w_.n;
+        if (!n) return DIO_OK;
+        DioBodyMotion* dm = reinterpret_cast<DioBodyMotion*>(dstage_);
+        DIO_CK(cudaMemcpyAsync(dm, motion, (size_t)n * sizeof(DioBodyMotion), cudaMemcpyHostToDevice, stream_));
+        k_unpack_motion<P, R><<<grid_for(n, 256), 256, 0, stream_>>>(w_, dm, n);
+        ++launches_;
+        return DIO_OK;
+    }
+    int download_motion_async(DioBodyMotion* motion) override {
+        if (!world_ready_) return state_err("no world uploaded");
+        if (!motion) return inval("null motion records");
+        const uint32_t n = w_.n;
+        if (!n) return DIO_OK;
+        // staged behind the upload's half of the staging buffer, so a
+        // read-back and the next frame's upload never share bytes
+        DioBodyMotion* dm = reinterpret_cast<DioBodyMotion*>(reinterpret_cast<char*>(dstage_) +
+                                                             align256((size_t)n * sizeof(DioBodyMotion)));
+        k_pack_motion<P, R><<<grid_for(n, 256), 256, 0, stream_>>>(w_, dm, n);
+        ++launches_;
+        DIO_CK(cudaMemcpyAsync(motion, dm, (size_t)n * sizeof(DioBodyMotion), cudaMemcpyDeviceToHost, stream_));
         return DIO_OK;
     }
 

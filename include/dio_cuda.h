@@ -101,6 +101,21 @@ typedef struct DioContactOut {
     float point_b[4];
 } DioContactOut;
 
+/* The part of a body that a frame loop changes and reads back every frame
+ * (64 bytes; extension): its pose and velocities.  Shapes, masses, joints and
+ * containers stay on the device from dio_world_upload, so a frame moves 64 B
+ * per body each way instead of the GpuBody + GpuAvbdBodyState records'
+ * 192 B of AvbdSolver::sync_bodies_from_gpu and the uploads of
+ * demos/avbd_box/src/main.rs:232-257.  Positions are FP32: an FP64 world
+ * (DIO_PREC_SPLIT / DIO_PREC_F64) takes and returns them rounded. */
+typedef struct DioBodyMotion {
+    float position[3];
+    float orientation[4]; /* quaternion x, y, z, w */
+    float velocity[3];
+    float angular_velocity[3];
+    float prev_velocity[3];
+} DioBodyMotion;
+
 /* GpuAvbdBodyState, engine/src/render/gpu_physics.rs:18-26 (80 bytes) */
 typedef struct DioBodyState {
     float vel[4];
@@ -430,6 +445,22 @@ int dio_world_download(DioCtx* ctx, DioGpuBody* bodies, DioBodyState* state);
  * context it came from.  No argument may be NULL; count == 0 is a no-op. */
 int dio_worlds_step_host(DioCtx* const* ctxs, uint32_t count, DioGpuBody* const* bodies,
                          DioBodyState* const* states, const DioAvbdOptions* options, uint32_t steps);
+/* Extension: replace every body's pose and velocities from `motion` (n
+ * records), keeping shapes, masses, joints and the warm-start rows; enqueued
+ * on the context's stream (a page-locked array keeps the copy asynchronous;
+ * leave it unchanged until the stream has passed the copy). */
+int dio_world_set_motion(DioCtx* ctx, const DioBodyMotion* motion);
+/* Extension: read every body's pose and velocities into `motion` (n
+ * records); the _async form returns once the copy is enqueued. */
+int dio_world_download_motion(DioCtx* ctx, DioBodyMotion* motion);
+int dio_world_download_motion_async(DioCtx* ctx, DioBodyMotion* motion);
+/* Extension: dio_worlds_step_host with motion records: per step and world,
+ * dio_world_set_motion, dio_step_async(1), dio_world_download_motion_async,
+ * every world's copy queued before the next world's step; every context is
+ * synchronised before the call returns.  No argument may be NULL; count == 0
+ * is a no-op. */
+int dio_worlds_step_motion_host(DioCtx* const* ctxs, uint32_t count, DioBodyMotion* const* motions,
+                                const DioAvbdOptions* options, uint32_t steps);
 /* FP64 poses (exact in DIO_PREC_SPLIT / DIO_PREC_F64 worlds). */
 int dio_world_download_f64(DioCtx* ctx, double* positions, double* orientations);
 /* The last step's contact rows with their solved lambda / penalty. */

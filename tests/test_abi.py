@@ -101,6 +101,12 @@ def test_bad_arguments_are_rejected_before_any_device_work():
     one = (ctypes.c_void_p * 1)(None)
     assert L.dio_worlds_step_host(one, 1, one, one, ctypes.byref(o), 1) == abi.DIO_ERR_INVALID
     assert L.dio_worlds_step_host(one, 1, one, one, None, 1) == abi.DIO_ERR_INVALID
+    assert L.dio_world_set_motion(None, None) == abi.DIO_ERR_INVALID
+    assert L.dio_world_download_motion(None, None) == abi.DIO_ERR_INVALID
+    assert L.dio_world_download_motion_async(None, None) == abi.DIO_ERR_INVALID
+    assert L.dio_worlds_step_motion_host(None, 0, None, ctypes.byref(o), 1) == abi.DIO_OK
+    assert L.dio_worlds_step_motion_host(one, 1, one, ctypes.byref(o), 1) == abi.DIO_ERR_INVALID
+    assert abi.MOTION.itemsize == 64
 
 
 def test_context_creation_without_a_device_fails_loudly():

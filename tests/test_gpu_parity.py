@@ -744,3 +744,51 @@ def test_colored_world_matches_oracle(batched_solver, use_graph):
         assert np.array_equal(_bits(gs), _bits(rs)), sc.name
         dyn = sc.state["inv_mass"] != 0
         assert _independent(gc, rows, sc.constraints, dyn), sc.name
+
+
+def test_motion_records_round_trip_and_host_loop():
+    """The per-frame motion records (pose and velocities, 64 B per body):
+    a world stepped by dio_world_set_motion / dio_step / dio_world_download_motion
+    equals the world stepped by set_state / dio_step / download; and
+    dio_worlds_step_motion_host over three worlds on three streams gives,
+    frame by frame, the bits of the packed world."""
+    torch = pytest.importorskip("torch")
+    parts = [scenes.pyramid(levels=3), scenes.constraints_demo(), scenes.box_demo(),
+             scenes.mixed_pile(n=120, extent=3.0)]
+    for p in parts:
+        p.options = parts[0].options
+    packed = scenes.pack(parts)
+    frames = 4
+    with _world(packed) as w:
+        b, s = w.download()
+        for _ in range(frames):
+            w.set_state(b, s)
+            w.step(packed.options, 1)
+            b, s = w.download()
+    with _world(packed) as w:
+        m = w.download_motion()
+        assert np.array_equal(m["position"], packed.bodies["position"][:, :3])
+        for _ in range(frames):
+            w.set_motion(m)
+            w.step(packed.options, 1)
+            m = w.download_motion()
+        gb, gs = w.download()
+    assert np.array_equal(_bits(gb), _bits(b)) and np.array_equal(_bits(gs), _bits(s))
+    assert np.array_equal(m["position"], b["position"][:, :3]) and np.array_equal(m["orientation"], b["orientation"])
+    assert np.array_equal(m["velocity"], s["vel"][:, :3]) and np.array_equal(m["prev_velocity"], s["prev_vel"][:, :3])
+    groups, starts = packed.split(3)
+    hm = torch.empty(packed.n * abi.MOTION.itemsize, dtype=torch.uint8, pin_memory=True).numpy().view(abi.MOTION)
+    with _world(packed) as w0:
+        hm[:] = w0.download_motion()
+    streams = [torch.cuda.Stream() for _ in groups]
+    worlds = [_world(g) for g in groups]
+    try:
+        for wg, st in zip(worlds, streams):
+            wg.set_stream(st.cuda_stream)
+        views = [hm[lo:lo + g.n] for g, lo in zip(groups, starts)]
+        compute.step_motion_host(worlds, views, packed.options, frames)
+        assert np.array_equal(hm["position"], b["position"][:, :3])
+        assert np.array_equal(hm["angular_velocity"], s["ang"][:, :3])
+    finally:
+        for wg in worlds:
+            wg.close()
