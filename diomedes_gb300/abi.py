@@ -119,7 +119,7 @@ class StepStats(ctypes.Structure):
                 ("solve_ms", ctypes.c_double), ("chunk_launches", _u32), ("pad", _u32), ("chunk_ms", ctypes.c_double)]
 
 
-# every symbol include/dio_cuda.h declares, with its argument types
+# every symbol include/*.h declares, with its argument types
 _P = _vp
 _PROTOS = {
     "dio_ctx_create": [ctypes.POINTER(Capacity), ctypes.POINTER(_vp)],
@@ -167,6 +167,10 @@ _PROTOS = {
     "dio_world_checkpoint": [_P, _vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)],
     "dio_world_resume": [_P, _vp, ctypes.c_size_t],
     "dio_autotune": [_P, ctypes.POINTER(AvbdOptions), _u32, ctypes.c_char_p, ctypes.POINTER(Config)],
+    # include/dio_selftest.h: the device prefix sum and radix sort on host arrays
+    "dio_selftest_scan": [_vp, _vp, _u32, _u32, _u32, ctypes.POINTER(_u32)],
+    "dio_selftest_sort_u32": [_vp, _vp, _u32, _u32, _u32, _vp, _vp],
+    "dio_selftest_sort_u64": [_vp, _vp, _u32, _u32, _u32, _vp, _vp],
 }
 
 _LIB = None

@@ -404,3 +404,34 @@ class World(Context):
         buf = np.frombuffer(image, np.uint8)
         check(self.L.dio_world_resume(self.h, ptr(buf), buf.size), self.h, "resume")
         self.n = int(checkpoint_header(image)["n"])
+
+
+def device_exclusive_scan(values, repeats=1, live=None, out=None):
+    """Exclusive prefix sum of a uint32 array by the pipeline's device scan
+    (uint32 wrap-around), run `repeats` times on the same buffers.  With
+    `live`, only the first `live` entries are scanned (the count is handed
+    over in device memory); the rest of `out` keeps its contents.  Returns
+    (prefix sums, total of the live entries)."""
+    a = np.ascontiguousarray(values, dtype=np.uint32)
+    res = np.zeros_like(a) if out is None else np.array(out, dtype=np.uint32, copy=True)
+    total = ctypes.c_uint32(0)
+    n_live = a.size if live is None else live
+    check(abi.lib().dio_selftest_scan(ptr(a), ptr(res), a.size, n_live, repeats, ctypes.byref(total)))
+    return res, total.value
+
+
+def device_sort_pairs(keys, values, begin_bit=0, end_bit=None):
+    """Stable sort of (keys, values) by key bits [begin_bit, end_bit) with the
+    pipeline's device radix sort; keys uint32 or uint64, values uint32."""
+    k = np.ascontiguousarray(keys)
+    if k.dtype not in (np.uint32, np.uint64):
+        raise TypeError("keys must be uint32 or uint64")
+    v = np.ascontiguousarray(values, dtype=np.uint32)
+    if v.shape != k.shape:
+        raise ValueError("keys and values differ in length")
+    if end_bit is None:
+        end_bit = 8 * k.dtype.itemsize
+    ko, vo = np.empty_like(k), np.empty_like(v)
+    fn = abi.lib().dio_selftest_sort_u64 if k.dtype == np.uint64 else abi.lib().dio_selftest_sort_u32
+    check(fn(ptr(k), ptr(v), k.size, begin_bit, end_bit, ptr(ko), ptr(vo)))
+    return ko, vo

@@ -203,6 +203,21 @@ __device__ __forceinline__ void pdl_enter() {
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
+// Warp-aggregated append (ballot/popc compaction): the lanes that reach the
+// call together take consecutive slots from *cursor with one atomic, in lane
+// order.  Works on shared or global cursors.
+__device__ __forceinline__ uint32_t warp_append(uint32_t* cursor) {
+    uint32_t lane, lt;
+    asm("mov.u32 %0, %%laneid;" : "=r"(lane));
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+    const uint32_t m = __activemask();
+    const uint32_t leader = (uint32_t)(__ffs(m) - 1);
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(cursor, (uint32_t)__popc(m));
+    base = __shfl_sync(m, base, (int)leader);
+    return base + (uint32_t)__popc(m & lt);
+}
+
 template <typename... KArgs, typename... Args>
 inline cudaError_t launch_k(bool pdl, void (*kern)(KArgs...), int grid, int block, size_t smem, cudaStream_t s,
                             Args&&... args) {
@@ -218,14 +233,5 @@ inline cudaError_t launch_k(bool pdl, void (*kern)(KArgs...), int grid, int bloc
     cfg.numAttrs = pdl ? 1 : 0;
     return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
 }
-
-// ---- launch entry points (explicitly instantiated per precision) ----
-template <class P, class R>
-void launch_aabb(const DevWorld<P, R>& w, uint32_t lo, uint32_t hi, cudaStream_t s);
-template <class P, class R>
-void launch_broad_dense(const DevWorld<P, R>& w, uint32_t lo, uint32_t hi, uint32_t* counts, uint32_t* offsets,
-                        void* scan_tmp, size_t scan_tmp_bytes, cudaStream_t s);
-template <class P, class R>
-void launch_narrow(const DevWorld<P, R>& w, uint32_t pair_lo, uint32_t pair_hi, cudaStream_t s);
 
 }  // namespace dio

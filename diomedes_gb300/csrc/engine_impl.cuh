@@ -3,8 +3,6 @@
 // Included by exactly one translation unit per precision.
 #pragma once
 
-#include <cub/cub.cuh>
-
 #include <algorithm>
 #include <cstddef>
 #include <cstring>
@@ -18,6 +16,7 @@
 #include "k_lbvh.cuh"
 #include "k_narrow_kernels.cuh"
 #include "k_rows.cuh"
+#include "k_scan.cuh"
 
 namespace dio {
 
@@ -545,15 +544,10 @@ class Engine final : public EngineBase {
         DIO_TRY(alloc(&hull_, H));
         DIO_TRY(alloc(&ctr_, 1));
         DIO_CK(cudaMallocHost(&hctr_, sizeof(Counters)));
-        // CUB temporary storage for the largest sort / scan
-        size_t t1 = 0, t2 = 0, t3 = 0;
-        cub::DeviceRadixSort::SortPairs(nullptr, t1, keys_raw_, keys_s_[0], ids_raw_, ids_s_[0], (int)std::max(M, N),
-                                        0, 64, stream_);
-        cub::DeviceRadixSort::SortPairs(nullptr, t2, inc_body_, inc_body_s_, inc_row_, inc_row_s_, (int)INC, 0, 32,
-                                        stream_);
-        cub::DeviceScan::ExclusiveSum(nullptr, t3, counts_, offsets_, (int)CNT, stream_);
-        cub_bytes_ = std::max(t1, std::max(t2, t3)) + 256;
-        DIO_CK(cudaMalloc(&cub_tmp_, cub_bytes_));
+        // prefix sums and radix sorts: up to CNT scanned counts, and sorts of
+        // row keys (M), incidences (INC) and per-body keys (N)
+        DIO_CK(ss_.init((uint32_t)std::max<size_t>(std::max<size_t>(M, N), INC),
+                        (uint32_t)std::max<size_t>(CNT, (size_t)kMaxColors + 2), &ctr_->error_flags, stream_));
         // API staging (device + pinned host)
         stage_bytes_ = (size_t)N * (sizeof(DioGpuBody) + sizeof(DioBodyState) + 64 + 16) + (size_t)M * sizeof(DioContact) +
                        (size_t)J * sizeof(DioConstraint) + ((size_t)N + 1) * 4 + 2ull * M * 4 +
@@ -587,6 +581,8 @@ class Engine final : public EngineBase {
         const int tree_bytes = (int)scene_tree_bytes<R>(scene_tree_cap<R>());
         DIO_CK(cudaFuncSetAttribute(k_scene_tree<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, tree_bytes));
         DIO_CK(cudaFuncSetAttribute(k_scene_tree<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tree_bytes));
+        DIO_CK(cudaFuncSetAttribute(k_chunk_build<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)chunk_build_bytes<R>()));
         DIO_CK(cudaFuncSetAttribute(k_solve_chunks<P, R, kChunkThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)chunk_smem_bytes<P>(solve_chunk_cap<P>())));
         DIO_CK(cudaFuncSetAttribute(k_solve_chunks<P, R, kChunkThreadsWide>,
@@ -1201,11 +1197,11 @@ class Engine final : public EngineBase {
     void release() {
         for (void* p : allocs_) cudaFree(p);
         allocs_.clear();
-        if (cub_tmp_) cudaFree(cub_tmp_);
+        ss_.release();
         if (dstage_) cudaFree(dstage_);
         if (hstage_) cudaFreeHost(hstage_);
         if (hctr_) cudaFreeHost(hctr_);
-        cub_tmp_ = dstage_ = nullptr;
+        dstage_ = nullptr;
         hstage_ = nullptr;
         hctr_ = nullptr;
     }
@@ -1288,8 +1284,7 @@ class Engine final : public EngineBase {
         dyn_list_n_ = n;
         k_dyn_flags<P, R><<<grid_for(n, 256), 256, 0, stream_>>>(w_, n, counts2_, dyn_keep_);
         DIO_CK(cudaMemsetAsync(counts2_ + n, 0, 4, stream_));
-        size_t tb = cub_bytes_;
-        DIO_CK(cub::DeviceScan::ExclusiveSum(cub_tmp_, tb, counts2_, offsets2_, (int)n + 1, stream_));
+        DIO_CK(ss_.scan(counts2_, offsets2_, n + 1, false, stream_));
         k_dyn_fill<<<grid_for(n, 256), 256, 0, stream_>>>(counts2_, offsets2_, n, dyn_list_);
         uint32_t nd = 0;
         DIO_CK(cudaMemcpyAsync(&nd, offsets2_ + n, 4, cudaMemcpyDeviceToHost, stream_));
@@ -1310,10 +1305,8 @@ class Engine final : public EngineBase {
         // solve walks its chunk's run), else by signature alone
         const uint32_t* sch = chunked_scenes_ ? scene_chunk_ : nullptr;
         k_dyn_keys<P, R><<<grid_for(nd, 256), 256, 0, stream_>>>(w_, dyn_list_, nd, sch, counts2_);
-        size_t tb = cub_bytes_;
-        const int end_bit = 7 + (sch ? (int)bits_for(nc) : 0);
-        DIO_CK(cub::DeviceRadixSort::SortPairs(cub_tmp_, tb, counts2_, offsets2_, dyn_list_, dyn_tmp_, (int)nd, 0,
-                                               end_bit, stream_));
+        const uint32_t end_bit = 7u + (sch ? bits_for(nc) : 0u);
+        DIO_CK(ss_.sort_pairs(counts2_, offsets2_, dyn_list_, dyn_tmp_, nd, 0u, end_bit, false, stream_));
         DIO_CK(cudaMemcpyAsync(dyn_list_, dyn_tmp_, (size_t)nd * 4, cudaMemcpyDeviceToDevice, stream_));
         if (sch) k_chunk_dyn_runs<P, R><<<grid_for(nd, 256), 256, 0, stream_>>>(w_, dyn_list_, nd, sch, chunk_dyn_);
         return DIO_OK;
@@ -1396,13 +1389,11 @@ class Engine final : public EngineBase {
         DIO_CK(cudaMemcpyAsync(joints_, cons, (size_t)nj * sizeof(DioConstraint), cudaMemcpyHostToDevice, stream_));
         uint32_t total = 2 * nj;
         k_joint_inc<<<grid_for(nj, 256), 256, 0, stream_>>>(joints_, nj, n, inc_body_, inc_row_, &ctr_->error_flags);
-        size_t tb = cub_bytes_;
-        DIO_CK(cub::DeviceRadixSort::SortPairs(cub_tmp_, tb, inc_body_, inc_body_s_, inc_row_, inc_row_s_, (int)total,
-                                               0, (int)bits_for(n + 1), stream_));
+        DIO_CK(ss_.sort_pairs(inc_body_, inc_body_s_, inc_row_, inc_row_s_, total, 0u, bits_for(n + 1), false,
+                              stream_));
         DIO_CK(cudaMemsetAsync(counts2_, 0, ((size_t)n + 1) * 4, stream_));
         k_count_lt<<<grid_for(total, 256), 256, 0, stream_>>>(inc_body_s_, total, n, counts2_);
-        tb = cub_bytes_;
-        DIO_CK(cub::DeviceScan::ExclusiveSum(cub_tmp_, tb, counts2_, joint_off_, (int)n + 1, stream_));
+        DIO_CK(ss_.scan(counts2_, joint_off_, n + 1, false, stream_));
         DIO_CK(cudaMemcpyAsync(joint_idx_, inc_row_s_, (size_t)total * 4, cudaMemcpyDeviceToDevice, stream_));
         k_build_jview<<<grid_for(n, 128), 128, 0, stream_>>>(joints_, joint_off_, joint_idx_, n, jview_);
         w_.jview = jview_;
@@ -1447,8 +1438,7 @@ class Engine final : public EngineBase {
         int gd = grid_for(n, kB);
         k_dense<P, R, kB><<<gd, kB, 0, stream_>>>(w_, lo, hi, counts_, offsets_, false);
         DIO_CK(cudaMemsetAsync(counts_ + n, 0, 4, stream_));
-        size_t tb = cub_bytes_;
-        DIO_CK(cub::DeviceScan::ExclusiveSum(cub_tmp_, tb, counts_, offsets_, (int)n + 1, stream_));
+        DIO_CK(ss_.scan(counts_, offsets_, n + 1, false, stream_));
         k_dense<P, R, kB><<<gd, kB, 0, stream_>>>(w_, lo, hi, counts_, offsets_, true);
         k_pairs_total<<<1, 1, 0, stream_>>>(ctr_, offsets_ + n, w_.max_pairs);
         launches_ += 4;
@@ -1460,17 +1450,27 @@ class Engine final : public EngineBase {
         uint32_t ns = std::max(1u, w_.n_scenes);
         int g = grid_for(n, 256);
         if (!rebuild_now_) return run_lbvh_refit(n, g);
+        const uint32_t sbits = ns > 1 ? bits_for(ns - 1) : 0;
+        const uint32_t abits = std::min(10u, (32u - sbits) / 3u);
+        if (!chunks_host_.empty() && scene_max_ <= scene_tree_cap<R>()) {
+            // every scene has a shared-memory tree: one CTA per chunk builds
+            // its trees (bounds, keys, sort, nodes) in one launch
+            DIO_CK(launch_k(pdl(), k_chunk_build<R>, (int)chunks_host_.size(), kSceneTreeThreads,
+                            chunk_build_bytes<R>(), stream_, (const A4<R>*)w_.aabb_min, (const A4<R>*)w_.aabb_max,
+                            (const SceneDesc*)scenes_, (const uint32_t*)w_.scene, (const uint2*)chunks_, n,
+                            std::max(2u, chunk_max_), sbits, abits, lb_keys_s_, lb_leaf_, lb_children_, lb_parent_,
+                            &ctr_->error_flags));
+            ++launches_;
+            return run_lbvh_refit(n, g);
+        }
         DIO_CK(launch_k(pdl(), k_bounds_init, grid_for(ns, 128), 128, 0, stream_, lb_bounds_, ns));
         DIO_CK(launch_k(pdl(), k_scene_bounds<R>, g, 256, 0, stream_, (const A4<R>*)w_.aabb_min,
                         (const A4<R>*)w_.aabb_max, (const uint32_t*)w_.scene, n, lb_bounds_));
-        const uint32_t sbits = ns > 1 ? bits_for(ns - 1) : 0;
-        const uint32_t abits = std::min(10u, (32u - sbits) / 3u);
         DIO_CK(launch_k(pdl(), k_morton<R>, g, 256, 0, stream_, (const A4<R>*)w_.aabb_min, (const A4<R>*)w_.aabb_max,
                         (const uint32_t*)w_.scene, n, (const uint32_t*)lb_bounds_, sbits, abits, lb_keys_, lb_vals_));
-        size_t tb = cub_bytes_;
-        DIO_CK(cub::DeviceRadixSort::SortPairs(cub_tmp_, tb, lb_keys_, lb_keys_s_, lb_vals_, lb_leaf_, (int)n, 0,
-                                               (int)(sbits + 3 * abits), stream_));
-        k_karras<<<g, 256, 0, stream_>>>(lb_keys_s_, scenes_, w_.scene, n, lb_children_, lb_parent_);
+        DIO_CK(ss_.sort_pairs(lb_keys_, lb_keys_s_, lb_vals_, lb_leaf_, n, 0u, sbits + 3u * abits, pdl(), stream_));
+        DIO_CK(launch_k(pdl(), k_karras, g, 256, 0, stream_, (const uint32_t*)lb_keys_s_, (const SceneDesc*)scenes_,
+                        (const uint32_t*)w_.scene, n, lb_children_, lb_parent_));
         launches_ += 4;
         return run_lbvh_refit(n, g);
     }
@@ -1509,8 +1509,8 @@ class Engine final : public EngineBase {
         auto scene_tree = [&](bool write) -> cudaError_t {
             if (!nchunks) return cudaSuccess;
             ++launches_;
-            if (write)  // after a scan: a plain launch
-                return launch_k(false, k_scene_tree<R, true>, (int)nchunks, kSceneTreeThreads, tbytes, stream_,
+            if (write)
+                return launch_k(pdl(), k_scene_tree<R, true>, (int)nchunks, kSceneTreeThreads, tbytes, stream_,
                                 (const A4<R>*)w_.aabb_min, (const A4<R>*)w_.aabb_max, lb_leaf_min_, lb_leaf_max_,
                                 lb_node_min_, lb_node_max_, ta);
             return launch_k(pdl(), k_scene_tree<R, false>, (int)nchunks, kSceneTreeThreads, tbytes, stream_,
@@ -1530,8 +1530,7 @@ class Engine final : public EngineBase {
             launches_ += 2;
         }
         if (!world_step_) DIO_CK(cudaMemsetAsync(counts_ + n, 0, 4, stream_));  // else k_roll_counters
-        size_t tb = cub_bytes_;
-        DIO_CK(cub::DeviceScan::ExclusiveSum(cub_tmp_, tb, counts_, offsets_, (int)n + 1, stream_));
+        DIO_CK(ss_.scan(counts_, offsets_, n + 1, pdl(), stream_));
         DIO_CK(scene_tree(true));
         if (global_path) {
             k_traverse<R><<<gt, 128, 0, stream_>>>(lb_leaf_, scenes_, w_.scene, n, lb_children_, lb_leaf_min_,
@@ -1539,8 +1538,7 @@ class Engine final : public EngineBase {
                                                    lb_pb_, w_.max_pairs, true, &ctr_->error_flags, tcap_skip);
             ++launches_;
         }
-        // a plain launch when nothing of ours ran since the scan
-        DIO_CK(launch_k(pdl() && (nchunks || global_path), k_pairs_total, 1, 1, 0, stream_, ctr_,
+        DIO_CK(launch_k(pdl(), k_pairs_total, 1, 1, 0, stream_, ctr_,
                         (const uint32_t*)(offsets_ + n), w_.max_pairs));
         if (!world_step_) DIO_CK(cudaMemsetAsync(lb_long_count_, 0, 4, stream_));  // else k_roll_counters
         DIO_CK(launch_k(pdl(), k_sort_segments, g, 256, 0, stream_, (const uint32_t*)offsets_, n, w_.max_pairs, lb_pb_,
@@ -1573,21 +1571,23 @@ class Engine final : public EngineBase {
         uint32_t G = groups;
         if (!src) src = w_.slots;
         if (G) {
-            DIO_CK(launch_k(pdl(), k_slot_count<R>, grid_for(G, 256), 256, 0, stream_, src, per, groups_dev, G,
-                            counts_));
-            size_t tb = cub_bytes_;
-            DIO_CK(cub::DeviceScan::ExclusiveSum(cub_tmp_, tb, counts_, offsets_, (int)G + 1, stream_));
-            k_slot_rows<P, R><<<grid_for(G, 128), 128, 0, stream_>>>(w_, src, per, groups_dev, G, offsets_, o);
+            // grid-stride over the live groups (a device count: fixed grids)
+            DIO_CK(launch_k(pdl(), k_slot_count<R>, std::min(grid_for(G, 256), sms_ * 8), 256, 0, stream_, src, per,
+                            groups_dev, G, counts_));
+            // offsets of the live groups, the total at offsets_[G]
+            DIO_CK(ss_.scan(counts_, offsets_, G, pdl(), stream_, groups_dev, offsets_ + G));
+            DIO_CK(launch_k(pdl(), k_slot_rows<P, R>, std::min(grid_for(G, 128), sms_ * 16), 128, 0, stream_, w_, src,
+                            per, groups_dev, G, (const uint32_t*)offsets_, o));
         } else {
             DIO_CK(cudaMemsetAsync(offsets_, 0, 4, stream_));
         }
         const uint32_t* pair_rows = offsets_ + G;
         if (n) {
             DIO_CK(launch_k(pdl() && G, k_cont_count<P, R>, grid_for(n, 128), 128, 0, stream_, w_, 0u, n, o, counts2_));
-            size_t tb = cub_bytes_;
-            DIO_CK(cub::DeviceScan::ExclusiveSum(cub_tmp_, tb, counts2_, offsets2_, (int)n + 1, stream_));
+            DIO_CK(ss_.scan(counts2_, offsets2_, n + 1, pdl(), stream_));
             // clears counts2_ for the CSR count of finish_rows_world
-            k_cont_rows<P, R><<<grid_for(n, 128), 128, 0, stream_>>>(w_, 0, n, o, offsets2_, pair_rows, counts2_);
+            DIO_CK(launch_k(pdl(), k_cont_rows<P, R>, grid_for(n, 128), 128, 0, stream_, w_, 0u, n, o,
+                            (const uint32_t*)offsets2_, pair_rows, counts2_));
         } else {
             DIO_CK(cudaMemsetAsync(offsets2_, 0, 4, stream_));
         }
@@ -1603,19 +1603,15 @@ class Engine final : public EngineBase {
         if (M) {
             k_row_keys<<<grid_for(M, 256), 256, 0, stream_>>>(w_.ab, &ctr_->rows, M, keys_raw_, ids_raw_, inc_body_,
                                                               inc_row_, n);
-            size_t tb = cub_bytes_;
-            DIO_CK(cub::DeviceRadixSort::SortPairs(cub_tmp_, tb, keys_raw_, keys_s_[cur_], ids_raw_, ids_s_[cur_],
-                                                   (int)M, 0, 64, stream_));
+            DIO_CK(ss_.sort_pairs(keys_raw_, keys_s_[cur_], ids_raw_, ids_s_[cur_], M, 0u, 64u, false, stream_));
             k_warm<P, R><<<grid_for(M, 256), 256, 0, stream_>>>(w_, &ctr_->rows, keys_s_[cur_], ids_s_[cur_],
                                                                 keys_s_[pb], ids_s_[pb], n_prev_rows_, rd_[pb], o);
-            tb = cub_bytes_;
-            DIO_CK(cub::DeviceRadixSort::SortPairs(cub_tmp_, tb, inc_body_, inc_body_s_, inc_row_, inc_row_s_,
-                                                   (int)(2 * M), 0, (int)bits_for(n + 1), stream_));
+            DIO_CK(ss_.sort_pairs(inc_body_, inc_body_s_, inc_row_, inc_row_s_, 2 * M, 0u, bits_for(n + 1), false,
+                                  stream_));
         }
         DIO_CK(cudaMemsetAsync(counts2_, 0, ((size_t)n + 1) * 4, stream_));
         if (M) k_inc_count<<<grid_for(2 * M, 256), 256, 0, stream_>>>(inc_body_s_, &ctr_->rows, n, counts2_);
-        size_t tb = cub_bytes_;
-        DIO_CK(cub::DeviceScan::ExclusiveSum(cub_tmp_, tb, counts2_, w_.row_off, (int)n + 1, stream_));
+        DIO_CK(ss_.scan(counts2_, w_.row_off, n + 1, false, stream_));
         if (M) k_csr_fill<P, R><<<grid_for(2 * M, 256), 256, 0, stream_>>>(w_, inc_body_s_, inc_row_s_, &ctr_->rows);
         launches_ += M ? 4 : 0;
         return DIO_OK;
@@ -2089,8 +2085,7 @@ class Engine final : public EngineBase {
         }
         DIO_CK(cudaMemsetAsync(color_hist_, 0, (kMaxColors + 1) * 4, stream_));
         k_color_hist<P, R><<<g, 256, 0, stream_>>>(w_, color_hist_);
-        size_t tb = cub_bytes_;
-        DIO_CK(cub::DeviceScan::ExclusiveSum(cub_tmp_, tb, color_hist_, w_.color_off, (int)kMaxColors + 1, stream_));
+        DIO_CK(ss_.scan(color_hist_, w_.color_off, kMaxColors + 1, false, stream_));
         DIO_CK(cudaMemsetAsync(color_hist_, 0, (kMaxColors + 1) * 4, stream_));
         k_color_fill<P, R><<<g, 256, 0, stream_>>>(w_, color_hist_);
         launches_ += 3;
@@ -2125,9 +2120,9 @@ class Engine final : public EngineBase {
         // counts2_ was cleared by k_cont_rows (build_rows, bodies [0, n))
         if (!n) DIO_CK(cudaMemsetAsync(counts2_, 0, 4, stream_));
         DIO_CK(launch_k(pdl() && n, k_csr_count_dyn<P, R>, gf, 256, 0, stream_, w_, counts2_));
-        size_t tb = cub_bytes_;
-        DIO_CK(cub::DeviceScan::ExclusiveSum(cub_tmp_, tb, counts2_, w_.row_off, (int)n + 1, stream_));
-        k_csr_scatter_dyn<P, R><<<gf, 256, 0, stream_>>>(w_, counts2_);  // takes the counts back to zero
+        DIO_CK(ss_.scan(counts2_, w_.row_off, n + 1, pdl(), stream_));
+        // takes the counts back to zero
+        DIO_CK(launch_k(pdl(), k_csr_scatter_dyn<P, R>, gf, 256, 0, stream_, w_, counts2_));
         int gn = grid_for(n, 256);
         DIO_CK(launch_k(pdl(), k_sort_segments, gn, 256, 0, stream_, (const uint32_t*)w_.row_off, n, w_.max_incid,
                         w_.row_idx, lb_long_, &ctr_->long_count));
@@ -2288,8 +2283,7 @@ class Engine final : public EngineBase {
     A4<R>* hull_ = nullptr;
     Counters* ctr_ = nullptr;
     Counters* hctr_ = nullptr;
-    void* cub_tmp_ = nullptr;
-    size_t cub_bytes_ = 0;
+    ScanSort ss_;  // prefix sums and radix sorts
     void* dstage_ = nullptr;
     void* hstage_ = nullptr;
     size_t stage_bytes_ = 0;
@@ -2332,9 +2326,7 @@ static __global__ void k_keys_only(const uint2* ab, uint32_t m, unsigned long lo
 template <class P, class R>
 int Engine<P, R>::sort_keys_n(const uint2* ab, uint32_t m, unsigned long long* keys_out, uint32_t* ids_out) {
     k_keys_only<<<grid_for(m, 256), 256, 0, stream_>>>(ab, m, keys_raw_, ids_raw_);
-    size_t tb = cub_bytes_;
-    DIO_CK(cub::DeviceRadixSort::SortPairs(cub_tmp_, tb, keys_raw_, keys_out, ids_raw_, ids_out, (int)m, 0, 64,
-                                           stream_));
+    DIO_CK(ss_.sort_pairs(keys_raw_, keys_out, ids_raw_, ids_out, m, 0u, 64u, false, stream_));
     return DIO_OK;
 }
 

@@ -5,10 +5,12 @@
 //   k_scene_bounds   centroid bounds per scene (ordered-int atomics)
 //   k_morton         30-bit Morton code of each AABB centre within its scene's
 //                    bounds; key = scene << 32 | code (scenes stay contiguous)
-//   radix sort       (key, body) pairs
+//   radix sort       (key, body) pairs (k_scan.cuh)
 //   k_karras         binary radix tree per scene (Karras 2012), internal node
 //                    k of a scene covers a key range; children are leaves or
 //                    internal nodes of the same scene
+//   k_chunk_build    the four steps above in one launch when every scene fits
+//                    the shared-memory trees: one CTA per chunk of scenes
 //   k_refit          bottom-up AABB union (second arrival at a node continues)
 //   k_traverse       stack traversal per leaf; a pair (i, j) is reported only
 //                    by its smaller body i, so each overlap is found once;
@@ -37,16 +39,25 @@ __device__ __forceinline__ uint64_t d2ord(double f) {
     return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
 }
 
-// per-scene centroid bounds: 6 ordered uints (min xyz, max xyz); the Morton
-// grid only needs to be monotone in the centre, so FP32 bounds suffice
+// AABB centre, rounded to FP32 (the Morton grid only needs to be monotone
+// in the centre)
+template <class R>
+__device__ __forceinline__ void aabb_centre(const A4<R>& a, const A4<R>& b, float c[3]) {
+    c[0] = float(a.x * R(0.5) + b.x * R(0.5));
+    c[1] = float(a.y * R(0.5) + b.y * R(0.5));
+    c[2] = float(a.z * R(0.5) + b.z * R(0.5));
+}
+
+// per-scene centroid bounds: 6 ordered uints (min xyz, max xyz)
 template <class R>
 __global__ void k_scene_bounds(const A4<R>* mn, const A4<R>* mx, const uint32_t* scene, uint32_t n, uint32_t* bounds) {
     pdl_enter();
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        A4<R> a = mn[i], b = mx[i];
-        uint32_t ox = f2ord(float(a.x * R(0.5) + b.x * R(0.5)));
-        uint32_t oy = f2ord(float(a.y * R(0.5) + b.y * R(0.5)));
-        uint32_t oz = f2ord(float(a.z * R(0.5) + b.z * R(0.5)));
+        float c[3];
+        aabb_centre(mn[i], mx[i], c);
+        uint32_t ox = f2ord(c[0]);
+        uint32_t oy = f2ord(c[1]);
+        uint32_t oz = f2ord(c[2]);
         const uint32_t s = scene[i];
         // lanes of one scene reduce first; their leader issues the atomics
         const uint32_t grp = __match_any_sync(__activemask(), s);
@@ -78,38 +89,42 @@ __device__ __forceinline__ uint32_t spread10(uint32_t v) {
 // 32-bit key: scene index in the top `scene_bits`, then a Morton code with
 // `axis_bits` per axis (10 for one scene, 7 for up to 2048 scenes); the key
 // only has to keep scenes contiguous and order bodies spatially within one
+// Morton code of centre c within the scene bounds bs (6 ordered uints)
+__device__ __forceinline__ uint32_t morton_code(const float c[3], const uint32_t* bs, uint32_t axis_bits) {
+    const float cells = float(1u << axis_bits);
+    const uint32_t top = (1u << axis_bits) - 1u;
+    uint32_t q[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        float lo = ord2f(bs[k]), hi = ord2f(bs[3 + k]);
+        float ext = hi - lo;
+        float t = ext > 0.f ? (c[k] - lo) / ext : 0.f;
+        t = fminf(fmaxf(t, 0.f), 1.f);
+        q[k] = min((uint32_t)(t * cells), top);
+    }
+    return (spread10(q[0]) << 2) | (spread10(q[1]) << 1) | spread10(q[2]);
+}
+
 template <class R>
 __global__ void k_morton(const A4<R>* mn, const A4<R>* mx, const uint32_t* scene, uint32_t n, const uint32_t* bounds,
                          uint32_t scene_bits, uint32_t axis_bits, uint32_t* keys, uint32_t* vals) {
     pdl_enter();
-    const float cells = float(1u << axis_bits);
-    const uint32_t top = (1u << axis_bits) - 1u;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        A4<R> a = mn[i], b = mx[i];
-        float c[3] = {float(a.x * R(0.5) + b.x * R(0.5)), float(a.y * R(0.5) + b.y * R(0.5)),
-                      float(a.z * R(0.5) + b.z * R(0.5))};
-        uint32_t s = scene[i];
-        const uint32_t* bs = bounds + 6 * s;
-        uint32_t q[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            float lo = ord2f(bs[k]), hi = ord2f(bs[3 + k]);
-            float ext = hi - lo;
-            float t = ext > 0.f ? (c[k] - lo) / ext : 0.f;
-            t = fminf(fmaxf(t, 0.f), 1.f);
-            q[k] = min((uint32_t)(t * cells), top);
-        }
-        uint32_t code = (spread10(q[0]) << 2) | (spread10(q[1]) << 1) | spread10(q[2]);
+        float c[3];
+        aabb_centre(mn[i], mx[i], c);
+        const uint32_t s = scene[i];
+        const uint32_t code = morton_code(c, bounds + 6 * s, axis_bits);
         keys[i] = scene_bits ? ((s << (3 * axis_bits)) | code) : code;
         vals[i] = i;
     }
 }
 
-// Karras prefix length of sorted positions a, b within a segment of length
-// n (local indices); duplicates tie-break on the index.
-__device__ __forceinline__ int kdelta(const uint32_t* keys, uint32_t lo, int n, int a, int b) {
+// Karras prefix length of sorted positions a, b of a scene's sorted keys
+// seg[0, n); duplicates tie-break on the index.  Only XORs and equality of
+// keys of one scene enter, so any key offset common to the scene cancels.
+__device__ __forceinline__ int kdelta(const uint32_t* seg, int n, int a, int b) {
     if (b < 0 || b >= n) return -1;
-    uint32_t ka = keys[lo + a], kb = keys[lo + b];
+    uint32_t ka = seg[a], kb = seg[b];
     if (ka == kb) return 32 + __clz((uint32_t)(a ^ b));
     return __clz(ka ^ kb);
 }
@@ -131,10 +146,38 @@ __device__ __forceinline__ A4<double> ldcg4(const A4<double>* p) {
     return {a.x, a.y, b.x, b.y};
 }
 
-// internal node k of scene s lives at global slot lo_s + k; child codes are
-// global slots, leaves flagged with kLeafFlag (leaf = sorted position)
+// Internal node k of a scene whose sorted keys are seg[0, ns) and whose
+// slots start at global slot lo: node k lives at slot lo + k; child codes
+// are global slots, leaves flagged with kLeafFlag (leaf = sorted position);
+// parents of internal slots in [0, n), of leaves in [n, 2n)
+__device__ __forceinline__ void karras_node(const uint32_t* seg, uint32_t lo, int ns, int k, uint32_t n,
+                                            uint2* children, uint32_t* parent) {
+    int d = (kdelta(seg, ns, k, k + 1) - kdelta(seg, ns, k, k - 1)) >= 0 ? 1 : -1;
+    int dmin = kdelta(seg, ns, k, k - d);
+    int lmax = 2;
+    while (kdelta(seg, ns, k, k + lmax * d) > dmin) lmax <<= 1;
+    int l = 0;
+    for (int t = lmax >> 1; t >= 1; t >>= 1)
+        if (kdelta(seg, ns, k, k + (l + t) * d) > dmin) l += t;
+    int j = k + l * d;
+    int dnode = kdelta(seg, ns, k, j);
+    int s = 0;
+    int t = l;
+    do {
+        t = (t + 1) >> 1;
+        if (kdelta(seg, ns, k, k + (s + t) * d) > dnode) s += t;
+    } while (t > 1);
+    int gamma = k + s * d + min(d, 0);
+    uint32_t left = (min(k, j) == gamma) ? ((lo + gamma) | kLeafFlag) : (lo + gamma);
+    uint32_t right = (max(k, j) == gamma + 1) ? ((lo + gamma + 1) | kLeafFlag) : (lo + gamma + 1);
+    children[lo + k] = make_uint2(left, right);
+    parent[(left & kLeafFlag) ? n + (left & ~kLeafFlag) : left] = lo + k;
+    parent[(right & kLeafFlag) ? n + (right & ~kLeafFlag) : right] = lo + k;
+}
+
+// binary radix tree per scene (Karras 2012) over the globally sorted keys
 static __global__ void k_karras(const uint32_t* keys, const SceneDesc* scenes, const uint32_t* scene_of_pos,
-                         uint32_t n, uint2* children, uint32_t* parent) {
+                                uint32_t n, uint2* children, uint32_t* parent) {
     pdl_enter();
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
         const SceneDesc sc = scenes[scene_of_pos[p]];
@@ -142,28 +185,7 @@ static __global__ void k_karras(const uint32_t* keys, const SceneDesc* scenes, c
         const int ns = (int)(sc.body_hi - sc.body_lo);
         const int k = (int)(p - lo);
         if (k >= ns - 1) continue;  // ns - 1 internal nodes
-        int d = (kdelta(keys, lo, ns, k, k + 1) - kdelta(keys, lo, ns, k, k - 1)) >= 0 ? 1 : -1;
-        int dmin = kdelta(keys, lo, ns, k, k - d);
-        int lmax = 2;
-        while (kdelta(keys, lo, ns, k, k + lmax * d) > dmin) lmax <<= 1;
-        int l = 0;
-        for (int t = lmax >> 1; t >= 1; t >>= 1)
-            if (kdelta(keys, lo, ns, k, k + (l + t) * d) > dmin) l += t;
-        int j = k + l * d;
-        int dnode = kdelta(keys, lo, ns, k, j);
-        int s = 0;
-        int t = l;
-        do {
-            t = (t + 1) >> 1;
-            if (kdelta(keys, lo, ns, k, k + (s + t) * d) > dnode) s += t;
-        } while (t > 1);
-        int gamma = k + s * d + min(d, 0);
-        uint32_t left = (min(k, j) == gamma) ? ((lo + gamma) | kLeafFlag) : (lo + gamma);
-        uint32_t right = (max(k, j) == gamma + 1) ? ((lo + gamma + 1) | kLeafFlag) : (lo + gamma + 1);
-        children[lo + k] = make_uint2(left, right);
-        // parents: internal slots in [0, n), leaves in [n, 2n)
-        parent[(left & kLeafFlag) ? n + (left & ~kLeafFlag) : left] = lo + k;
-        parent[(right & kLeafFlag) ? n + (right & ~kLeafFlag) : right] = lo + k;
+        karras_node(keys + lo, lo, ns, k, n, children, parent);
     }
 }
 
@@ -340,7 +362,7 @@ struct TreeArgs {
 };
 
 // Count-pass traversal from the leaf at chunk position p: pairs with leaves at
-// higher positions, counted for the lower body and appended to the chunk's
+// higher positions, counted for the lower body and appended (warp-aggregated) to the chunk's
 // scratch.  Both children's boxes (and their tags) are loaded before either
 // is tested, so the loads of one step overlap.
 template <class R>
@@ -373,7 +395,7 @@ __device__ __forceinline__ void tree_count_leaf(uint32_t p, uint32_t root, const
                 const uint32_t j = tag_of(bmn[k]);
                 const uint32_t a = min(i, j), b = max(i, j);
                 atomicAdd(&vis[a - lo], 1u);
-                const uint32_t slot = atomicAdd(s_cursor, 1u);
+                const uint32_t slot = warp_append(s_cursor);
                 if (slot < region) dst[slot] = make_uint2(a, b);
             } else {
                 if (push == 0)
@@ -578,6 +600,122 @@ __global__ void __launch_bounds__(kSceneTreeThreads)
     }
 }
 
+// ---- tree build of one chunk of scenes in one CTA ----
+// The same trees as k_scene_bounds + k_morton + the global key sort +
+// k_karras, for a world whose scenes all fit the shared-memory trees: per
+// scene centroid bounds (shared-memory atomics), Morton keys, a sort of the
+// chunk's keys in shared memory, and the Karras nodes from the sorted keys.
+// The chunk's sorted order equals its slice of the global sort: scenes are
+// consecutive body ranges and the scene index is the key's top field, so
+// keys of the chunk sort among themselves.  Inside the CTA a key carries
+// (scene - first scene of the chunk) in that field; the composite word
+// (key << 32 | chunk position) is unique, so a bitonic network gives the
+// stable order.
+template <class R>
+__host__ __device__ constexpr uint32_t chunk_build_pow2() { return scene_tree_cap<R>(); }
+template <class R>
+__host__ __device__ constexpr size_t chunk_build_bytes() {
+    // sort words, then 6 bound words per scene (at most one scene per body),
+    // reused for the sorted keys
+    return (size_t)chunk_build_pow2<R>() * 8 + (size_t)scene_tree_cap<R>() * 24;
+}
+static_assert((scene_tree_cap<float>() & (scene_tree_cap<float>() - 1)) == 0 &&
+                  (scene_tree_cap<double>() & (scene_tree_cap<double>() - 1)) == 0,
+              "the chunk sort pads to a power of two no larger than the tree cap");
+
+template <class R>
+__global__ void __launch_bounds__(kSceneTreeThreads)
+    k_chunk_build(const A4<R>* aabb_min, const A4<R>* aabb_max, const SceneDesc* scenes, const uint32_t* scene_of,
+                  const uint2* chunks, uint32_t n, uint32_t cap_bodies, uint32_t scene_bits, uint32_t axis_bits,
+                  uint32_t* keys_sorted, uint32_t* leaf_body, uint2* children, uint32_t* parent, uint32_t* err) {
+    pdl_enter();
+    extern __shared__ __align__(16) unsigned char build_smem[];
+    const uint2 chunk = chunks[blockIdx.x];  // scenes [x, y)
+    const uint32_t lo = scenes[chunk.x].body_lo;
+    const uint32_t nb = scenes[chunk.y - 1].body_hi - lo;
+    const uint32_t nsc = chunk.y - chunk.x;
+    if (nb > cap_bodies || cap_bodies > chunk_build_pow2<R>()) {  // the host packs chunks within the cap
+        if (threadIdx.x == 0) atomicOr(err, kErrIndexOverflow);
+        return;
+    }
+    const uint32_t tid = threadIdx.x, nt = blockDim.x;
+    unsigned long long* s_sort = reinterpret_cast<unsigned long long*>(build_smem);
+    uint32_t* s_bounds = reinterpret_cast<uint32_t*>(s_sort + chunk_build_pow2<R>());
+    for (uint32_t i = tid; i < nsc; i += nt) {
+        s_bounds[6 * i + 0] = s_bounds[6 * i + 1] = s_bounds[6 * i + 2] = 0xFFFFFFFFu;
+        s_bounds[6 * i + 3] = s_bounds[6 * i + 4] = s_bounds[6 * i + 5] = 0u;
+    }
+    __syncthreads();
+    for (uint32_t p = tid; p < nb; p += nt) {
+        float c[3];
+        aabb_centre(aabb_min[lo + p], aabb_max[lo + p], c);
+        const uint32_t ox = f2ord(c[0]), oy = f2ord(c[1]), oz = f2ord(c[2]);
+        const uint32_t ls = scene_of[lo + p] - chunk.x;
+        // lanes of one scene reduce first; their leader issues the atomics
+        const uint32_t grp = __match_any_sync(__activemask(), ls);
+        const uint32_t nx = __reduce_min_sync(grp, ox), ny = __reduce_min_sync(grp, oy),
+                       nz = __reduce_min_sync(grp, oz);
+        const uint32_t xx = __reduce_max_sync(grp, ox), xy = __reduce_max_sync(grp, oy),
+                       xz = __reduce_max_sync(grp, oz);
+        if ((tid & 31u) == (uint32_t)(__ffs(grp) - 1)) {
+            uint32_t* bs = s_bounds + 6 * ls;
+            atomicMin(&bs[0], nx);
+            atomicMin(&bs[1], ny);
+            atomicMin(&bs[2], nz);
+            atomicMax(&bs[3], xx);
+            atomicMax(&bs[4], xy);
+            atomicMax(&bs[5], xz);
+        }
+    }
+    __syncthreads();
+    uint32_t p2 = 1;
+    while (p2 < nb) p2 <<= 1;
+    for (uint32_t p = tid; p < p2; p += nt) {
+        unsigned long long word = ~0ull;  // padding sorts last
+        if (p < nb) {
+            float c[3];
+            aabb_centre(aabb_min[lo + p], aabb_max[lo + p], c);
+            const uint32_t ls = scene_of[lo + p] - chunk.x;
+            const uint32_t code = morton_code(c, s_bounds + 6 * ls, axis_bits);
+            const uint32_t key = scene_bits ? ((ls << (3 * axis_bits)) | code) : code;
+            word = ((unsigned long long)key << 32) | p;
+        }
+        s_sort[p] = word;
+    }
+    __syncthreads();
+    for (uint32_t size = 2; size <= p2; size <<= 1) {
+        for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+            for (uint32_t t = tid; t < p2 / 2; t += nt) {
+                const uint32_t i = 2 * t - (t & (stride - 1)), j = i + stride;
+                const unsigned long long a = s_sort[i], b = s_sort[j];
+                if ((a > b) == ((i & size) == 0)) {
+                    s_sort[i] = b;
+                    s_sort[j] = a;
+                }
+            }
+            __syncthreads();
+        }
+    }
+    // sorted keys of the chunk (the bounds are no longer needed)
+    uint32_t* s_key = s_bounds;
+    const uint32_t key_base = scene_bits ? (chunk.x << (3 * axis_bits)) : 0u;
+    for (uint32_t p = tid; p < nb; p += nt) {
+        const unsigned long long word = s_sort[p];
+        const uint32_t key = (uint32_t)(word >> 32);
+        s_key[p] = key;
+        keys_sorted[lo + p] = key + key_base;
+        leaf_body[lo + p] = lo + (uint32_t)word;
+    }
+    __syncthreads();
+    for (uint32_t p = tid; p < nb; p += nt) {
+        const SceneDesc sc = scenes[scene_of[lo + p]];
+        const int ns = (int)(sc.body_hi - sc.body_lo);
+        const int k = (int)(lo + p - sc.body_lo);
+        if (k >= ns - 1) continue;  // ns - 1 internal nodes
+        karras_node(s_key + (sc.body_lo - lo), sc.body_lo, ns, k, n, children, parent);
+    }
+}
+
 // sort each body's partner list ascending; short lists in-thread, long
 // lists (> 32) by one CTA in shared memory (bitonic, up to 4096 entries)
 static __global__ void k_bounds_init(uint32_t* b, uint32_t ns) {
@@ -596,7 +734,7 @@ static __global__ void k_sort_segments(const uint32_t* offsets, uint32_t n, uint
         uint32_t len = b - a;
         if (len <= 1 || b > cap) continue;  // overflow is reported by the pair count
         if (len > 32) {
-            long_list[atomicAdd(long_count, 1u)] = i;
+            long_list[warp_append(long_count)] = i;
             continue;
         }
         uint32_t v[32];

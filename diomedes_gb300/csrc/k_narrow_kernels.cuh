@@ -66,7 +66,7 @@ __global__ void __launch_bounds__(128) k_narrow_main(DevWorld<P, R> w, const uin
                          sub(b.pos, scale(n, b.shape.c[0].x)));
             }
         } else {
-            uint32_t e = atomicAdd(&w.ctr->gjk_work, 1u);
+            const uint32_t e = warp_append(&w.ctr->gjk_work);
             w.gjk_list[e] = p;
         }
     }
@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(128) k_gjk(DevWorld<P, R> w) {
         NB<R> b = load_nb(w, pr.b);
         Simplex<R> s;
         if (gjk(a, b, w.hull, s)) {
-            uint32_t q = atomicAdd(&w.ctr->epa_work, 1u);
+            const uint32_t q = warp_append(&w.ctr->epa_work);
             w.epa_list[q] = p;
             A4<R>* dst = w.simplex + (size_t)q * 8;
 #pragma unroll

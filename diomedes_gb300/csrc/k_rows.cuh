@@ -53,18 +53,16 @@ __device__ __forceinline__ void write_row(const DevWorld<P, R>& w, uint32_t r, u
     w.ab[r] = make_uint2(a, b);
 }
 
-// Valid slots of the first `n_groups` groups of `per` slots; counts[n_groups]
-// is set to 0 for the exclusive scan over n_groups + 1 entries.
+// Valid slots of each live group of `per` slots (the first min(*n_groups_dev,
+// n_groups) groups); the scan that follows stops at the same count.
 template <class R>
 __global__ void k_slot_count(const Slot<R>* slots, uint32_t per, const uint32_t* n_groups_dev, uint32_t n_groups,
                              uint32_t* counts) {
     pdl_enter();
-    if (blockIdx.x == 0 && threadIdx.x == 0) counts[n_groups] = 0u;
-    uint32_t ng = n_groups_dev ? *n_groups_dev : n_groups;
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n_groups; p += gridDim.x * blockDim.x) {
+    const uint32_t ng = n_groups_dev ? min(*n_groups_dev, n_groups) : n_groups;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < ng; p += gridDim.x * blockDim.x) {
         uint32_t c = 0;
-        if (p < ng)
-            for (uint32_t k = 0; k < per; ++k) c += slots[p * per + k].valid ? 1u : 0u;
+        for (uint32_t k = 0; k < per; ++k) c += slots[p * per + k].valid ? 1u : 0u;
         counts[p] = c;
     }
 }

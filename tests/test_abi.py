@@ -11,11 +11,11 @@ import pytest
 from diomedes_gb300 import abi, physics as ph
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-HEADER = os.path.join(ROOT, "include", "dio_cuda.h")
+HEADERS = [os.path.join(ROOT, "include", f) for f in ("dio_cuda.h", "dio_selftest.h")]
 
 
 def _declared():
-    text = open(HEADER).read()
+    text = "".join(open(h).read() for h in HEADERS)
     return sorted(set(re.findall(r"^(?:int|const char\*)\s+(dio_\w+)\(", text, re.M)))
 
 
@@ -167,3 +167,10 @@ def test_hull_ranges_are_checked_on_the_host():
     compute.check_hull_ranges(b, nh)
     with pytest.raises(ValueError):
         compute.check_hull_ranges(b, nh - 1)
+
+
+def test_no_library_code_in_the_scans_and_sorts():
+    # the prefix sums and radix sorts are the library's own kernels (k_scan.cuh)
+    out = subprocess.run(["nm", "-C", abi.LIB_PATH], capture_output=True, text=True).stdout
+    assert "cub::" not in out
+    assert "dio::k_scan_excl" in out and "dio::k_radix_pass" in out
