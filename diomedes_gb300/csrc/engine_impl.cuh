@@ -538,6 +538,7 @@ class Engine final : public EngineBase {
         DIO_TRY(alloc(&scene_chunk_, S));
         DIO_TRY(alloc(&chunk_n_, S));
         DIO_TRY(alloc(&chunk_ovf_, S));
+        DIO_TRY(alloc(&chunk_tot_, S));
         // pair scratch of the shared-memory trees: scratch_k_ slots per body
         scratch_k_ = (uint32_t)std::min<uint64_t>(8, std::max<uint64_t>(2, 2 * ((uint64_t)PP + N - 1) / N));
         DIO_TRY(alloc(&tree_scratch_, (size_t)N * scratch_k_));
@@ -1505,7 +1506,14 @@ class Engine final : public EngineBase {
         ta.scratch_k = scratch_k_;
         ta.chunk_n = chunk_n_;
         ta.chunk_ovf = chunk_ovf_;
+        ta.chunk_tot = chunk_tot_;
         ta.err = &ctr_->error_flags;
+        // every scene in a shared-memory tree: the write pass also forms the
+        // offsets, sorts the partner lists and emits the pairs
+        ta.fused = (nchunks && !global_path) ? 1u : 0u;
+        ta.nchunks = nchunks;
+        ta.pairs = w_.pairs;
+        ta.ctr = ctr_;
         auto scene_tree = [&](bool write) -> cudaError_t {
             if (!nchunks) return cudaSuccess;
             ++launches_;
@@ -1519,6 +1527,10 @@ class Engine final : public EngineBase {
         };
         int gt = grid_for(n, 128);
         DIO_CK(scene_tree(false));
+        if (ta.fused) {
+            DIO_CK(scene_tree(true));
+            return DIO_OK;
+        }
         if (global_path) {
             DIO_CK(cudaMemsetAsync(lb_visits_, 0, (size_t)n * 4, stream_));
             k_refit<R><<<g, 256, 0, stream_>>>(w_.aabb_min, w_.aabb_max, lb_leaf_, scenes_, w_.scene, n,
@@ -2276,6 +2288,7 @@ class Engine final : public EngineBase {
     bool lag_primed_ = false;  // the previous step's slots are this mode's
     uint32_t* chunk_n_ = nullptr;
     uint32_t* chunk_ovf_ = nullptr;
+    uint32_t* chunk_tot_ = nullptr;
     uint2* tree_scratch_ = nullptr;
     uint32_t scratch_k_ = 2;
     A4<P>* origin_ = nullptr;

@@ -351,14 +351,21 @@ struct TreeArgs {
     const uint2* children;
     const uint32_t* parent;
     uint32_t* counts;
-    const uint32_t* offsets;
+    uint32_t* offsets;
     uint32_t* pb;
     uint32_t cap;
     uint2* scratch;
     uint32_t scratch_k;
     uint32_t* chunk_n;
     uint32_t* chunk_ovf;
+    uint32_t* chunk_tot;  // pairs found per chunk (count pass)
     uint32_t* err;
+    // write pass of a world whose scenes all have shared-memory trees: it
+    // also forms the offsets, sorts each body's partners and emits the pairs
+    uint32_t fused;
+    uint32_t nchunks;
+    DioPair* pairs;
+    Counters* ctr;
 };
 
 // Count-pass traversal from the leaf at chunk position p: pairs with leaves at
@@ -471,6 +478,136 @@ __device__ __forceinline__ void tree_write_leaf(uint32_t p, uint32_t root, const
     }
 }
 
+static_assert(scene_tree_cap<float>() <= 2u * kSceneTreeThreads && scene_tree_cap<double>() <= 2u * kSceneTreeThreads,
+              "the fused offsets scan takes two bodies a thread");
+// Fused write pass, part 1: the chunk's pair offsets.  base = pairs of the
+// chunks whose bodies come first (chunks are contiguous body ranges),
+// then a CTA-wide exclusive sum of the per-body counts: offsets[lo + p],
+// the scan's prefix in excl[p], the count in cnt[p].  CTA 0 also stores the
+// world's pair count (and the overflow flag), as k_pairs_total does.
+__device__ __forceinline__ void fused_offsets(const TreeArgs& t, uint32_t lo, uint32_t nb, uint32_t* excl,
+                                             uint32_t* cnt, uint32_t* s_red) {
+    const uint32_t tid = threadIdx.x, nt = blockDim.x, lane = tid & 31u, warp = tid >> 5;
+    unsigned long long before = 0, grand = 0;
+    for (uint32_t c = tid; c < t.nchunks; c += nt) {
+        const uint32_t tot = t.chunk_tot[c];
+        grand += tot;
+        if (t.scenes[t.chunks[c].x].body_lo < lo) before += tot;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        before += __shfl_xor_sync(0xFFFFFFFFu, before, o);
+        grand += __shfl_xor_sync(0xFFFFFFFFu, grand, o);
+    }
+    unsigned long long* s_sum = reinterpret_cast<unsigned long long*>(s_red);  // 2 x 32 u64 (128 words)
+    if (lane == 0) {
+        s_sum[warp] = before;
+        s_sum[32 + warp] = grand;
+    }
+    __syncthreads();
+    before = grand = 0;
+    for (uint32_t w = 0; w < nt / 32u; ++w) {
+        before += s_sum[w];
+        grand += s_sum[32 + w];
+    }
+    __syncthreads();
+    if (blockIdx.x == 0 && tid == 0) {
+        t.ctr->pairs = grand > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)grand;
+        if (grand > t.cap) atomicOr(&t.ctr->error_flags, kErrPairOverflow);
+    }
+    // per-body counts, two consecutive bodies a thread
+    const uint32_t p0 = 2u * tid;
+    const uint32_t c0 = p0 < nb ? t.counts[lo + p0] : 0u, c1 = p0 + 1u < nb ? t.counts[lo + p0 + 1u] : 0u;
+    uint32_t x = c0 + c1;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= (uint32_t)o) x += y;
+    }
+    if (lane == 31u) s_red[warp] = x;
+    __syncthreads();
+    uint32_t wofs = 0;
+    for (uint32_t w = 0; w < warp; ++w) wofs += s_red[w];
+    const uint32_t e0 = wofs + x - (c0 + c1);
+    const uint32_t b32 = (uint32_t)before;
+    if (p0 < nb) {
+        excl[p0] = e0;
+        cnt[p0] = c0;
+        t.offsets[lo + p0] = b32 + e0;
+    }
+    if (p0 + 1u < nb) {
+        excl[p0 + 1u] = e0 + c0;
+        cnt[p0 + 1u] = c1;
+        t.offsets[lo + p0 + 1u] = b32 + e0 + c0;
+    }
+    __syncthreads();
+}
+
+// Fused write pass, part 2: each body's partners (placed at its offsets in
+// pb) sorted ascending -- up to 32 in registers by the body's thread, longer
+// lists by the whole CTA (bitonic in `scratch`, the shared tree space) --
+// then the pairs (body, partner) in (a, b) order.
+__device__ __forceinline__ void fused_emit(const TreeArgs& t, uint32_t lo, uint32_t nb, const uint32_t* cnt,
+                                          uint32_t* long_list, uint32_t* s_nlong, uint32_t* scratch,
+                                          uint32_t scratch_words) {
+    const uint32_t tid = threadIdx.x, nt = blockDim.x;
+    if (tid == 0) *s_nlong = 0u;
+    __syncthreads();
+    for (uint32_t p = tid; p < nb; p += nt) {
+        const uint32_t a = t.offsets[lo + p], len = cnt[p];
+        if (len <= 1u || a + len > t.cap) continue;  // overflow is reported by the pair count
+        if (len > 32u) {
+            long_list[atomicAdd(s_nlong, 1u)] = p;
+            continue;
+        }
+        uint32_t v[32];
+        for (uint32_t k = 0; k < len; ++k) v[k] = t.pb[a + k];
+        for (uint32_t k = 1; k < len; ++k) {
+            const uint32_t x = v[k];
+            int m = (int)k - 1;
+            while (m >= 0 && v[m] > x) {
+                v[m + 1] = v[m];
+                --m;
+            }
+            v[m + 1] = x;
+        }
+        for (uint32_t k = 0; k < len; ++k) t.pb[a + k] = v[k];
+    }
+    __syncthreads();
+    const uint32_t nlong = *s_nlong;
+    for (uint32_t q = 0; q < nlong; ++q) {
+        const uint32_t p = long_list[q];
+        const uint32_t a = t.offsets[lo + p], len = cnt[p];
+        uint32_t p2 = 1;
+        while (p2 < len) p2 <<= 1;
+        if (p2 > scratch_words) {  // cannot happen: a list is shorter than the chunk
+            if (tid == 0) atomicOr(t.err, kErrIndexOverflow);
+            continue;
+        }
+        for (uint32_t k = tid; k < p2; k += nt) scratch[k] = k < len ? t.pb[a + k] : 0xFFFFFFFFu;
+        __syncthreads();
+        for (uint32_t size = 2; size <= p2; size <<= 1) {
+            for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+                for (uint32_t u = tid; u < p2 / 2u; u += nt) {
+                    const uint32_t i = 2u * u - (u & (stride - 1u)), j = i + stride;
+                    const uint32_t x = scratch[i], y = scratch[j];
+                    if ((x > y) == ((i & size) == 0u)) {
+                        scratch[i] = y;
+                        scratch[j] = x;
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        for (uint32_t k = tid; k < len; k += nt) t.pb[a + k] = scratch[k];
+        __syncthreads();
+    }
+    for (uint32_t p = tid; p < nb; p += nt) {
+        const uint32_t a = t.offsets[lo + p], len = cnt[p];
+        for (uint32_t k = a; k < a + len && k < t.cap; ++k) t.pairs[k] = DioPair{lo + p, t.pb[k]};
+    }
+}
+
 template <class R, bool WRITE>
 __global__ void __launch_bounds__(kSceneTreeThreads)
     k_scene_tree(const A4<R>* aabb_min, const A4<R>* aabb_max, A4<R>* g_leaf_min, A4<R>* g_leaf_max,
@@ -497,6 +634,12 @@ __global__ void __launch_bounds__(kSceneTreeThreads)
     uint32_t* npar = lpar + cb;
     uint32_t* vis = npar + cb;  // visit flags, then per-body pair counts
     uint32_t* lroot = vis + cb;
+    // fused write pass: per-body prefix in lpar, count in npar (both unused
+    // by the write pass), the long list in lroot once the trees are walked
+    __shared__ uint32_t s_red[128];
+    __shared__ uint32_t s_nlong;
+    const bool fused = WRITE && t.fused;
+    if (fused) fused_offsets(t, lo, nb, lpar, npar, s_red);
     if (WRITE && !t.chunk_ovf[cidx]) {
         // place the scratch pairs: body a's segment starts at offsets[a]
         for (uint32_t p = tid; p < nb; p += nt) vis[p] = 0u;
@@ -507,6 +650,11 @@ __global__ void __launch_bounds__(kSceneTreeThreads)
             const uint2 ab = src[k];
             const uint32_t pos = t.offsets[ab.x] + atomicAdd(&vis[ab.x - lo], 1u);
             if (pos < t.cap) t.pb[pos] = ab.y;
+        }
+        if (fused) {
+            __syncthreads();
+            fused_emit(t, lo, nb, npar, lroot, &s_nlong, reinterpret_cast<uint32_t*>(lmn),
+                       (uint32_t)(cb * 2u * sizeof(A4<R>) / 4u));
         }
         return;
     }
@@ -596,7 +744,13 @@ __global__ void __launch_bounds__(kSceneTreeThreads)
             const uint32_t total = *s_cursor;
             t.chunk_n[cidx] = min(total, region);
             t.chunk_ovf[cidx] = total > region ? 1u : 0u;
+            t.chunk_tot[cidx] = total;
         }
+    }
+    if (fused) {
+        __syncthreads();
+        fused_emit(t, lo, nb, npar, lroot, &s_nlong, reinterpret_cast<uint32_t*>(lmn),
+                   (uint32_t)(cb * 2u * sizeof(A4<R>) / 4u));
     }
 }
 
