@@ -93,6 +93,8 @@ def parse():
     ap.add_argument("--no-tune", action="store_true", help="keep the default configuration (profiling runs)")
     ap.add_argument("--block-size", type=int, default=None, choices=[0, 640],
                     help="threads per CTA of the scene-chunk solve (0: 512); default: the autotuner's choice")
+    ap.add_argument("--primal-variant", type=int, default=None,
+                    help="primal kernel variant of the per-phase solve; default: the autotuner's choice")
     ap.add_argument("--per-phase", action="store_true",
                     help="time the per-phase solve launches as the headline (profiling the primal kernel)")
     ap.add_argument("--save-state", default=None, metavar="PATH",
@@ -443,6 +445,8 @@ def main():
         w.configure(batched_solver=abi.SOLVE_PER_PHASE)
     if args.block_size is not None:
         w.configure(block_size=args.block_size)
+    if args.primal_variant is not None:
+        w.configure(primal_variant=args.primal_variant)
     tuned = tuned_config(w)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     # the clock sampler starts with the warm-up so that its 50 ms samples

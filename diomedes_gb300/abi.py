@@ -34,7 +34,7 @@ CKPT_HEADER = np.dtype([("magic", "S8"), ("version", "<u4"), ("precision", "<u4"
                         ("n_hull", "<u4"), ("rows", "<u4"), ("pair_rows", "<u4"), ("has_container", "<u4"),
                         ("per_pair", "<u4"), ("lag_pairs", "<u4"), ("pad", "<u4"), ("steps", "<u8"),
                         ("total_bytes", "<u8")])
-PRIMAL_VARIANTS = 10  # DIO_PRIMAL_VARIANTS
+PRIMAL_VARIANTS = 11  # DIO_PRIMAL_VARIANTS
 XFORM_POSE, XFORM_MAT4 = 0, 1  # DIO_XFORM_*
 DEBUG_EPA_NO_FIRST_WAIT = 1  # DIO_DEBUG_EPA_NO_FIRST_WAIT (DioConfig.debug_flags, tests only)
 SOLVE_AUTO, SOLVE_PER_PHASE = 0, 1  # DioSolveLaunch (DioConfig.batched_solver)

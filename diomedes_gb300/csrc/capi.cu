@@ -457,10 +457,15 @@ int dio_autotune(DioCtx* ctx, const DioAvbdOptions* options, uint32_t trial_step
         return time_steps(ctx, e, options, trial_steps, ms);
     };
     // 1) the solve launch: one scene-chunk launch (where the world allows
-    // it) against the per-phase launches, at the default shape and period
+    // it) against the per-phase launches, at the default shape and period;
+    // a world without the scene-chunk solve takes the per-phase launches
+    // under either setting, so only those are timed (and the primal shapes
+    // after them)
     double best_ms = 1e300;
     DioConfig best_cfg = cfg;
+    const bool chunkable = e->chunk_solve_possible();
     for (uint32_t solve : {(uint32_t)DIO_SOLVE_AUTO, (uint32_t)DIO_SOLVE_PER_PHASE}) {
+        if (!chunkable && solve == DIO_SOLVE_AUTO) continue;
         DioConfig c = cfg;
         c.batched_solver = solve;
         double ms = 0.0;

@@ -65,6 +65,8 @@ struct EngineBase {
     virtual int world_sizes(uint32_t* n, uint32_t* n_dyn, uint32_t* n_joints, uint32_t* n_scenes) = 0;
     virtual void set_stream(cudaStream_t s) = 0;
     virtual void set_config(const DioConfig& c) = 0;
+    // every scene of the uploaded world fits the scene-chunk solve
+    virtual bool chunk_solve_possible() const = 0;
 
     std::string err;
 };

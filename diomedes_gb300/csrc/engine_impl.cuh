@@ -584,6 +584,8 @@ class Engine final : public EngineBase {
         DIO_CK(cudaFuncSetAttribute(k_scene_tree<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tree_bytes));
         DIO_CK(cudaFuncSetAttribute(k_chunk_build<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)chunk_build_bytes<R>()));
+        DIO_CK(cudaFuncSetAttribute(k_primal_warp<P, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)primal_warp_smem<R>()));
         DIO_CK(cudaFuncSetAttribute(k_solve_chunks<P, R, kChunkThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)chunk_smem_bytes<P>(solve_chunk_cap<P>())));
         DIO_CK(cudaFuncSetAttribute(k_solve_chunks<P, R, kChunkThreadsWide>,
@@ -1352,6 +1354,7 @@ class Engine final : public EngineBase {
     }
     // the whole solve of a world step as one launch (k_solve_chunks)
     bool use_chunk_solve() const { return chunk_world_ && cfg_.batched_solver == DIO_SOLVE_AUTO; }
+    bool chunk_solve_possible() const override { return chunk_world_; }
     int solve_chunks(const SolveParams<R>& o) {
         const uint32_t cap = solve_chunk_max_;  // shared memory sized to the largest chunk
         cudaEvent_t e0 = span_begin();

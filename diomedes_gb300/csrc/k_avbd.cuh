@@ -267,11 +267,13 @@ __device__ __forceinline__ void row_forces(const RowDual<P, R>& du, R mu, R c0, 
     }
 }
 
-// One contact row seen from body i (avbd/src/lib.rs:321-418).
+// One contact row seen from body i (avbd/src/lib.rs:321-418): its three
+// stamps (normal, tangent 1, tangent 2) as Jacobian rows (jl, ja), stiffness
+// k and force f.
 template <class P, class R, class F>
-__device__ __forceinline__ void primal_row_core(const RowStatic<R>& rs, const RowDual<P, R>& du, uint32_t oth,
-                                                const F& fetch, Q4<R> sqr, V3<R> dqsl, V3<R> dqsa, R k_alpha,
-                                                Block6<R>& B) {
+__device__ __forceinline__ void primal_row_terms(const RowStatic<R>& rs, const RowDual<P, R>& du, uint32_t oth,
+                                                 const F& fetch, Q4<R> sqr, V3<R> dqsl, V3<R> dqsa, R k_alpha,
+                                                 V3<R> jl[3], V3<R> ja[3], R k[3], R f[3]) {
     const bool container = oth == kContainer;
     const bool is_a = container || !(oth & kIsB);
     const uint32_t other = oth & ~kIsB;
@@ -299,9 +301,28 @@ __device__ __forceinline__ void primal_row_core(const RowStatic<R>& rs, const Ro
     const RowDual<Fq, R> dv{du.penalty, A4<Fq>{Fq(du.lambda.x), Fq(du.lambda.y), Fq(du.lambda.z), Fq(0)}};
     Fq f0, f1, f2, tm, bounds;
     row_forces(dv, rs.n.w, c0, c1, c2, f0, f1, f2, tm, bounds);
-    stamp(B, r0, j0, du.penalty.x, R(f0));
-    stamp(B, r1, j1, du.penalty.y, R(f1));
-    stamp(B, r2, j2, du.penalty.z, R(f2));
+    jl[0] = r0;
+    jl[1] = r1;
+    jl[2] = r2;
+    ja[0] = j0;
+    ja[1] = j1;
+    ja[2] = j2;
+    k[0] = du.penalty.x;
+    k[1] = du.penalty.y;
+    k[2] = du.penalty.z;
+    f[0] = R(f0);
+    f[1] = R(f1);
+    f[2] = R(f2);
+}
+template <class P, class R, class F>
+__device__ __forceinline__ void primal_row_core(const RowStatic<R>& rs, const RowDual<P, R>& du, uint32_t oth,
+                                                const F& fetch, Q4<R> sqr, V3<R> dqsl, V3<R> dqsa, R k_alpha,
+                                                Block6<R>& B) {
+    V3<R> jl[3], ja[3];
+    R k[3], f[3];
+    primal_row_terms<P, R>(rs, du, oth, fetch, sqr, dqsl, dqsa, k_alpha, jl, ja, k, f);
+#pragma unroll
+    for (int s = 0; s < 3; ++s) stamp(B, jl[s], ja[s], k[s], f[s]);
 }
 template <class P, class R, class F>
 __device__ __forceinline__ void primal_row_f(const DevWorld<P, R>& w, uint32_t r, uint32_t oth, const F& fetch,
@@ -421,16 +442,11 @@ __device__ __forceinline__ void primal_jview_f(const JView& jv, const F& fetch, 
     primal_jview_p<P, R>(jv, fetch.pos(jv.other), fetch.rot(jv.other), sp, sq, sqr, B);
 }
 
-// avbd_primal for one body: reads the snapshot through `fetch` and stores
-// the new pose through it.  [k0, k1) is the body's joint-view range.
-template <class P, class R, class F, class Rows = RowsFromWorld>
-__device__ __forceinline__ void primal_body_f(const DevWorld<P, R>& w, uint32_t i, uint32_t k0, uint32_t k1,
-                                              const SolveParams<R>& o, const F& fetch, const Rows& rows = Rows()) {
-    const A4<R> inv = w.inv[i];
-    if (inv.w == R(0)) return;
-    const V3<P> sp = xyz(fetch.pos(i));
-    const Q4<P> sq = quat(fetch.rot(i));
-    const Q4<R> sqr = castq<R>(sq);
+// The inertial start of body i's 6x6 system: diagonal M/dt^2, I/dt^2 and
+// the gradient toward the inertial pose.
+template <class P, class R>
+__device__ __forceinline__ void primal_inertia(const DevWorld<P, R>& w, uint32_t i, const A4<R>& inv, V3<P> sp,
+                                               Q4<R> sqr, const SolveParams<R>& o, Block6<R>& B) {
     R mdt2;
     V3<R> idt2;
     if (w.mdt2) {
@@ -444,7 +460,6 @@ __device__ __forceinline__ void primal_body_f(const DevWorld<P, R>& w, uint32_t 
         mdt2 = mass / dt2;
         idt2 = divs(moment, dt2);
     }
-    Block6<R> B;
 #pragma unroll
     for (int k = 0; k < 21; ++k) B.h[k] = R(0);
     B.h[tri(0, 0)] = mdt2;
@@ -461,14 +476,13 @@ __device__ __forceinline__ void primal_body_f(const DevWorld<P, R>& w, uint32_t 
     B.g[3] = ra.x;
     B.g[4] = ra.y;
     B.g[5] = ra.z;
-    const uint32_t j0 = w.row_off[i], j1 = w.row_off[i + 1];
-    if (j0 < j1) {
-        // displacement since the step start: read only by contact rows
-        const V3<R> dqsl = cast3<R>(sub(sp, xyz(fetch.ipos(i))));
-        const V3<R> dqsa = ang_diff(sqr, castq<R>(quat(fetch.irot(i))));
-        const R k_alpha = R(1) - o.alpha;
-        for (uint32_t j = j0; j < j1; ++j) rows(w, i, w.row_idx[j], w.row_oth[j], fetch, sqr, dqsl, dqsa, k_alpha, B);
-    }
+}
+
+// Joint rows, the 6x6 solve and the pose update of body i (the tail of
+// avbd_primal)
+template <class P, class R, class F>
+__device__ __forceinline__ void primal_finish(const DevWorld<P, R>& w, uint32_t i, uint32_t k0, uint32_t k1,
+                                              const F& fetch, V3<P> sp, Q4<P> sq, Q4<R> sqr, Block6<R>& B) {
     for (uint32_t k = k0; k < k1; ++k) {
         const JView jv = w.jview[k];
         primal_jview_f<P, R>(jv, fetch, sp, sq, sqr, B);
@@ -480,6 +494,29 @@ __device__ __forceinline__ void primal_body_f(const DevWorld<P, R>& w, uint32_t 
         fetch.store(i, np, packq(quat_step(sq, V3<P>{dx[3], dx[4], dx[5]})));
     else
         fetch.store(i, np, packq(quat_step_split<P, R>(sq, V3<R>{dx[3], dx[4], dx[5]})));
+}
+
+// avbd_primal for one body: reads the snapshot through `fetch` and stores
+// the new pose through it.  [k0, k1) is the body's joint-view range.
+template <class P, class R, class F, class Rows = RowsFromWorld>
+__device__ __forceinline__ void primal_body_f(const DevWorld<P, R>& w, uint32_t i, uint32_t k0, uint32_t k1,
+                                              const SolveParams<R>& o, const F& fetch, const Rows& rows = Rows()) {
+    const A4<R> inv = w.inv[i];
+    if (inv.w == R(0)) return;
+    const V3<P> sp = xyz(fetch.pos(i));
+    const Q4<P> sq = quat(fetch.rot(i));
+    const Q4<R> sqr = castq<R>(sq);
+    Block6<R> B;
+    primal_inertia(w, i, inv, sp, sqr, o, B);
+    const uint32_t j0 = w.row_off[i], j1 = w.row_off[i + 1];
+    if (j0 < j1) {
+        // displacement since the step start: read only by contact rows
+        const V3<R> dqsl = cast3<R>(sub(sp, xyz(fetch.ipos(i))));
+        const V3<R> dqsa = ang_diff(sqr, castq<R>(quat(fetch.irot(i))));
+        const R k_alpha = R(1) - o.alpha;
+        for (uint32_t j = j0; j < j1; ++j) rows(w, i, w.row_idx[j], w.row_oth[j], fetch, sqr, dqsl, dqsa, k_alpha, B);
+    }
+    primal_finish(w, i, k0, k1, fetch, sp, sq, sqr, B);
 }
 
 template <class P, class R>
@@ -522,11 +559,99 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_primal(DevWorld<P, R> w, int rd
         primal_body(w, w.dyn_list[t], rd, o);
 }
 
+// Warp per dynamic body, for worlds whose bodies carry many contact rows
+// (a thread per body walks its rows one dependent gather after another):
+// lane l forms the three stamps of the body's incidence j0 + 32 q + l and
+// writes their 27 products each (21 Hessian terms, 6 gradient terms, the
+// products exactly as stamp() forms them) to shared memory; lane e < 27 then
+// adds entry e of the 6x6 system over the incidences and stamps in the
+// serial order -- the same sums, term for term, as primal_body_f.  Lane 0
+// adds the joint rows and solves.
+constexpr int kPrimalWarpWarps = 4;
+template <class R>
+__host__ __device__ constexpr size_t primal_warp_smem() {
+    return (size_t)kPrimalWarpWarps * 32 * 3 * 28 * sizeof(R);
+}
+template <class P, class R>
+__global__ void __launch_bounds__(kPrimalWarpWarps * 32) k_primal_warp(DevWorld<P, R> w, int rd, int wr,
+                                                                        SolveParams<R> o) {
+    pdl_enter();
+    extern __shared__ __align__(16) unsigned char primal_warp_smem_raw[];
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    R* prod = reinterpret_cast<R*>(primal_warp_smem_raw) + (size_t)warp * 32 * 3 * 28;  // [32][3][28]
+    const GlobalFetch<P, R> fetch{w, rd};
+    const uint32_t nwarps = gridDim.x * kPrimalWarpWarps;
+    for (uint32_t t = blockIdx.x * kPrimalWarpWarps + warp; t < w.n_dyn; t += nwarps) {
+        const uint32_t i = w.dyn_list[t];
+        const A4<R> inv = w.inv[i];
+        if (inv.w == R(0)) continue;  // warp-uniform
+        const V3<P> sp = xyz(fetch.pos(i));
+        const Q4<P> sq = quat(fetch.rot(i));
+        const Q4<R> sqr = castq<R>(sq);
+        Block6<R> B;
+        primal_inertia(w, i, inv, sp, sqr, o, B);
+        // lane e holds entry e: h[0..20], then g[0..5]
+        R acc = R(0);
+#pragma unroll
+        for (int e = 0; e < 21; ++e)
+            if (lane == (uint32_t)e) acc = B.h[e];
+#pragma unroll
+        for (int e = 0; e < 6; ++e)
+            if (lane == (uint32_t)(21 + e)) acc = B.g[e];
+        const uint32_t j0 = w.row_off[i], j1 = w.row_off[i + 1];
+        if (j0 < j1) {
+            const V3<R> dqsl = cast3<R>(sub(sp, xyz(fetch.ipos(i))));
+            const V3<R> dqsa = ang_diff(sqr, castq<R>(quat(fetch.irot(i))));
+            const R k_alpha = R(1) - o.alpha;
+            for (uint32_t base = j0; base < j1; base += 32u) {
+                const uint32_t cnt = min(32u, j1 - base);
+                if (lane < cnt) {
+                    const uint32_t j = base + lane;
+                    const uint32_t r = w.row_idx[j];
+                    V3<R> jl[3], ja[3];
+                    R k[3], f[3];
+                    primal_row_terms<P, R>(w.rs[r], w.rd[r], w.row_oth[j], fetch, sqr, dqsl, dqsa, k_alpha, jl, ja,
+                                           k, f);
+                    R* mine = prod + lane * (3 * 28);
+#pragma unroll
+                    for (int s = 0; s < 3; ++s) {
+                        const R J[6] = {jl[s].x, jl[s].y, jl[s].z, ja[s].x, ja[s].y, ja[s].z};
+#pragma unroll
+                        for (int a = 0; a < 6; ++a)
+#pragma unroll
+                            for (int b = 0; b <= a; ++b) mine[s * 28 + tri(a, b)] = J[a] * J[b] * k[s];
+#pragma unroll
+                        for (int a = 0; a < 6; ++a) mine[s * 28 + 21 + a] = J[a] * f[s];
+                    }
+                }
+                __syncwarp();
+                if (lane < 27u)
+                    for (uint32_t q = 0; q < cnt; ++q) {
+                        const R* pq = prod + q * (3 * 28) + lane;
+                        acc = acc + pq[0];
+                        acc = acc + pq[28];
+                        acc = acc + pq[56];
+                    }
+                __syncwarp();
+            }
+        }
+#pragma unroll
+        for (int e = 0; e < 21; ++e) B.h[e] = __shfl_sync(0xFFFFFFFFu, acc, e);
+#pragma unroll
+        for (int e = 0; e < 6; ++e) B.g[e] = __shfl_sync(0xFFFFFFFFu, acc, 21 + e);
+        if (lane == 0u) {
+            const uint32_t k0 = w.n_joints ? w.joint_off[i] : 0u, k1 = w.n_joints ? w.joint_off[i + 1] : 0u;
+            primal_finish(w, i, k0, k1, fetch, sp, sq, sqr, B);
+        }
+    }
+}
+
 // variants: 0-5 k_primal over the dynamic-body list with {threads per CTA,
-// min CTAs per SM}; 6-9 k_primal_tile over body tiles
+// min CTAs per SM}; 6-9 k_primal_tile over body tiles; 10 k_primal_warp
 constexpr int kPrimalVariants = DIO_PRIMAL_VARIANTS;
 constexpr int kPrimalShape[kPrimalVariants][2] = {{128, 4}, {128, 5}, {128, 6}, {256, 2}, {256, 3},
-                                                  {64, 10}, {128, 5}, {128, 6}, {256, 3}, {64, 10}};
+                                                  {64, 10}, {128, 5}, {128, 6}, {256, 3}, {64, 10},
+                                                  {kPrimalWarpWarps * 32, 1}};
 
 template <class P, class R>
 inline void launch_primal(int variant, bool pdl, const DevWorld<P, R>& w, int rd, int wr, const SolveParams<R>& o,
@@ -560,6 +685,10 @@ inline void launch_primal(int variant, bool pdl, const DevWorld<P, R>& w, int rd
             break;
         case 9:
             launch_k(pdl, k_primal_tile<P, R, 64, 10>, grid_for(w.n, 64), 64, 0, s, w, rd, wr, o);
+            break;
+        case 10:
+            launch_k(pdl, k_primal_warp<P, R>, grid_for(nd, kPrimalWarpWarps), kPrimalWarpWarps * 32,
+                     primal_warp_smem<R>(), s, w, rd, wr, o);
             break;
         default:
             launch_k(pdl, k_primal<P, R, 128, 5>, grid(128), 128, 0, s, w, rd, wr, o);

@@ -222,7 +222,7 @@ enum DioPrecision {
 };
 
 /* number of primal kernel variants selectable by DioConfig.primal_variant */
-#define DIO_PRIMAL_VARIANTS 10
+#define DIO_PRIMAL_VARIANTS 11
 
 typedef struct DioConfig {
     uint32_t solver_mode;       /* DioSolverMode                          */

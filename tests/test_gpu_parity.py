@@ -635,14 +635,28 @@ def test_hull_pairs_with_staged_vertices_match_oracle():
     assert np.array_equal(_bits(got), _bits(ref))
 
 
+def _platform_scene():
+    """A dynamic plate on the ground carrying a 4 x 4 grid of cubes: the plate
+    has 16 x 4 contact rows plus its ground rows, over two 32-row rounds of
+    the warp-per-body primal."""
+    items = [ph.box((0.0, 0.1, 0.0), (2.2, 0.1, 2.2), 40.0)]
+    for gx in range(4):
+        for gz in range(4):
+            items.append(ph.cube((-1.5 + gx * 1.0, 0.2 + 0.25 + 0.004, -1.5 + gz * 1.0), 0.25, 2.0))
+    b, st = ph.pack_bodies(items)
+    return scenes.Scene("platform", b, st, containers=[scenes.ground()], options=ph.avbd_options(), steps=8)
+
+
 @pytest.mark.parametrize("variant", range(abi.PRIMAL_VARIANTS))
 def test_every_primal_variant_matches_oracle(variant):
-    """Launch shapes, tiles, per-position records and paired joint loads all
-    compute the oracle's bits (joints of every kind, contacts, ground)."""
-    sc = scenes.pack([scenes.box_demo(), scenes.constraints_demo(), scenes.pyramid(levels=4)])
+    """Launch shapes, tiles, per-position records, paired joint loads and the
+    warp-per-body sums all compute the oracle's bits (joints of every kind,
+    contacts, ground, a body with more than 64 rows); the per-phase solve is
+    the one that runs the primal variants."""
+    sc = scenes.pack([scenes.box_demo(), scenes.constraints_demo(), scenes.pyramid(levels=4), _platform_scene()])
     ow = O.World(sc)
     ow.step(sc.options, 8)
-    with _world(sc, primal_variant=variant) as w:
+    with _world(sc, primal_variant=variant, batched_solver=abi.SOLVE_PER_PHASE) as w:
         w.step(sc.options, 8)
         gb, gs = w.download()
     rb, rs = ow.download()
