@@ -59,7 +59,7 @@ struct Counters {
     uint32_t long_count;      // CSR segments too long for the in-thread sort
     uint32_t dyn_changed;     // a state update turned a body static or dynamic
     uint32_t prev_pairs;      // pairs of the previous step (contact-lag rows)
-    uint32_t pad[1];
+    uint32_t traverse_pairs;  // pairs appended by the global trees' count pass
 };
 
 // Static part of one contact row (80 B at R = float):

@@ -499,6 +499,7 @@ class Engine final : public EngineBase {
         DIO_TRY(alloc(&lb_node_min_, N));
         DIO_TRY(alloc(&lb_node_max_, N));
         DIO_TRY(alloc(&lb_pb_, PP));
+        DIO_TRY(alloc(&lb_gscratch_, PP));
         DIO_TRY(alloc(&lb_long_, N));
         DIO_TRY(alloc(&lb_long_count_, 1));
         for (int b = 0; b < 2; ++b) {
@@ -1536,22 +1537,31 @@ class Engine final : public EngineBase {
         }
         if (global_path) {
             DIO_CK(cudaMemsetAsync(lb_visits_, 0, (size_t)n * 4, stream_));
+            if (!world_step_) DIO_CK(cudaMemsetAsync(&ctr_->traverse_pairs, 0, 4, stream_));  // else k_roll_counters
             k_refit<R><<<g, 256, 0, stream_>>>(w_.aabb_min, w_.aabb_max, lb_leaf_, scenes_, w_.scene, n,
                                                lb_children_, lb_parent_, lb_leaf_min_, lb_leaf_max_, lb_node_min_,
-                                               lb_node_max_, lb_visits_, tcap_skip);
-            k_traverse<R><<<gt, 128, 0, stream_>>>(lb_leaf_, scenes_, w_.scene, n, lb_children_, lb_leaf_min_,
-                                                   lb_leaf_max_, lb_node_min_, lb_node_max_, counts_, offsets_,
-                                                   lb_pb_, w_.max_pairs, false, &ctr_->error_flags, tcap_skip);
+                                               lb_node_max_, lb_visits_, tcap_skip, counts_);
+            k_traverse_count<R><<<gt, 128, 0, stream_>>>(lb_leaf_, scenes_, w_.scene, n, lb_children_, lb_leaf_min_,
+                                                         lb_leaf_max_, lb_node_min_, lb_node_max_, counts_,
+                                                         lb_gscratch_, w_.max_pairs, &ctr_->traverse_pairs,
+                                                         &ctr_->error_flags, tcap_skip);
             launches_ += 2;
         }
         if (!world_step_) DIO_CK(cudaMemsetAsync(counts_ + n, 0, 4, stream_));  // else k_roll_counters
         DIO_CK(ss_.scan(counts_, offsets_, n + 1, pdl(), stream_));
         DIO_CK(scene_tree(true));
         if (global_path) {
-            k_traverse<R><<<gt, 128, 0, stream_>>>(lb_leaf_, scenes_, w_.scene, n, lb_children_, lb_leaf_min_,
-                                                   lb_leaf_max_, lb_node_min_, lb_node_max_, counts_, offsets_,
-                                                   lb_pb_, w_.max_pairs, true, &ctr_->error_flags, tcap_skip);
-            ++launches_;
+            // the scratch pairs to their offsets (counts_ taken down to zero),
+            // or, when the scratch overflowed, the full write traversal
+            DIO_CK(launch_k(pdl(), k_place_scratch, sms_ * 4, 256, 0, stream_, (const uint2*)lb_gscratch_,
+                            (const uint32_t*)&ctr_->traverse_pairs, w_.max_pairs, (const uint32_t*)offsets_, counts_,
+                            lb_pb_, w_.max_pairs));
+            DIO_CK(launch_k(pdl(), k_traverse<R>, gt, 128, 0, stream_, (const uint32_t*)lb_leaf_,
+                            (const SceneDesc*)scenes_, (const uint32_t*)w_.scene, n, (const uint2*)lb_children_,
+                            (const A4<R>*)lb_leaf_min_, (const A4<R>*)lb_leaf_max_, (const A4<R>*)lb_node_min_,
+                            (const A4<R>*)lb_node_max_, (const uint32_t*)offsets_, lb_pb_, w_.max_pairs,
+                            (const uint32_t*)&ctr_->traverse_pairs, w_.max_pairs, &ctr_->error_flags, tcap_skip));
+            launches_ += 2;
         }
         DIO_CK(launch_k(pdl(), k_pairs_total, 1, 1, 0, stream_, ctr_,
                         (const uint32_t*)(offsets_ + n), w_.max_pairs));
@@ -2325,6 +2335,7 @@ class Engine final : public EngineBase {
     uint2* lb_children_ = nullptr;
     A4<R>*lb_leaf_min_ = nullptr, *lb_leaf_max_ = nullptr, *lb_node_min_ = nullptr, *lb_node_max_ = nullptr;
     uint32_t *lb_pb_ = nullptr, *lb_long_ = nullptr, *lb_long_count_ = nullptr;
+    uint2* lb_gscratch_ = nullptr;  // pairs of the global trees' count pass
     double primal_ms_ = 0.0, dual_ms_ = 0.0;
     double phase_ms_[4] = {0.0, 0.0, 0.0, 0.0};  // broad, narrow, rows, solve
     uint32_t primal_n_ = 0, dual_n_ = 0, solve_chunk_n_ = 0;

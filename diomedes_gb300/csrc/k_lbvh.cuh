@@ -146,6 +146,16 @@ __device__ __forceinline__ A4<double> ldcg4(const A4<double>* p) {
     return {a.x, a.y, b.x, b.y};
 }
 
+// a 32-bit tag in (and out of) the unused w slot of a box corner, as bits
+__device__ __forceinline__ uint32_t tag_of(const A4<float>& a) { return __float_as_uint(a.w); }
+__device__ __forceinline__ uint32_t tag_of(const A4<double>& a) { return (uint32_t)__double_as_longlong(a.w); }
+template <class R>
+__device__ __forceinline__ R tag_bits(uint32_t v);
+template <>
+__device__ __forceinline__ float tag_bits<float>(uint32_t v) { return __uint_as_float(v); }
+template <>
+__device__ __forceinline__ double tag_bits<double>(uint32_t v) { return __longlong_as_double((long long)v); }
+
 // Internal node k of a scene whose sorted keys are seg[0, ns) and whose
 // slots start at global slot lo: node k lives at slot lo + k; child codes
 // are global slots, leaves flagged with kLeafFlag (leaf = sorted position);
@@ -189,16 +199,19 @@ static __global__ void k_karras(const uint32_t* keys, const SceneDesc* scenes, c
     }
 }
 
-// leaf boxes in sorted order, then bottom-up unions
+// leaf boxes in sorted order, then bottom-up unions; a node's max corner
+// carries in w its highest leaf position (as bits).  counts: the per-body
+// pair counters of the count pass, cleared here.
 template <class R>
 __global__ void k_refit(const A4<R>* mn, const A4<R>* mx, const uint32_t* leaf_body, const SceneDesc* scenes,
                         const uint32_t* scene_of_pos, uint32_t n, const uint2* children, const uint32_t* parent,
                         A4<R>* leaf_min, A4<R>* leaf_max, A4<R>* node_min, A4<R>* node_max, uint32_t* visits,
-                        uint32_t skip_max) {
+                        uint32_t skip_max, uint32_t* counts) {
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
         const SceneDesc sc = scenes[scene_of_pos[p]];
         if (sc.body_hi - sc.body_lo <= skip_max) continue;  // k_scene_tree's scene
         uint32_t b = leaf_body[p];
+        counts[b] = 0u;
         leaf_min[p] = mn[b];
         leaf_max[p] = mx[b];
         if (sc.body_hi - sc.body_lo < 2) continue;
@@ -215,8 +228,9 @@ __global__ void k_refit(const A4<R>* mn, const A4<R>* mx, const uint32_t* leaf_b
             uint32_t li = c.x & ~kLeafFlag, ri = c.y & ~kLeafFlag;
             // boxes written by other CTAs in this launch: read through L2
             A4<R> a0 = ldcg4(&lmn[li]), a1 = ldcg4(&lmx[li]), b0 = ldcg4(&rmn[ri]), b1 = ldcg4(&rmx[ri]);
+            const uint32_t hi = max((c.x & kLeafFlag) ? li : tag_of(a1), (c.y & kLeafFlag) ? ri : tag_of(b1));
             node_min[node] = A4<R>{fmin_(a0.x, b0.x), fmin_(a0.y, b0.y), fmin_(a0.z, b0.z), R(0)};
-            node_max[node] = A4<R>{fmax_(a1.x, b1.x), fmax_(a1.y, b1.y), fmax_(a1.z, b1.z), R(0)};
+            node_max[node] = A4<R>{fmax_(a1.x, b1.x), fmax_(a1.y, b1.y), fmax_(a1.z, b1.z), tag_bits<R>(hi)};
             __threadfence();
             if (node == sc.body_lo) break;  // scene root
             node = parent[node];
@@ -226,66 +240,139 @@ __global__ void k_refit(const A4<R>* mn, const A4<R>* mx, const uint32_t* leaf_b
 
 constexpr int kStack = 64;
 
-// count (write_out false) or write partner lists; per body i the partners j
-// land unsorted in pb[offsets[i] ...]
+// Count pass of the global trees (scenes beyond the shared-memory trees):
+// the leaf at position p visits only the subtrees holding positions above
+// p (a node's highest leaf position is its max corner's w), so each
+// overlapping pair is found once, by its lower position; it is counted for
+// body a = min(i, j) and appended as (a, b) to the pair scratch through a
+// warp-aggregated cursor, from which the write pass places it without
+// walking the trees again.
+template <class R>
+__global__ void __launch_bounds__(128)
+    k_traverse_count(const uint32_t* leaf_body, const SceneDesc* scenes, const uint32_t* scene_of_pos, uint32_t n,
+                     const uint2* children, const A4<R>* leaf_min, const A4<R>* leaf_max, const A4<R>* node_min,
+                     const A4<R>* node_max, uint32_t* counts, uint2* scratch, uint32_t scratch_cap,
+                     uint32_t* scratch_n, uint32_t* err, uint32_t skip_max) {
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        const SceneDesc sc = scenes[scene_of_pos[p]];
+        if (sc.body_hi - sc.body_lo <= skip_max) continue;  // k_scene_tree's scene
+        if (sc.body_hi - sc.body_lo < 2) continue;
+        const uint32_t i = leaf_body[p];
+        const A4<R> qmn = leaf_min[p], qmx = leaf_max[p];
+        uint32_t stack[kStack];
+        int sp = 0;
+        uint32_t node = sc.body_lo;  // root
+        while (true) {
+            const uint2 c = children[node];
+            const uint32_t ch[2] = {c.x, c.y};
+            uint32_t push = 0;
+            uint32_t next[2];
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const uint32_t x = ch[k];
+                const uint32_t idx = x & ~kLeafFlag;
+                if (x & kLeafFlag) {
+                    if (idx > p && overlap(qmn, qmx, leaf_min[idx], leaf_max[idx])) {
+                        const uint32_t j = leaf_body[idx];
+                        const uint32_t a = min(i, j), b = max(i, j);
+                        atomicAdd(&counts[a], 1u);
+                        const uint32_t slot = warp_append(scratch_n);
+                        if (slot < scratch_cap) scratch[slot] = make_uint2(a, b);
+                    }
+                } else {
+                    const A4<R> bmx = node_max[idx];
+                    if (tag_of(bmx) > p && overlap(qmn, qmx, node_min[idx], bmx)) next[push++] = idx;
+                }
+            }
+            if (push == 0) {
+                if (sp == 0) break;
+                node = stack[--sp];
+            } else {
+                node = next[0];
+                if (push == 2) {
+                    if (sp < kStack)
+                        stack[sp++] = next[1];
+                    else
+                        atomicOr(err, kErrIndexOverflow);
+                }
+            }
+        }
+    }
+}
+
+// Write pass of the global trees from the count pass's scratch: pair (a, b)
+// goes to offsets[a] + (a's remaining count, taken down by one; the
+// segment is sorted afterwards).  Nothing when the scratch overflowed: the
+// full write traversal (k_traverse) runs instead.
+static __global__ void k_place_scratch(const uint2* scratch, const uint32_t* scratch_n, uint32_t scratch_cap,
+                                       const uint32_t* offsets, uint32_t* remaining, uint32_t* pb, uint32_t cap) {
+    pdl_enter();
+    const uint32_t m = *scratch_n;
+    if (m > scratch_cap) return;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
+        const uint2 ab = scratch[k];
+        const uint32_t pos = offsets[ab.x] + atomicSub(&remaining[ab.x], 1u) - 1u;
+        if (pos < cap) pb[pos] = ab.y;
+    }
+}
+
+// Full write traversal of the global trees, only when the count pass's
+// scratch overflowed: per body i the partners j > i land unsorted in
+// pb[offsets[i] ...]
 template <class R>
 __global__ void __launch_bounds__(128) k_traverse(const uint32_t* leaf_body, const SceneDesc* scenes,
                                                   const uint32_t* scene_of_pos, uint32_t n, const uint2* children,
                                                   const A4<R>* leaf_min, const A4<R>* leaf_max,
-                                                  const A4<R>* node_min, const A4<R>* node_max, uint32_t* counts,
-                                                  const uint32_t* offsets, uint32_t* pb, uint32_t cap, bool write_out,
-                                                  uint32_t* err, uint32_t skip_max) {
+                                                  const A4<R>* node_min, const A4<R>* node_max,
+                                                  const uint32_t* offsets, uint32_t* pb, uint32_t cap,
+                                                  const uint32_t* scratch_n, uint32_t scratch_cap, uint32_t* err,
+                                                  uint32_t skip_max) {
+    pdl_enter();
+    if (*scratch_n <= scratch_cap) return;
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
         const SceneDesc sc = scenes[scene_of_pos[p]];
         if (sc.body_hi - sc.body_lo <= skip_max) continue;  // k_scene_tree's scene
+        if (sc.body_hi - sc.body_lo < 2) continue;
         const uint32_t i = leaf_body[p];
-        uint32_t found = 0;
-        uint32_t out = write_out ? offsets[i] : 0;
-        if (sc.body_hi - sc.body_lo >= 2) {
-            const A4<R> qmn = leaf_min[p], qmx = leaf_max[p];
-            uint32_t stack[kStack];
-            int sp = 0;
-            uint32_t node = sc.body_lo;  // root
-            while (true) {
-                uint2 c = children[node];
-                uint32_t ch[2] = {c.x, c.y};
-                uint32_t push = 0;
-                uint32_t next[2];
+        uint32_t out = offsets[i];
+        const A4<R> qmn = leaf_min[p], qmx = leaf_max[p];
+        uint32_t stack[kStack];
+        int sp = 0;
+        uint32_t node = sc.body_lo;  // root
+        while (true) {
+            uint2 c = children[node];
+            uint32_t ch[2] = {c.x, c.y};
+            uint32_t push = 0;
+            uint32_t next[2];
 #pragma unroll
-                for (int k = 0; k < 2; ++k) {
-                    uint32_t x = ch[k];
-                    uint32_t idx = x & ~kLeafFlag;
-                    if (x & kLeafFlag) {
-                        if (overlap(qmn, qmx, leaf_min[idx], leaf_max[idx])) {
-                            uint32_t j = leaf_body[idx];
-                            if (j > i) {
-                                if (write_out) {
-                                    if (out < cap) pb[out] = j;
-                                    ++out;
-                                } else {
-                                    ++found;
-                                }
-                            }
+            for (int k = 0; k < 2; ++k) {
+                uint32_t x = ch[k];
+                uint32_t idx = x & ~kLeafFlag;
+                if (x & kLeafFlag) {
+                    if (overlap(qmn, qmx, leaf_min[idx], leaf_max[idx])) {
+                        uint32_t j = leaf_body[idx];
+                        if (j > i) {
+                            if (out < cap) pb[out] = j;
+                            ++out;
                         }
-                    } else if (overlap(qmn, qmx, node_min[idx], node_max[idx])) {
-                        next[push++] = idx;
                     }
+                } else if (overlap(qmn, qmx, node_min[idx], node_max[idx])) {
+                    next[push++] = idx;
                 }
-                if (push == 0) {
-                    if (sp == 0) break;
-                    node = stack[--sp];
-                } else {
-                    node = next[0];
-                    if (push == 2) {
-                        if (sp < kStack)
-                            stack[sp++] = next[1];
-                        else
-                            atomicOr(err, kErrIndexOverflow);
-                    }
+            }
+            if (push == 0) {
+                if (sp == 0) break;
+                node = stack[--sp];
+            } else {
+                node = next[0];
+                if (push == 2) {
+                    if (sp < kStack)
+                        stack[sp++] = next[1];
+                    else
+                        atomicOr(err, kErrIndexOverflow);
                 }
             }
         }
-        if (!write_out) counts[i] = found;
     }
 }
 
@@ -320,15 +407,6 @@ __host__ __device__ constexpr size_t scene_tree_bytes(uint32_t cap) {
     // flag (then per-body count), leaf's scene root
     return (size_t)cap * (4 * sizeof(A4<R>) + sizeof(uint2) + 4 * sizeof(uint32_t)) + 16;
 }
-// a 32-bit tag in (and out of) the unused w slot of a box corner, as bits
-__device__ __forceinline__ uint32_t tag_of(const A4<float>& a) { return __float_as_uint(a.w); }
-__device__ __forceinline__ uint32_t tag_of(const A4<double>& a) { return (uint32_t)__double_as_longlong(a.w); }
-template <class R>
-__device__ __forceinline__ R tag_bits(uint32_t v);
-template <>
-__device__ __forceinline__ float tag_bits<float>(uint32_t v) { return __uint_as_float(v); }
-template <>
-__device__ __forceinline__ double tag_bits<double>(uint32_t v) { return __longlong_as_double((long long)v); }
 // a node's children (chunk positions with leaf flags) as one 24-bit word
 constexpr uint32_t kCwIndex = 0x7FFu, kCwLeaf = 0x800u;
 static_assert(scene_tree_cap<float>() <= kCwIndex + 1 && scene_tree_cap<double>() <= kCwIndex + 1,

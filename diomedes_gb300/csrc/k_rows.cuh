@@ -396,6 +396,7 @@ static __global__ void k_roll_counters(Counters* c, uint32_t* zero0, uint32_t* z
     c->epa_work = 0;
     c->long_count = 0;
     c->colors = 0;
+    c->traverse_pairs = 0;
 }
 
 template <class P, class R>

@@ -102,40 +102,110 @@ __device__ __forceinline__ uint32_t lb_walk(const Lookback& lb, uint32_t tile, u
     return prefix;
 }
 
-// The same for a one-column status array, one warp reading 32 lower tiles
-// per round; all 32 lanes call it and get the prefix.
+// The same for a one-column status array, one warp reading 32 x K lower
+// tiles per round (lane l the K tiles at distances l K + 1 .. l K + K);
+// all 32 lanes call it and get the prefix.
+template <int K = 1>
 __device__ __forceinline__ uint32_t lb_walk_warp(const Lookback& lb, uint32_t tile, uint32_t epoch, uint32_t lane) {
     const uint32_t tag = lb_tag(epoch);
     uint32_t prefix = 0;
-    int64_t p = (int64_t)tile - 1;
+    int64_t p = (int64_t)tile - 1;  // nearest tile of this round
     while (p >= 0) {
-        const int64_t q = p - (int64_t)lane;
-        uint32_t v = 0u, f = kLbInclusive;  // before tile 0: an inclusive 0
-        if (q >= 0) {
-            for (uint32_t polls = 0;; ++polls) {
+        uint32_t v[K], f[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const int64_t q = p - (int64_t)(lane * K + k);
+            v[k] = 0u;
+            f[k] = kLbInclusive;  // before tile 0: an inclusive 0
+            if (q >= 0) {
                 const unsigned long long s = lb_load(lb.status + q);
-                const uint32_t lo = (uint32_t)s;
-                if ((lo & ~3u) == tag && (lo & 3u) != 0u) {
-                    v = (uint32_t)(s >> 32);
-                    f = lo & 3u;
-                    break;
-                }
-                if (polls >= kLookbackPolls) {
-                    atomicOr(lb.err, kErrTimeout);
-                    break;
-                }
+                v[k] = (uint32_t)(s >> 32);
+                f[k] = ((uint32_t)s & ~3u) == tag ? ((uint32_t)s & 3u) : 0u;
             }
         }
-        const uint32_t incl = __ballot_sync(0xFFFFFFFFu, f == kLbInclusive);
+        // wait for the entries not yet published, then sum up to this lane's
+        // first inclusive entry
+        uint32_t part = 0, first = K;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const int64_t q = p - (int64_t)(lane * K + k);
+            if (first < (uint32_t)K) continue;  // beyond this lane's inclusive entry
+            for (uint32_t polls = 0; f[k] == 0u; ++polls) {
+                if (polls >= kLookbackPolls) {
+                    atomicOr(lb.err, kErrTimeout);
+                    v[k] = 0u;
+                    f[k] = kLbInclusive;
+                    break;
+                }
+                const unsigned long long s = lb_load(lb.status + q);
+                v[k] = (uint32_t)(s >> 32);
+                f[k] = ((uint32_t)s & ~3u) == tag ? ((uint32_t)s & 3u) : 0u;
+            }
+            part += v[k];
+            if (f[k] == kLbInclusive) first = (uint32_t)k;
+        }
+        const uint32_t incl = __ballot_sync(0xFFFFFFFFu, first < (uint32_t)K);
         const uint32_t upto = incl ? (uint32_t)(__ffs(incl) - 1) : 31u;
-        uint32_t x = lane <= upto ? v : 0u;
+        uint32_t x = lane <= upto ? part : 0u;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xFFFFFFFFu, x, o);
         prefix += x;
         if (incl) break;
-        p -= 32;
+        p -= 32 * K;
     }
     return prefix;
+}
+
+// Exclusive prefix of each thread's v over the launch: tiles in order, then
+// threads in order within a tile.  Every thread of the CTA calls it once per
+// tile (the CTA's tiles in increasing order); *tile_end receives the
+// inclusive prefix at the tile's end (the launch total after the last
+// tile).  s_warp holds THREADS / 32 words, s_pair 2; ep is the launch's
+// epoch (lb_epoch, stored before the first call and read after its barrier).
+template <int THREADS, int K = 1>
+__device__ __forceinline__ uint32_t tile_exclusive(uint32_t v, uint32_t tile, const uint32_t* s_ep, const Lookback& lb,
+                                                   uint32_t* s_warp, uint32_t* s_pair, uint32_t* tile_end) {
+    constexpr int NW = THREADS / 32;
+    static_assert(NW <= 32, "one warp scans the warp totals");
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t x = v;  // inclusive over the warp
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= (uint32_t)o) x += y;
+    }
+    if (lane == 31u) s_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t ep = *s_ep;
+        const uint32_t wv = lane < (uint32_t)NW ? s_warp[lane] : 0u;
+        uint32_t wi = wv;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, wi, o);
+            if (lane >= (uint32_t)o) wi += y;
+        }
+        if (lane < (uint32_t)NW) s_warp[lane] = wi - wv;
+        const uint32_t agg = __shfl_sync(0xFFFFFFFFu, wi, 31);
+        unsigned long long* slot = lb.status + tile;
+        uint32_t pre = 0u;
+        if (tile == 0u) {
+            if (lane == 0u) lb_store(slot, lb_word(agg, ep, kLbInclusive));
+        } else {
+            if (lane == 0u) lb_store(slot, lb_word(agg, ep, kLbAggregate));
+            pre = lb_walk_warp<K>(lb, tile, ep, lane);
+            if (lane == 0u) lb_store(slot, lb_word(pre + agg, ep, kLbInclusive));
+        }
+        if (lane == 0u) {
+            s_pair[0] = pre;
+            s_pair[1] = pre + agg;
+        }
+    }
+    __syncthreads();
+    const uint32_t r = s_pair[0] + s_warp[warp] + (x - v);
+    *tile_end = s_pair[1];
+    __syncthreads();  // s_warp and s_pair serve the next tile
+    return r;
 }
 
 // ---- exclusive prefix sum ---------------------------------------------
@@ -149,13 +219,11 @@ constexpr uint32_t kScanTile = (uint32_t)(kScanThreads * kScanItems);
 static __global__ void __launch_bounds__(kScanThreads)
     k_scan_excl(const uint32_t* in, uint32_t* out, uint32_t n, const uint32_t* n_dev, uint32_t* total, Lookback lb) {
     pdl_enter();
-    constexpr int NW = kScanThreads / 32;
-    __shared__ uint32_t s_warp[NW];
-    __shared__ uint32_t s_ep, s_prefix;
+    __shared__ uint32_t s_warp[kScanThreads / 32];
+    __shared__ uint32_t s_ep, s_pair[2];
     if (threadIdx.x == 0) s_ep = lb_epoch(lb.ctl);
     if (n_dev) n = min(*n_dev, n);
     if (n == 0u && total && blockIdx.x == 0 && threadIdx.x == 0) *total = 0u;
-    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const bool in16 = (reinterpret_cast<uintptr_t>(in) & 15u) == 0u;
     const bool out16 = (reinterpret_cast<uintptr_t>(out) & 15u) == 0u;
     const uint32_t tiles = (uint32_t)(((size_t)n + kScanTile - 1) / kScanTile);
@@ -180,41 +248,9 @@ static __global__ void __launch_bounds__(kScanThreads)
         uint32_t sum = 0;
 #pragma unroll
         for (int j = 0; j < kScanItems; ++j) sum += v[j];
-        uint32_t x = sum;  // inclusive over the warp
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
-            if (lane >= (uint32_t)o) x += y;
-        }
-        if (lane == 31u) s_warp[warp] = x;
-        __syncthreads();
-        if (warp == 0) {
-            const uint32_t ep = s_ep;
-            const uint32_t wv = lane < (uint32_t)NW ? s_warp[lane] : 0u;
-            uint32_t wi = wv;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, wi, o);
-                if (lane >= (uint32_t)o) wi += y;
-            }
-            if (lane < (uint32_t)NW) s_warp[lane] = wi - wv;
-            const uint32_t agg = __shfl_sync(0xFFFFFFFFu, wi, 31);
-            unsigned long long* slot = lb.status + tile;
-            uint32_t pre = 0u;
-            if (tile == 0u) {
-                if (lane == 0u) lb_store(slot, lb_word(agg, ep, kLbInclusive));
-            } else {
-                if (lane == 0u) lb_store(slot, lb_word(agg, ep, kLbAggregate));
-                pre = lb_walk_warp(lb, tile, ep, lane);
-                if (lane == 0u) lb_store(slot, lb_word(pre + agg, ep, kLbInclusive));
-            }
-            if (lane == 0u) {
-                s_prefix = pre;
-                if (total && tile + 1u == tiles) *total = pre + agg;
-            }
-        }
-        __syncthreads();
-        uint32_t run = s_prefix + s_warp[warp] + (x - sum);
+        uint32_t end = 0;
+        uint32_t run = tile_exclusive<kScanThreads>(sum, tile, &s_ep, lb, s_warp, s_pair, &end);
+        if (total && tile + 1u == tiles && threadIdx.x == 0) *total = end;
         if (full && out16) {
             uint4* d4 = reinterpret_cast<uint4*>(out + base);
 #pragma unroll
@@ -237,7 +273,6 @@ static __global__ void __launch_bounds__(kScanThreads)
                 run += v[j];
             }
         }
-        __syncthreads();  // s_warp and s_prefix serve the next tile
     }
     if (threadIdx.x == 0) lb_done(lb.ctl);
 }
@@ -478,13 +513,17 @@ struct ScanSort {
     int scan_ctas = 1, pass_ctas32 = 1, pass_ctas64 = 1;
     uint64_t launches = 0;
 
-    static size_t status_words(uint32_t max_sort, uint32_t max_scan) {
+    // status words for sorts of max_sort keys, scans of max_scan entries and
+    // other look-back launches of up to max_tiles tiles
+    static size_t status_words(uint32_t max_sort, uint32_t max_scan, size_t max_tiles) {
         const size_t radix_tiles = ((size_t)max_sort + radix_tile<unsigned long long>() - 1) /
                                    radix_tile<unsigned long long>();
         const size_t scan_tiles = ((size_t)max_scan + kScanTile - 1) / kScanTile;
-        return std::max<size_t>(1, std::max(radix_tiles * 256u, scan_tiles));
+        return std::max<size_t>(1, std::max(std::max(radix_tiles * 256u, scan_tiles), max_tiles));
     }
-    cudaError_t init(uint32_t max_sort_n, uint32_t max_scan_n, uint32_t* err_flags, cudaStream_t s) {
+    size_t max_status = 0;  // status words allocated
+    cudaError_t init(uint32_t max_sort_n, uint32_t max_scan_n, uint32_t* err_flags, cudaStream_t s,
+                     size_t max_tiles = 0) {
         max_sort = max_sort_n;
         max_scan = max_scan_n;
         err = err_flags;
@@ -504,7 +543,8 @@ struct ScanSort {
             cudaSuccess)
             return e;
         pass_ctas64 = std::max(1, per) * sms;
-        const size_t sw = status_words(max_sort, max_scan);
+        const size_t sw = status_words(max_sort, max_scan, max_tiles);
+        max_status = sw;
         if ((e = cudaMalloc(&ctl, 8)) != cudaSuccess) return e;
         if ((e = cudaMalloc(&status, sw * 8)) != cudaSuccess) return e;
         if ((e = cudaMalloc(&hist, kRadixMaxPasses * 256 * 4)) != cudaSuccess) return e;
