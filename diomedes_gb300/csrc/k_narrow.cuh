@@ -89,6 +89,38 @@ __device__ __forceinline__ V3<R> support(const ShapeR<R>& s, V3<R> d, const A4<R
     }
 }
 
+// support() of a hull with the 32 lanes of a warp over its vertices (every
+// lane calls it with the same arguments and gets the same vertex): each
+// lane keeps its first maximum over vertices lane, lane + 32, ..., then the
+// warp keeps the largest value, ties to the lower index -- the first
+// maximum in vertex order, as the serial scan finds it (NaN products never
+// win a strict comparison there, and a NaN first product keeps vertex 0).
+template <class R>
+__device__ __forceinline__ V3<R> support_warp(const ShapeR<R>& s, V3<R> d, const A4<R>* hull, uint32_t lane) {
+    if (s.tag != DIO_SHAPE_HULL || s.hc == 0 || hull == nullptr) return support(s, d, hull);
+    const V3<R> v0 = xyz(hull[s.hf]);
+    if (isnan(dot(v0, d))) return v0;
+    R bv = R(0);
+    uint32_t bi = 0xFFFFFFFFu;
+    for (uint32_t i = lane; i < s.hc; i += 32) {
+        const R dd = dot(xyz(hull[s.hf + i]), d);
+        if (!isnan(dd) && (bi == 0xFFFFFFFFu || dd > bv)) {
+            bv = dd;
+            bi = i;
+        }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const R ov = __shfl_xor_sync(0xFFFFFFFFu, bv, off);
+        const uint32_t oi = __shfl_xor_sync(0xFFFFFFFFu, bi, off);
+        if (oi != 0xFFFFFFFFu && (bi == 0xFFFFFFFFu || ov > bv || (ov == bv && oi < bi))) {
+            bv = ov;
+            bi = oi;
+        }
+    }
+    return xyz(hull[s.hf + bi]);
+}
+
 template <class R>
 __device__ __forceinline__ void support_witness(const NB<R>& a, const NB<R>& b, V3<R> d, const A4<R>* hull,
                                                 V3<R>& point, V3<R>& wit) {
@@ -96,6 +128,17 @@ __device__ __forceinline__ void support_witness(const NB<R>& a, const NB<R>& b, 
     V3<R> ap = add(rotate(a.rot, support(a.shape, al, hull)), a.pos);
     V3<R> bl = rotate(conj(b.rot), neg(d));
     V3<R> bp = add(rotate(b.rot, support(b.shape, bl, hull)), b.pos);
+    point = sub(ap, bp);
+    wit = ap;
+}
+// the same with the warp's lanes over hull vertices (all 32 lanes call it)
+template <class R>
+__device__ __forceinline__ void support_witness_warp(const NB<R>& a, const NB<R>& b, V3<R> d, const A4<R>* hull,
+                                                     V3<R>& point, V3<R>& wit, uint32_t lane) {
+    V3<R> al = rotate(conj(a.rot), d);
+    V3<R> ap = add(rotate(a.rot, support_warp(a.shape, al, hull, lane)), a.pos);
+    V3<R> bl = rotate(conj(b.rot), neg(d));
+    V3<R> bp = add(rotate(b.rot, support_warp(b.shape, bl, hull, lane)), b.pos);
     point = sub(ap, bp);
     wit = ap;
 }
@@ -596,7 +639,7 @@ __device__ bool epa_warp(EpaSmem<R>& S, const NB<R>& a, const NB<R>& b, const A4
         A4<R> mnd = S.fnd[mi];
         uint32_t mabc = S.fabc[mi];
         V3<R> sp, sw;
-        support_witness(a, b, xyz(mnd), hull, sp, sw);
+        support_witness_warp(a, b, xyz(mnd), hull, sp, sw, lane);
         R sd = dot(xyz(mnd), sp);
         if (sd - mnd.w < R(1e-4)) {
             face_contact(S, mnd, mabc, normal, depth, pa, pb);
