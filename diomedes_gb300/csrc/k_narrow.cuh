@@ -660,6 +660,8 @@ __device__ bool epa_warp(EpaSmem<R>& S, const NB<R>& a, const NB<R>& b, const A4
         uint32_t vm[kEpaF / 32];
 #pragma unroll
         for (int c = 0; c < kEpaF / 32; ++c) {
+            vm[c] = 0u;
+            if (c * 32 >= (int)nf) continue;  // warp-uniform
             uint32_t i = c * 32 + lane;
             bool vis = false;
             if (i < nf) {

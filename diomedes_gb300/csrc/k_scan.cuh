@@ -3,8 +3,9 @@
 // launch with decoupled look-back.
 //
 // Every pipeline count -> offset step (pair counts per body, rows per slot
-// group and per body, CSR incidences per body, colour histograms) is one
-// k_scan_excl launch; every sort (LBVH Morton keys of worlds with scenes
+// group and per body, CSR incidences per body, colour histograms) is a
+// k_scan_partials + k_scan_apply pair of launches (reduce, then scan with
+// the lower tiles' sums; one k_scan_excl launch for a single tile); every sort (LBVH Morton keys of worlds with scenes
 // beyond the shared-memory trees, the dynamic-body work order, warm-start
 // row keys, incidence lists) is one k_radix_hist launch plus one
 // k_radix_pass launch per 8-bit digit.  All of them open with
@@ -277,6 +278,118 @@ static __global__ void __launch_bounds__(kScanThreads)
     if (threadIdx.x == 0) lb_done(lb.ctl);
 }
 
+// The same prefix sum as two launches without waits: k_scan_partials sums
+// each tile, k_scan_apply adds the partials of the lower tiles (one load a
+// thread) and scans its tile.  With programmatic dependent launch the
+// second launch overlaps the first's tail; neither waits on another CTA.
+__device__ __forceinline__ void scan_load_tile(const uint32_t* in, uint32_t n, size_t base, bool in16,
+                                               uint32_t v[kScanItems]) {
+    if (base + kScanItems <= n && in16) {
+        const uint4* s4 = reinterpret_cast<const uint4*>(in + base);
+#pragma unroll
+        for (int k = 0; k < kScanItems / 4; ++k) {
+            const uint4 q = s4[k];
+            v[4 * k + 0] = q.x;
+            v[4 * k + 1] = q.y;
+            v[4 * k + 2] = q.z;
+            v[4 * k + 3] = q.w;
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < kScanItems; ++j) v[j] = base + j < n ? in[base + j] : 0u;
+    }
+}
+__device__ __forceinline__ uint32_t block_sum_scan(uint32_t v, uint32_t* s_warp, uint32_t* total) {
+    // exclusive over the CTA's threads; *total = the CTA's sum
+    constexpr int NW = kScanThreads / 32;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= (uint32_t)o) x += y;
+    }
+    if (lane == 31u) s_warp[warp] = x;
+    __syncthreads();
+    uint32_t wofs = 0, all = 0;
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+        const uint32_t sw = s_warp[w];
+        wofs += (uint32_t)w < warp ? sw : 0u;
+        all += sw;
+    }
+    __syncthreads();
+    *total = all;
+    return wofs + x - v;
+}
+static __global__ void __launch_bounds__(kScanThreads)
+    k_scan_partials(const uint32_t* in, uint32_t n, const uint32_t* n_dev, uint32_t* partials) {
+    pdl_enter();
+    __shared__ uint32_t s_warp[kScanThreads / 32];
+    if (n_dev) n = min(*n_dev, n);
+    const bool in16 = (reinterpret_cast<uintptr_t>(in) & 15u) == 0u;
+    const uint32_t tiles = (uint32_t)(((size_t)n + kScanTile - 1) / kScanTile);
+    for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        uint32_t v[kScanItems];
+        scan_load_tile(in, n, (size_t)tile * kScanTile + (size_t)threadIdx.x * kScanItems, in16, v);
+        uint32_t sum = 0;
+#pragma unroll
+        for (int j = 0; j < kScanItems; ++j) sum += v[j];
+        uint32_t all = 0;
+        block_sum_scan(sum, s_warp, &all);
+        if (threadIdx.x == 0) partials[tile] = all;
+    }
+}
+static __global__ void __launch_bounds__(kScanThreads)
+    k_scan_apply(const uint32_t* in, uint32_t* out, uint32_t n, const uint32_t* n_dev, const uint32_t* partials,
+                 uint32_t* total) {
+    pdl_enter();
+    __shared__ uint32_t s_warp[kScanThreads / 32];
+    if (n_dev) n = min(*n_dev, n);
+    if (n == 0u && total && blockIdx.x == 0 && threadIdx.x == 0) *total = 0u;
+    const bool in16 = (reinterpret_cast<uintptr_t>(in) & 15u) == 0u;
+    const bool out16 = (reinterpret_cast<uintptr_t>(out) & 15u) == 0u;
+    const uint32_t tiles = (uint32_t)(((size_t)n + kScanTile - 1) / kScanTile);
+    for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const size_t base = (size_t)tile * kScanTile + (size_t)threadIdx.x * kScanItems;
+        uint32_t v[kScanItems];
+        scan_load_tile(in, n, base, in16, v);
+        // partials of the lower tiles, one or more a thread
+        uint32_t low = 0;
+        for (uint32_t t = threadIdx.x; t < tile; t += kScanThreads) low += partials[t];
+        uint32_t sum = 0;
+#pragma unroll
+        for (int j = 0; j < kScanItems; ++j) sum += v[j];
+        // one pass: the tile's own thread sums and the lower partials
+        uint32_t lowall = 0, tileall = 0;
+        block_sum_scan(low, s_warp, &lowall);
+        uint32_t run = lowall + block_sum_scan(sum, s_warp, &tileall);
+        if (total && tile + 1u == tiles && threadIdx.x == 0) *total = lowall + tileall;
+        if (base + kScanItems <= n && out16) {
+            uint4* d4 = reinterpret_cast<uint4*>(out + base);
+#pragma unroll
+            for (int k = 0; k < kScanItems / 4; ++k) {
+                uint4 q;
+                q.x = run;
+                run += v[4 * k + 0];
+                q.y = run;
+                run += v[4 * k + 1];
+                q.z = run;
+                run += v[4 * k + 2];
+                q.w = run;
+                run += v[4 * k + 3];
+                d4[k] = q;
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < kScanItems; ++j) {
+                if (base + j < n) out[base + j] = run;
+                run += v[j];
+            }
+        }
+    }
+}
+
 // ---- LSD radix sort ---------------------------------------------------
 constexpr int kRadixThreads = 256;  // one thread per digit value
 constexpr int kRadixHistThreads = 256;
@@ -504,6 +617,7 @@ struct ScanSort {
     uint32_t* hist = nullptr;   // kRadixMaxPasses * 256, zero at rest
     uint32_t* done = nullptr;   // CTAs of k_radix_hist finished, zero at rest
     uint32_t* bases = nullptr;  // kRadixMaxPasses * 256
+    uint32_t* partials = nullptr;  // per-tile sums of the two-launch scan
     void* kalt = nullptr;       // max_sort keys of 8 bytes
     uint32_t* valt = nullptr;   // max_sort values
     uint32_t* err = nullptr;    // not owned
@@ -550,6 +664,8 @@ struct ScanSort {
         if ((e = cudaMalloc(&hist, kRadixMaxPasses * 256 * 4)) != cudaSuccess) return e;
         if ((e = cudaMalloc(&done, 4)) != cudaSuccess) return e;
         if ((e = cudaMalloc(&bases, kRadixMaxPasses * 256 * 4)) != cudaSuccess) return e;
+        if ((e = cudaMalloc(&partials, (((size_t)max_scan + kScanTile - 1) / kScanTile + 1) * 4)) != cudaSuccess)
+            return e;
         if ((e = cudaMalloc(&kalt, std::max<size_t>(1, max_sort) * 8)) != cudaSuccess) return e;
         if ((e = cudaMalloc(&valt, std::max<size_t>(1, max_sort) * 4)) != cudaSuccess) return e;
         if ((e = cudaMemsetAsync(ctl, 0, 8, s)) != cudaSuccess) return e;
@@ -558,10 +674,11 @@ struct ScanSort {
         return cudaMemsetAsync(done, 0, 4, s);
     }
     void release() {
-        for (void* p : {(void*)ctl, (void*)status, (void*)hist, (void*)done, (void*)bases, kalt, (void*)valt})
+        for (void* p : {(void*)ctl, (void*)status, (void*)hist, (void*)done, (void*)bases, (void*)partials, kalt,
+                        (void*)valt})
             if (p) cudaFree(p);
         ctl = status = nullptr;
-        hist = done = bases = valt = nullptr;
+        hist = done = bases = partials = valt = nullptr;
         kalt = nullptr;
     }
     Lookback lookback() const { return Lookback{ctl, status, err}; }
@@ -572,10 +689,16 @@ struct ScanSort {
                      const uint32_t* n_dev = nullptr, uint32_t* total = nullptr) {
         if (n > max_scan) return cudaErrorInvalidValue;
         if (n == 0 && !total) return cudaSuccess;
-        ++launches;
-        const int g = (int)std::max<size_t>(
-            1, std::min<size_t>(((size_t)n + kScanTile - 1) / kScanTile, (size_t)scan_ctas));
-        return launch_k(pdl, k_scan_excl, g, kScanThreads, 0, s, in, out, n, n_dev, total, lookback());
+        const int g = (int)std::max<size_t>(1, ((size_t)n + kScanTile - 1) / kScanTile);
+        if (g == 1) {  // one tile: the single launch (its look-back has nothing to wait for)
+            ++launches;
+            return launch_k(pdl, k_scan_excl, 1, kScanThreads, 0, s, in, out, n, n_dev, total, lookback());
+        }
+        launches += 2;
+        cudaError_t e = launch_k(pdl, k_scan_partials, g, kScanThreads, 0, s, in, n, n_dev, partials);
+        if (e != cudaSuccess) return e;
+        return launch_k(true, k_scan_apply, g, kScanThreads, 0, s, in, out, n, n_dev, (const uint32_t*)partials,
+                        total);
     }
 
     // stable sort of n pairs by key bits [begin_bit, end_bit) (n <= max_sort);
