@@ -550,6 +550,7 @@ class Engine final : public EngineBase {
         // row keys (M), incidences (INC) and per-body keys (N)
         DIO_CK(ss_.init((uint32_t)std::max<size_t>(std::max<size_t>(M, N), INC),
                         (uint32_t)std::max<size_t>(CNT, (size_t)kMaxColors + 2), &ctr_->error_flags, stream_));
+        ss_.counter = &launches_;  // the scans and sorts count as the step's kernels
         // API staging (device + pinned host)
         stage_bytes_ = (size_t)N * (sizeof(DioGpuBody) + sizeof(DioBodyState) + 64 + 16) + (size_t)M * sizeof(DioContact) +
                        (size_t)J * sizeof(DioConstraint) + ((size_t)N + 1) * 4 + 2ull * M * 4 +
@@ -1438,6 +1439,7 @@ class Engine final : public EngineBase {
         uint32_t n = hi - lo;
         int g = grid_for(n, 128);
         DIO_CK(launch_k(pdl(), k_aabb<P, R>, g, 128, 0, stream_, w_, lo, hi));
+        ++launches_;
         if (cfg_.broad_phase == 0 && lo == 0) return run_lbvh(n);
         constexpr int kB = 128;
         int gd = grid_for(n, kB);
@@ -1446,7 +1448,7 @@ class Engine final : public EngineBase {
         DIO_CK(ss_.scan(counts_, offsets_, n + 1, false, stream_));
         k_dense<P, R, kB><<<gd, kB, 0, stream_>>>(w_, lo, hi, counts_, offsets_, true);
         k_pairs_total<<<1, 1, 0, stream_>>>(ctr_, offsets_ + n, w_.max_pairs);
-        launches_ += 4;
+        launches_ += 3;
         return DIO_OK;
     }
 
@@ -1572,7 +1574,7 @@ class Engine final : public EngineBase {
                         (const uint32_t*)lb_long_, (const uint32_t*)lb_long_count_, &ctr_->error_flags));
         DIO_CK(launch_k(pdl(), k_pairs_from_segments, g, 256, 0, stream_, (const uint32_t*)offsets_, n,
                         (const uint32_t*)lb_pb_, w_.pairs, w_.max_pairs));
-        launches_ += 5;
+        launches_ += 4;
         return DIO_OK;
     }
 

@@ -625,7 +625,12 @@ struct ScanSort {
     int sms = 1;
     // CTAs that the SMs hold at once: the grid limit of the look-back kernels
     int scan_ctas = 1, pass_ctas32 = 1, pass_ctas64 = 1;
-    uint64_t launches = 0;
+    uint64_t launches = 0;        // kernels launched through this object
+    uint64_t* counter = nullptr;  // optional: the owner's launch counter, advanced too
+    void counted(uint64_t k) {
+        launches += k;
+        if (counter) *counter += k;
+    }
 
     // status words for sorts of max_sort keys, scans of max_scan entries and
     // other look-back launches of up to max_tiles tiles
@@ -691,10 +696,10 @@ struct ScanSort {
         if (n == 0 && !total) return cudaSuccess;
         const int g = (int)std::max<size_t>(1, ((size_t)n + kScanTile - 1) / kScanTile);
         if (g == 1) {  // one tile: the single launch (its look-back has nothing to wait for)
-            ++launches;
+            counted(1);
             return launch_k(pdl, k_scan_excl, 1, kScanThreads, 0, s, in, out, n, n_dev, total, lookback());
         }
-        launches += 2;
+        counted(2);
         cudaError_t e = launch_k(pdl, k_scan_partials, g, kScanThreads, 0, s, in, n, n_dev, partials);
         if (e != cudaSuccess) return e;
         return launch_k(true, k_scan_apply, g, kScanThreads, 0, s, in, out, n, n_dev, (const uint32_t*)partials,
@@ -736,7 +741,7 @@ struct ScanSort {
             ks = kd;
             vs = vd;
         }
-        launches += 1 + passes;
+        counted(1 + passes);
         return cudaSuccess;
     }
 };
