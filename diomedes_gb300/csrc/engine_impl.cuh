@@ -1543,10 +1543,12 @@ class Engine final : public EngineBase {
             k_refit<R><<<g, 256, 0, stream_>>>(w_.aabb_min, w_.aabb_max, lb_leaf_, scenes_, w_.scene, n,
                                                lb_children_, lb_parent_, lb_leaf_min_, lb_leaf_max_, lb_node_min_,
                                                lb_node_max_, lb_visits_, tcap_skip, counts_);
-            k_traverse_count<R><<<gt, 128, 0, stream_>>>(lb_leaf_, scenes_, w_.scene, n, lb_children_, lb_leaf_min_,
-                                                         lb_leaf_max_, lb_node_min_, lb_node_max_, counts_,
-                                                         lb_gscratch_, w_.max_pairs, &ctr_->traverse_pairs,
-                                                         &ctr_->error_flags, tcap_skip);
+            // a walk per leaf fills the SMs from about 512 leaves per SM; fewer
+            // leaves split each walk over four threads
+            const uint32_t split = (uint64_t)n < (uint64_t)sms_ * 512u ? kWalkSplit : 1u;
+            k_traverse_count<R><<<grid_for((uint64_t)n * split, 128), 128, 0, stream_>>>(
+                lb_leaf_, scenes_, w_.scene, n, lb_children_, lb_leaf_min_, lb_leaf_max_, lb_node_min_, lb_node_max_,
+                counts_, lb_gscratch_, w_.max_pairs, &ctr_->traverse_pairs, &ctr_->error_flags, tcap_skip, split);
             launches_ += 2;
         }
         if (!world_step_) DIO_CK(cudaMemsetAsync(counts_ + n, 0, 4, stream_));  // else k_roll_counters

@@ -246,22 +246,67 @@ constexpr int kStack = 64;
 // overlapping pair is found once, by its lower position; it is counted for
 // body a = min(i, j) and appended as (a, b) to the pair scratch through a
 // warp-aggregated cursor, from which the write pass places it without
-// walking the trees again.
+// walking the trees again.  With split = kWalkSplit each leaf's walk is
+// split over 4 threads, one per subtree two levels below the root (a leaf at
+// that depth is tested directly), so a scene of a few thousand bodies still
+// fills the SMs with walks; with split = 1 a thread walks from the root.
+constexpr uint32_t kWalkSplit = 4;
 template <class R>
 __global__ void __launch_bounds__(128)
     k_traverse_count(const uint32_t* leaf_body, const SceneDesc* scenes, const uint32_t* scene_of_pos, uint32_t n,
                      const uint2* children, const A4<R>* leaf_min, const A4<R>* leaf_max, const A4<R>* node_min,
                      const A4<R>* node_max, uint32_t* counts, uint2* scratch, uint32_t scratch_cap,
-                     uint32_t* scratch_n, uint32_t* err, uint32_t skip_max) {
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+                     uint32_t* scratch_n, uint32_t* err, uint32_t skip_max, uint32_t split) {
+    const uint64_t total = (uint64_t)n * split;
+    for (uint64_t u = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; u < total;
+         u += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t p = (uint32_t)(u / split), part = (uint32_t)(u % split);
         const SceneDesc sc = scenes[scene_of_pos[p]];
         if (sc.body_hi - sc.body_lo <= skip_max) continue;  // k_scene_tree's scene
         if (sc.body_hi - sc.body_lo < 2) continue;
+        // the root (split 1), or its children, each replaced by its own
+        // children when internal
+        uint32_t items[kWalkSplit];
+        uint32_t ni = 0;
+        if (split == 1u) {
+            items[ni++] = sc.body_lo;
+        } else {
+            const uint2 rc = children[sc.body_lo];
+            const uint32_t top[2] = {rc.x, rc.y};
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                if (top[k] & kLeafFlag) {
+                    items[ni++] = top[k];
+                } else {
+                    const uint2 gc = children[top[k]];
+                    items[ni++] = gc.x;
+                    items[ni++] = gc.y;
+                }
+            }
+        }
+        if (part >= ni) continue;
         const uint32_t i = leaf_body[p];
         const A4<R> qmn = leaf_min[p], qmx = leaf_max[p];
+        auto emit = [&](uint32_t idx) {
+            const uint32_t j = leaf_body[idx];
+            const uint32_t a = min(i, j), b = max(i, j);
+            atomicAdd(&counts[a], 1u);
+            const uint32_t slot = warp_append(scratch_n);
+            if (slot < scratch_cap) scratch[slot] = make_uint2(a, b);
+        };
+        const uint32_t first = items[part];
+        const uint32_t fidx = first & ~kLeafFlag;
+        if (first & kLeafFlag) {
+            if (fidx > p && overlap(qmn, qmx, leaf_min[fidx], leaf_max[fidx])) emit(fidx);
+            continue;
+        }
+        {
+            const A4<R> fmx = node_max[fidx];
+            if (!(tag_of(fmx) > p && overlap(qmn, qmx, node_min[fidx], fmx))) continue;
+        }
         uint32_t stack[kStack];
         int sp = 0;
-        uint32_t node = sc.body_lo;  // root
+        uint32_t node = fidx;
         while (true) {
             const uint2 c = children[node];
             const uint32_t ch[2] = {c.x, c.y};
@@ -272,13 +317,7 @@ __global__ void __launch_bounds__(128)
                 const uint32_t x = ch[k];
                 const uint32_t idx = x & ~kLeafFlag;
                 if (x & kLeafFlag) {
-                    if (idx > p && overlap(qmn, qmx, leaf_min[idx], leaf_max[idx])) {
-                        const uint32_t j = leaf_body[idx];
-                        const uint32_t a = min(i, j), b = max(i, j);
-                        atomicAdd(&counts[a], 1u);
-                        const uint32_t slot = warp_append(scratch_n);
-                        if (slot < scratch_cap) scratch[slot] = make_uint2(a, b);
-                    }
+                    if (idx > p && overlap(qmn, qmx, leaf_min[idx], leaf_max[idx])) emit(idx);
                 } else {
                     const A4<R> bmx = node_max[idx];
                     if (tag_of(bmx) > p && overlap(qmn, qmx, node_min[idx], bmx)) next[push++] = idx;
