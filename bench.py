@@ -95,6 +95,8 @@ def parse():
                     help="threads per CTA of the scene-chunk solve (0: 512); default: the autotuner's choice")
     ap.add_argument("--primal-variant", type=int, default=None,
                     help="primal kernel variant of the per-phase solve; default: the autotuner's choice")
+    ap.add_argument("--colored", action="store_true",
+                    help="coloured Gauss-Seidel solver mode instead of the reference's Jacobi schedule")
     ap.add_argument("--per-phase", action="store_true",
                     help="time the per-phase solve launches as the headline (profiling the primal kernel)")
     ap.add_argument("--save-state", default=None, metavar="PATH",
@@ -447,6 +449,8 @@ def main():
         w.configure(block_size=args.block_size)
     if args.primal_variant is not None:
         w.configure(primal_variant=args.primal_variant)
+    if args.colored:
+        w.configure(solver_mode=abi.SOLVER_COLORED)
     tuned = tuned_config(w)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     # the clock sampler starts with the warm-up so that its 50 ms samples

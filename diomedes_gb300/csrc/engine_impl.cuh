@@ -588,6 +588,8 @@ class Engine final : public EngineBase {
                                     (int)chunk_build_bytes<R>()));
         DIO_CK(cudaFuncSetAttribute(k_primal_warp<P, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)primal_warp_smem<R>()));
+        DIO_CK(cudaFuncSetAttribute(k_primal_color_warp<P, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)primal_warp_smem<R>()));
         DIO_CK(cudaFuncSetAttribute(k_solve_chunks<P, R, kChunkThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)chunk_smem_bytes<P>(solve_chunk_cap<P>())));
         DIO_CK(cudaFuncSetAttribute(k_solve_chunks<P, R, kChunkThreadsWide>,
@@ -2069,7 +2071,11 @@ class Engine final : public EngineBase {
                     uint32_t c0 = color_off_h_[c], c1 = color_off_h_[c + 1];
                     if (c1 <= c0) continue;
                     cudaEvent_t e0 = span_begin();
-                    k_primal_color<P, R><<<grid_for(c1 - c0, 128), 128, 0, stream_>>>(w_, c0, c1, so);
+                    if (cfg_.primal_variant == 10)  // warp per body
+                        k_primal_color_warp<P, R><<<grid_for(c1 - c0, kPrimalWarpWarps), kPrimalWarpWarps * 32,
+                                                    primal_warp_smem<R>(), stream_>>>(w_, c0, c1, so);
+                    else
+                        k_primal_color<P, R><<<grid_for(c1 - c0, 128), 128, 0, stream_>>>(w_, c0, c1, so);
                     span_end(e0, 0);
                     ++launches_;
                 }

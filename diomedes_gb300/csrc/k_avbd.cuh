@@ -572,6 +572,73 @@ template <class R>
 __host__ __device__ constexpr size_t primal_warp_smem() {
     return (size_t)kPrimalWarpWarps * 32 * 3 * 28 * sizeof(R);
 }
+// One body's primal by the calling warp (all 32 lanes, the same i);
+// prod: the warp's [32][3][28] product staging in shared memory.
+template <class P, class R, class F>
+__device__ __forceinline__ void primal_warp_body(const DevWorld<P, R>& w, uint32_t i, const SolveParams<R>& o,
+                                                 const F& fetch, R* prod, uint32_t lane) {
+    const A4<R> inv = w.inv[i];
+    if (inv.w == R(0)) return;  // warp-uniform
+    const V3<P> sp = xyz(fetch.pos(i));
+    const Q4<P> sq = quat(fetch.rot(i));
+    const Q4<R> sqr = castq<R>(sq);
+    Block6<R> B;
+    primal_inertia(w, i, inv, sp, sqr, o, B);
+    // lane e holds entry e: h[0..20], then g[0..5]
+    R acc = R(0);
+#pragma unroll
+    for (int e = 0; e < 21; ++e)
+        if (lane == (uint32_t)e) acc = B.h[e];
+#pragma unroll
+    for (int e = 0; e < 6; ++e)
+        if (lane == (uint32_t)(21 + e)) acc = B.g[e];
+    const uint32_t j0 = w.row_off[i], j1 = w.row_off[i + 1];
+    if (j0 < j1) {
+        const V3<R> dqsl = cast3<R>(sub(sp, xyz(fetch.ipos(i))));
+        const V3<R> dqsa = ang_diff(sqr, castq<R>(quat(fetch.irot(i))));
+        const R k_alpha = R(1) - o.alpha;
+        for (uint32_t base = j0; base < j1; base += 32u) {
+            const uint32_t cnt = min(32u, j1 - base);
+            if (lane < cnt) {
+                const uint32_t j = base + lane;
+                const uint32_t r = w.row_idx[j];
+                V3<R> jl[3], ja[3];
+                R k[3], f[3];
+                primal_row_terms<P, R>(w.rs[r], w.rd[r], w.row_oth[j], fetch, sqr, dqsl, dqsa, k_alpha, jl, ja, k,
+                                       f);
+                R* mine = prod + lane * (3 * 28);
+#pragma unroll
+                for (int s = 0; s < 3; ++s) {
+                    const R J[6] = {jl[s].x, jl[s].y, jl[s].z, ja[s].x, ja[s].y, ja[s].z};
+#pragma unroll
+                    for (int a = 0; a < 6; ++a)
+#pragma unroll
+                        for (int b = 0; b <= a; ++b) mine[s * 28 + tri(a, b)] = J[a] * J[b] * k[s];
+#pragma unroll
+                    for (int a = 0; a < 6; ++a) mine[s * 28 + 21 + a] = J[a] * f[s];
+                }
+            }
+            __syncwarp();
+            if (lane < 27u)
+                for (uint32_t q = 0; q < cnt; ++q) {
+                    const R* pq = prod + q * (3 * 28) + lane;
+                    acc = acc + pq[0];
+                    acc = acc + pq[28];
+                    acc = acc + pq[56];
+                }
+            __syncwarp();
+        }
+    }
+#pragma unroll
+    for (int e = 0; e < 21; ++e) B.h[e] = __shfl_sync(0xFFFFFFFFu, acc, e);
+#pragma unroll
+    for (int e = 0; e < 6; ++e) B.g[e] = __shfl_sync(0xFFFFFFFFu, acc, 21 + e);
+    if (lane == 0u) {
+        const uint32_t k0 = w.n_joints ? w.joint_off[i] : 0u, k1 = w.n_joints ? w.joint_off[i + 1] : 0u;
+        primal_finish(w, i, k0, k1, fetch, sp, sq, sqr, B);
+    }
+}
+
 template <class P, class R>
 __global__ void __launch_bounds__(kPrimalWarpWarps * 32) k_primal_warp(DevWorld<P, R> w, int rd, int wr,
                                                                         SolveParams<R> o) {
@@ -581,69 +648,8 @@ __global__ void __launch_bounds__(kPrimalWarpWarps * 32) k_primal_warp(DevWorld<
     R* prod = reinterpret_cast<R*>(primal_warp_smem_raw) + (size_t)warp * 32 * 3 * 28;  // [32][3][28]
     const GlobalFetch<P, R> fetch{w, rd};
     const uint32_t nwarps = gridDim.x * kPrimalWarpWarps;
-    for (uint32_t t = blockIdx.x * kPrimalWarpWarps + warp; t < w.n_dyn; t += nwarps) {
-        const uint32_t i = w.dyn_list[t];
-        const A4<R> inv = w.inv[i];
-        if (inv.w == R(0)) continue;  // warp-uniform
-        const V3<P> sp = xyz(fetch.pos(i));
-        const Q4<P> sq = quat(fetch.rot(i));
-        const Q4<R> sqr = castq<R>(sq);
-        Block6<R> B;
-        primal_inertia(w, i, inv, sp, sqr, o, B);
-        // lane e holds entry e: h[0..20], then g[0..5]
-        R acc = R(0);
-#pragma unroll
-        for (int e = 0; e < 21; ++e)
-            if (lane == (uint32_t)e) acc = B.h[e];
-#pragma unroll
-        for (int e = 0; e < 6; ++e)
-            if (lane == (uint32_t)(21 + e)) acc = B.g[e];
-        const uint32_t j0 = w.row_off[i], j1 = w.row_off[i + 1];
-        if (j0 < j1) {
-            const V3<R> dqsl = cast3<R>(sub(sp, xyz(fetch.ipos(i))));
-            const V3<R> dqsa = ang_diff(sqr, castq<R>(quat(fetch.irot(i))));
-            const R k_alpha = R(1) - o.alpha;
-            for (uint32_t base = j0; base < j1; base += 32u) {
-                const uint32_t cnt = min(32u, j1 - base);
-                if (lane < cnt) {
-                    const uint32_t j = base + lane;
-                    const uint32_t r = w.row_idx[j];
-                    V3<R> jl[3], ja[3];
-                    R k[3], f[3];
-                    primal_row_terms<P, R>(w.rs[r], w.rd[r], w.row_oth[j], fetch, sqr, dqsl, dqsa, k_alpha, jl, ja,
-                                           k, f);
-                    R* mine = prod + lane * (3 * 28);
-#pragma unroll
-                    for (int s = 0; s < 3; ++s) {
-                        const R J[6] = {jl[s].x, jl[s].y, jl[s].z, ja[s].x, ja[s].y, ja[s].z};
-#pragma unroll
-                        for (int a = 0; a < 6; ++a)
-#pragma unroll
-                            for (int b = 0; b <= a; ++b) mine[s * 28 + tri(a, b)] = J[a] * J[b] * k[s];
-#pragma unroll
-                        for (int a = 0; a < 6; ++a) mine[s * 28 + 21 + a] = J[a] * f[s];
-                    }
-                }
-                __syncwarp();
-                if (lane < 27u)
-                    for (uint32_t q = 0; q < cnt; ++q) {
-                        const R* pq = prod + q * (3 * 28) + lane;
-                        acc = acc + pq[0];
-                        acc = acc + pq[28];
-                        acc = acc + pq[56];
-                    }
-                __syncwarp();
-            }
-        }
-#pragma unroll
-        for (int e = 0; e < 21; ++e) B.h[e] = __shfl_sync(0xFFFFFFFFu, acc, e);
-#pragma unroll
-        for (int e = 0; e < 6; ++e) B.g[e] = __shfl_sync(0xFFFFFFFFu, acc, 21 + e);
-        if (lane == 0u) {
-            const uint32_t k0 = w.n_joints ? w.joint_off[i] : 0u, k1 = w.n_joints ? w.joint_off[i + 1] : 0u;
-            primal_finish(w, i, k0, k1, fetch, sp, sq, sqr, B);
-        }
-    }
+    for (uint32_t t = blockIdx.x * kPrimalWarpWarps + warp; t < w.n_dyn; t += nwarps)
+        primal_warp_body(w, w.dyn_list[t], o, fetch, prod, lane);
 }
 
 // variants: 0-5 k_primal over the dynamic-body list with {threads per CTA,
@@ -718,6 +724,18 @@ __global__ void __launch_bounds__(128) k_primal_color(DevWorld<P, R> w, uint32_t
         const uint32_t k0 = w.n_joints ? w.joint_off[i] : 0u, k1 = w.n_joints ? w.joint_off[i + 1] : 0u;
         primal_body_f(w, i, k0, k1, o, InPlaceFetch<P, R>{w});
     }
+}
+
+// The same sweep with a warp per body (primal variant 10)
+template <class P, class R>
+__global__ void __launch_bounds__(kPrimalWarpWarps * 32)
+    k_primal_color_warp(DevWorld<P, R> w, uint32_t c0, uint32_t c1, SolveParams<R> o) {
+    extern __shared__ __align__(16) unsigned char primal_warp_smem_raw[];
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    R* prod = reinterpret_cast<R*>(primal_warp_smem_raw) + (size_t)warp * 32 * 3 * 28;
+    const InPlaceFetch<P, R> fetch{w};
+    for (uint32_t t = c0 + blockIdx.x * kPrimalWarpWarps + warp; t < c1; t += gridDim.x * kPrimalWarpWarps)
+        primal_warp_body(w, w.color_order[t], o, fetch, prod, lane);
 }
 
 // avbd_dual, avbd/src/lib.rs:565-663: the row's dual update from its bodies' new poses (a, and b unless the

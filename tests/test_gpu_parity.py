@@ -732,20 +732,23 @@ def _independent(colors, rows, joints, dyn):
     return True
 
 
-@pytest.mark.parametrize("batched_solver,use_graph", [(abi.SOLVE_AUTO, 1), (abi.SOLVE_AUTO, 0),
-                                                      (abi.SOLVE_PER_PHASE, 1)])
-def test_colored_world_matches_oracle(batched_solver, use_graph):
+@pytest.mark.parametrize("batched_solver,use_graph,variant", [(abi.SOLVE_AUTO, 1, 0), (abi.SOLVE_AUTO, 0, 0),
+                                                              (abi.SOLVE_PER_PHASE, 1, 0),
+                                                              (abi.SOLVE_PER_PHASE, 1, 10)])
+def test_colored_world_matches_oracle(batched_solver, use_graph, variant):
     """Coloured Gauss-Seidel mode: the colouring (Jones-Plassmann, hashed
     priorities) and the resulting states equal the oracle's bit for bit --
     colouring and per-colour sweeps inside the scene-chunk solve (one launch
-    per step, graph-captured) and with the host-driven colour loop."""
+    per step, graph-captured) and with the host-driven colour loop, with a
+    thread or a warp per body in the sweeps."""
     parts = [scenes.pyramid(levels=3), scenes.constraints_demo(), scenes.box_demo()]
     for p in parts:
         p.options = parts[0].options
     for sc in [scenes.pyramid(levels=5), scenes.constraints_demo(), scenes.box_demo(),
                scenes.cube_field(nx=6, nz=6, ny=3), scenes.pack(parts)]:
         ow = O.World(sc, solver_mode=1)
-        with _world(sc, solver_mode=1, batched_solver=batched_solver, use_graph=use_graph) as w:
+        with _world(sc, solver_mode=1, batched_solver=batched_solver, use_graph=use_graph,
+                    primal_variant=variant) as w:
             for step in range(30):
                 ow.step(sc.options, 1)
                 w.step(sc.options, 1)
