@@ -84,7 +84,7 @@ def parse():
     ap.add_argument("--error-steps", type=int, default=600,
                     help="steps of the FP32 / split / FP64 error study (capped by the workload's own step count)")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--e2e-worlds", type=int, default=4,
+    ap.add_argument("--e2e-worlds", type=int, default=8,
                     help="e2e: the batch as this many worlds on as many streams (dio_worlds_step_host)")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
