@@ -1,17 +1,18 @@
 // k_scan.cuh -- device-wide exclusive prefix sum (u32) and stable LSD radix
-// sort of (key, u32 value) pairs for u32 and u64 keys, each pass a single
-// launch with decoupled look-back.
+// sort of (key, u32 value) pairs for u32 and u64 keys.
 //
 // Every pipeline count -> offset step (pair counts per body, rows per slot
 // group and per body, CSR incidences per body, colour histograms) is a
-// k_scan_partials + k_scan_apply pair of launches (reduce, then scan with
-// the lower tiles' sums; one k_scan_excl launch for a single tile); every sort (LBVH Morton keys of worlds with scenes
-// beyond the shared-memory trees, the dynamic-body work order, warm-start
-// row keys, incidence lists) is one k_radix_hist launch plus one
-// k_radix_pass launch per 8-bit digit.  All of them open with
-// griddepcontrol.wait and so chain with programmatic dependent launch.
+// k_scan_partials + k_scan_apply pair of launches (tile sums, then each tile
+// scanned with the lower tiles' sums; one k_scan_excl launch, a single-pass
+// look-back scan, for a single tile); every sort (LBVH Morton keys of worlds
+// with scenes beyond the shared-memory trees, the dynamic-body work order,
+// warm-start row keys, incidence lists) is one k_radix_hist launch plus one
+// k_radix_pass launch per 8-bit digit, each pass with decoupled look-back.
+// All of them open with griddepcontrol.wait and so chain with programmatic
+// dependent launch.
 //
-// Look-back protocol.  The input is cut into tiles; CTA b takes tiles b,
+// Look-back protocol (k_radix_pass, k_scan_excl).  The input is cut into tiles; CTA b takes tiles b,
 // b + grid, b + 2 grid, ... in order, and the grid is at most what the SMs
 // hold at once, so the lowest unfinished tile always belongs to a running
 // CTA that is working on it: every wait ends.  A tile publishes its
