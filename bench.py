@@ -441,8 +441,15 @@ def main():
         with open(args.load_state, "rb") as f:
             w.resume(f.read())
     o = sc.options
+    # the warm-up in two parts: the tuner times its candidates from the state
+    # the first part reaches (and restores it), the last three steps capture
+    # the chosen configuration's step graphs
+    w_pre = max(0, args.warmup - 3)
+    if w_pre:
+        w.step(o, w_pre)
     if not args.no_tune:
-        w.autotune(o, trial_steps=4)  # solve launch, CTA size / launch shape, LBVH rebuild period; state restored
+        # solve launch, CTA size / launch shape, LBVH rebuild period; state restored
+        w.autotune(o, trial_steps=16)
     if args.per_phase:
         w.configure(batched_solver=abi.SOLVE_PER_PHASE)
     if args.block_size is not None:
@@ -456,7 +463,7 @@ def main():
     # the clock sampler starts with the warm-up so that its 50 ms samples
     # cover the (sub-second) timed region
     with Clocks(local) as clk:
-        w.step(o, args.warmup)
+        w.step(o, args.warmup - w_pre)
         torch.cuda.synchronize()
         w.reset_timers()
         if dist:
