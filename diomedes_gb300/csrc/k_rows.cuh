@@ -72,9 +72,13 @@ template <class P, class R>
 __global__ void k_slot_rows(DevWorld<P, R> w, const Slot<R>* slots, uint32_t per, const uint32_t* n_groups_dev,
                             uint32_t n_groups, const uint32_t* offsets, PrepParams<R> o) {
     pdl_enter();
-    uint32_t ng = n_groups_dev ? *n_groups_dev : n_groups;
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < ng && p < n_groups; p += gridDim.x * blockDim.x) {
+    const uint32_t ng = n_groups_dev ? min(*n_groups_dev, n_groups) : n_groups;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < ng; p += gridDim.x * blockDim.x) {
         uint32_t r = offsets[p];
+        // a group without valid slots (a box overlap without contact) is
+        // skipped unread; the last live group ends at the total, offsets[n_groups]
+        const uint32_t r_end = p + 1 < ng ? offsets[p + 1] : offsets[n_groups];
+        if (r_end == r) continue;
         for (uint32_t k = 0; k < per; ++k) {
             const Slot<R> s = slots[p * per + k];
             if (!s.valid) continue;
@@ -250,8 +254,10 @@ __global__ void k_cont_rows(DevWorld<P, R> w, uint32_t lo, uint32_t hi, PrepPara
     if (zero && blockIdx.x == 0 && threadIdx.x == 0) zero[hi - lo] = 0u;
     for (uint32_t i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += gridDim.x * blockDim.x) {
         if (zero) zero[i - lo] = 0u;
+        const uint32_t r = offsets[i - lo];
+        if (offsets[i - lo + 1] == r) continue;  // no rows: nothing to recompute
         const SceneDesc sc = w.scenes[w.scene[i]];
-        if (w.inv[i].w != R(0) && sc.has_container) container_rows(w, i, sc, o, true, base + offsets[i - lo]);
+        if (w.inv[i].w != R(0) && sc.has_container) container_rows(w, i, sc, o, true, base + r);
     }
 }
 
