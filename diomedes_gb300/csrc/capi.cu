@@ -500,7 +500,7 @@ int dio_autotune(DioCtx* ctx, const DioAvbdOptions* options, uint32_t trial_step
         }
     }
     // 3) LBVH rebuild period with that solve
-    const uint32_t periods[] = {1, 2, 4, 8, 16};
+    const uint32_t periods[] = {1, 2, 4, 8, 16, 32};
     DioConfig base = best_cfg;
     for (uint32_t per : periods) {
         DioConfig c = base;
