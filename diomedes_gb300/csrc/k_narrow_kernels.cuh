@@ -142,7 +142,7 @@ constexpr uint32_t kEpaWaitPolls = 1u << 20;  // rounds of the bounded waits for
 // warp's shared memory with bulk TMA copies, so the support queries of the
 // expansion read shared memory.
 template <class P, class R>
-__global__ void __launch_bounds__(32 * epa_warps<R>()) k_epa(DevWorld<P, R> w) {
+__global__ void __launch_bounds__(32 * epa_warps<R>(), 4) k_epa(DevWorld<P, R> w) {
     pdl_enter();
     constexpr int kEpaWarps = epa_warps<R>();
     __shared__ EpaSmem<R> smem[kEpaWarps];
