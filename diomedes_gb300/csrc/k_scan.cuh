@@ -111,7 +111,7 @@ template <int K = 1>
 __device__ __forceinline__ uint32_t lb_walk_warp(const Lookback& lb, uint32_t tile, uint32_t epoch, uint32_t lane) {
     const uint32_t tag = lb_tag(epoch);
     uint32_t prefix = 0;
-    int64_t p = (int64_t)tile - 1;  // nearest tile of this round
+    int64_t p = (int64_t)tile - 1;  // nearest tile of this window
     while (p >= 0) {
         uint32_t v[K], f[K];
 #pragma unroll
