@@ -105,7 +105,7 @@ __device__ __forceinline__ uint32_t lb_walk(const Lookback& lb, uint32_t tile, u
 }
 
 // The same for a one-column status array, one warp reading 32 x K lower
-// tiles per round (lane l the K tiles at distances l K + 1 .. l K + K);
+// tiles per window (lane l the K tiles at distances l K + 1 .. l K + K);
 // all 32 lanes call it and get the prefix.
 template <int K = 1>
 __device__ __forceinline__ uint32_t lb_walk_warp(const Lookback& lb, uint32_t tile, uint32_t epoch, uint32_t lane) {
